@@ -1,0 +1,311 @@
+"""ctypes binding of the C ABI in include/am_gpu.h (libamgpu.so).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, the calls raise.  Host arrays are numpy float64 / int8 / int64 in the
+reference layouts (see include/am_gpu.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libamgpu.so")
+
+AM_OK = 0
+STATUS = {0: "AM_OK", 1: "AM_ERR_INVALID_ARG", 2: "AM_ERR_SIZE_MISMATCH", 3: "AM_ERR_DOF_OUT_OF_RANGE",
+          4: "AM_ERR_NOT_CONVERGED", 5: "AM_ERR_NAN_DETECTED", 6: "AM_ERR_SINGULAR", 7: "AM_ERR_CUDA",
+          8: "AM_ERR_TIMEOUT", 9: "AM_ERR_OOM", 10: "AM_ERR_NO_DEVICE"}
+
+LAYOUT_ZFASTEST, LAYOUT_XFASTEST = 0, 1
+VARIANT_CPP, VARIANT_PY = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_JACOBI, PRECOND_LEARNED = 0, 1
+
+
+class AmError(RuntimeError):
+    """A non-OK status returned by the native library."""
+
+    def __init__(self, status: int, where: str, detail: str):
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+        super().__init__(f"{where}: {self.name}: {detail}")
+
+
+class SimpConfig(ctypes.Structure):
+    """Mirror of ``am_simp_config``."""
+
+    _fields_ = [
+        ("volume_fraction", ctypes.c_double),
+        ("penalty", ctypes.c_double),
+        ("filter_radius", ctypes.c_double),
+        ("move_limit", ctypes.c_double),
+        ("rho_min", ctypes.c_double),
+        ("E_min", ctypes.c_double),
+        ("convergence_tol", ctypes.c_double),
+        ("max_iterations", ctypes.c_int),
+        ("variant", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("preconditioner", ctypes.c_int),
+        ("cg_tol", ctypes.c_double),
+        ("cg_max_iterations", ctypes.c_int),
+        ("warm_start", ctypes.c_int),
+        ("inner_tol", ctypes.c_double),
+        ("max_outer", ctypes.c_int),
+        ("layout", ctypes.c_int),
+        ("verbose", ctypes.c_int),
+    ]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int),
+        ("outer_iterations", ctypes.c_int),
+        ("residual", ctypes.c_double),
+        ("converged", ctypes.c_int),
+        ("solve_time_s", ctypes.c_double),
+        ("max_displacement", ctypes.c_double),
+        ("min_displacement", ctypes.c_double),
+    ]
+
+
+class IterationResult(ctypes.Structure):
+    _fields_ = [
+        ("compliance", ctypes.c_double),
+        ("compliance_energy", ctypes.c_double),
+        ("volume_fraction", ctypes.c_double),
+        ("max_density_change", ctypes.c_double),
+        ("solver_iterations", ctypes.c_int),
+        ("solver_outer_iterations", ctypes.c_int),
+        ("solver_residual", ctypes.c_double),
+        ("solver_converged", ctypes.c_int),
+        ("oc_passes", ctypes.c_int),
+        ("assembly_time_s", ctypes.c_double),
+        ("solve_time_s", ctypes.c_double),
+        ("sensitivity_time_s", ctypes.c_double),
+        ("update_time_s", ctypes.c_double),
+    ]
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i8p = ctypes.POINTER(ctypes.c_int8)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "am_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "am_last_error": (ctypes.c_char_p, []),
+    "am_is_available": (ctypes.c_int, []),
+    "am_device_info": (ctypes.c_int, [_ip, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+    "am_simp_config_default": (None, [ctypes.POINTER(SimpConfig), ctypes.c_int]),
+    "am_element_stiffness": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]),
+    "am_problem_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, _i8p, ctypes.c_int,
+                                         ctypes.POINTER(_vp)]),
+    "am_problem_destroy": (ctypes.c_int, [_vp]),
+    "am_problem_set_loads": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _i64p, _i64p]),
+    "am_ku_apply": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, ctypes.c_int]),
+    "am_solve": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _dp,
+                                ctypes.POINTER(SolveStats)]),
+    "am_sensitivities": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, _dp, _dp]),
+    "am_filter": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), ctypes.c_int, _dp, _dp, _dp]),
+    "am_oc_update": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _u8p, _dp, _dp, _ip]),
+    "am_simp_run": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, _dp, _dp, _ip, _ip]),
+    "am_simp_begin": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp]),
+    "am_simp_step": (ctypes.c_int, [_vp, ctypes.POINTER(IterationResult)]),
+    "am_simp_get_density": (ctypes.c_int, [_vp, _dp]),
+    "am_launch_count": (ctypes.c_longlong, []),
+    "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "am_problem_layout": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                         ctypes.POINTER(ctypes.c_longlong), _ip]),
+}
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libamgpu.so (raises if it is absent: there is no fallback)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(path):
+            raise ImportError(f"native library not built: {path} (run am_ml_suite_gb300._build.build())")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(status: int, where: str):
+    if status != AM_OK:
+        detail = load().am_last_error()
+        raise AmError(status, where, detail.decode() if detail else "")
+
+
+def f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def ptr(a, t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def default_config(variant: int = VARIANT_CPP, **kw) -> SimpConfig:
+    cfg = SimpConfig()
+    load().am_simp_config_default(ctypes.byref(cfg), int(variant))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise AttributeError(f"unknown config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+def is_available() -> bool:
+    try:
+        return bool(load().am_is_available())
+    except (ImportError, OSError):
+        return False
+
+
+def element_stiffness(E: float = 1.0, nu: float = 0.3, h: float = 1.0) -> np.ndarray:
+    out = np.zeros((24, 24))
+    check(load().am_element_stiffness(E, nu, h, ptr(out)), "am_element_stiffness")
+    return out
+
+
+class Problem:
+    """Owns an ``am_problem`` handle (one voxel domain on the current device)."""
+
+    def __init__(self, shape, h=1.0, E0=1.0, nu=0.3, grid=None, layout=LAYOUT_ZFASTEST):
+        L = load()
+        self.shape = tuple(int(s) for s in shape)
+        nx, ny, nz = self.shape
+        self.nel = nx * ny * nz
+        self.N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+        self.layout = layout
+        g = None if grid is None else np.ascontiguousarray(grid, dtype=np.int8).ravel()
+        if g is not None and g.size != self.nel:
+            raise ValueError("grid size mismatch")
+        self._grid = g
+        h_ = _vp()
+        check(L.am_problem_create(nx, ny, nz, float(h), float(E0), float(nu), ptr(g, _i8p), int(layout),
+                                  ctypes.byref(h_)), "am_problem_create")
+        self.handle = h_
+        self.n_cases = 0
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().am_problem_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_loads(self, F_list, fixed_list):
+        F = np.ascontiguousarray(np.stack([f64(f).ravel() for f in F_list]))
+        if F.shape[1] != self.N:
+            raise ValueError("force vector size mismatch")
+        fx = [np.asarray(f, dtype=np.int64).ravel() for f in fixed_list]
+        fixed = np.ascontiguousarray(np.concatenate(fx) if fx else np.zeros(0, np.int64))
+        nf = np.array([f.size for f in fx], dtype=np.int64)
+        check(load().am_problem_set_loads(self.handle, F.shape[0], ptr(F), ptr(fixed, _i64p), ptr(nf, _i64p)),
+              "am_problem_set_loads")
+        self.n_cases = F.shape[0]
+
+    def _rho(self, rho):
+        r = f64(rho).ravel()
+        if r.size != self.nel:
+            raise ValueError("density size mismatch")
+        return r
+
+    def ku(self, cfg, rho, u, precision=PREC_FP64):
+        u = f64(u).ravel()
+        y = np.zeros(self.N)
+        check(load().am_ku_apply(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), ptr(u), ptr(y),
+                                 int(precision)), "am_ku_apply")
+        return y
+
+    def solve(self, cfg, rho, load_case=0):
+        u = np.zeros(self.N)
+        st = SolveStats()
+        check(load().am_solve(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), int(load_case), ptr(u),
+                              ctypes.byref(st)), "am_solve")
+        return u, st
+
+    def sensitivities(self, cfg, rho, u):
+        dc = np.zeros(self.nel)
+        ce = np.zeros(self.nel)
+        c = ctypes.c_double(0.0)
+        check(load().am_sensitivities(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), ptr(f64(u).ravel()),
+                                      ptr(dc), ptr(ce), ctypes.byref(c)), "am_sensitivities")
+        return dc, ce, c.value
+
+    def filter(self, cfg, which, x, rho=None):
+        out = np.zeros(self.nel)
+        r = None if rho is None else self._rho(rho)
+        check(load().am_filter(self.handle, ctypes.byref(cfg), int(which), ptr(self._rho(x)), ptr(r), ptr(out)),
+              "am_filter")
+        return out
+
+    def oc_update(self, cfg, rho, dc, design):
+        out = np.zeros(self.nel)
+        d = np.ascontiguousarray(design, dtype=np.uint8).ravel()
+        mc = ctypes.c_double(0.0)
+        passes = ctypes.c_int(0)
+        check(load().am_oc_update(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), ptr(self._rho(dc)),
+                                  ptr(d, _u8p), ptr(out), ctypes.byref(mc), ctypes.byref(passes)),
+              "am_oc_update")
+        return out, mc.value, passes.value
+
+    def simp_run(self, cfg, rho0=None):
+        m = max(int(cfg.max_iterations), 1)
+        rho = np.zeros(self.nel)
+        ch, vh, dh = np.zeros(m), np.zeros(m), np.zeros(m)
+        it, conv = ctypes.c_int(0), ctypes.c_int(0)
+        r0 = None if rho0 is None else self._rho(rho0)
+        check(load().am_simp_run(self.handle, ctypes.byref(cfg), ptr(r0), ptr(rho), ptr(ch), ptr(vh), ptr(dh),
+                                 ctypes.byref(it), ctypes.byref(conv)), "am_simp_run")
+        n = it.value
+        return dict(density=rho, compliance=ch[:n], volume=vh[:n], change=dh[:n], iterations=n,
+                    converged=bool(conv.value))
+
+    def simp_begin(self, cfg, rho0=None):
+        r0 = None if rho0 is None else self._rho(rho0)
+        check(load().am_simp_begin(self.handle, ctypes.byref(cfg), ptr(r0)), "am_simp_begin")
+
+    def simp_step(self) -> IterationResult:
+        res = IterationResult()
+        check(load().am_simp_step(self.handle, ctypes.byref(res)), "am_simp_step")
+        return res
+
+    def simp_density(self):
+        out = np.zeros(self.nel)
+        check(load().am_simp_get_density(self.handle, ptr(out)), "am_simp_get_density")
+        return out
+
+    def bench_kernel(self, which: int, reps: int = 20, flush_l2: bool = True):
+        avg, mn = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        check(load().am_bench_kernel(self.handle, int(which), int(reps), int(flush_l2), ctypes.byref(avg),
+                                     ctypes.byref(mn)), "am_bench_kernel")
+        return avg.value, mn.value
+
+    def layout(self):
+        n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
+        t = ctypes.c_int(0)
+        check(load().am_problem_layout(self.handle, ctypes.byref(n), ctypes.byref(e), ctypes.byref(cs),
+                                       ctypes.byref(t)), "am_problem_layout")
+        return dict(nodes=n.value, elements=e.value, vector_stride=cs.value, ku_tiles=t.value)
+
+
+def launch_count() -> int:
+    return int(load().am_launch_count())

@@ -1,0 +1,1085 @@
+// am_gpu.cu -- host side of the GB300 SIMP engine: problem handles, the PCG /
+// defect-correction drivers (CUDA-graph chunks of device-driven iterations), the
+// SIMP loop of both reference variants, and the extern "C" ABI of include/am_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/am_gpu.h"
+#include "kernels.cuh"
+#include "ku.cuh"
+
+using namespace amk;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+am_status fail(am_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define CK(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            return fail(e_ == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,         \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+        }                                                                                   \
+    } while (0)
+
+#define CKS(expr)                        \
+    do {                                 \
+        am_status s_ = (expr);           \
+        if (s_ != AM_OK) return s_;      \
+    } while (0)
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        if (p && n >= count) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) {
+            n = count;
+            e = cudaMemset(p, 0, std::max<size_t>(count, 1) * sizeof(T));
+        }
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct LoadCaseDev {
+    DevBuf<double> F;           // device layout [3][cs]
+    DevBuf<uint8_t> fixed_bits; // per node
+    DevBuf<long long> f_idx;    // nonzero entries of F (device index) for u.F
+    DevBuf<double> f_val;
+    int f_nnz = 0;
+    double bnorm2_all = 0.0;    // ||F||^2 over all DOFs (free-DOF norm is computed per solve)
+    DevBuf<double> x64;         // warm-start displacement (device layout)
+    bool have_x = false;
+};
+
+}  // namespace
+
+struct am_problem {
+    int nx, ny, nz;
+    double h, E0, nu;
+    Layout L;
+    long long nn_ref;   // (nx+1)(ny+1)(nz+1)
+    long long N;        // 3 nn_ref
+    int device = 0;
+    cudaStream_t st = nullptr;
+    double ke00 = 0.0;  // KE[0][0] of the unit-modulus element (all diagonal entries equal)
+    Modal<double> M64;
+    Modal<float> M32;
+    KuLaunch plan32, plan64;
+    int nblocks_vec = 0;
+
+    std::vector<int8_t> grid_host;  // internal layout, empty = all design
+    DevBuf<int8_t> grid;
+
+    std::vector<LoadCaseDev> cases;
+
+    // element arrays
+    DevBuf<double> rho, rho_new, rho_f, s64, ce, dc, dcf, estage;
+    DevBuf<float> s32;
+    DevBuf<double> oc_a64, oc_lo64, oc_hi64;  // OC terms (FP64 mode)
+    DevBuf<float2> oc_a32, oc_lo32, oc_hi32;  // OC terms (double-float, mixed mode)
+    DevBuf<uint8_t> design;
+    // node arrays
+    DevBuf<double> dinv64;
+    DevBuf<float> dinv32;
+    DevBuf<uint8_t> mask, nofix;
+    // vectors
+    DevBuf<double> r64, xw64, p64a, p64b, q64v, vstage;
+    DevBuf<float> x32, r32, p32a, p32b, q32v;
+    DevBuf<double> partial;
+    Scalars *S = nullptr;    // device
+    Scalars *Sh = nullptr;   // pinned host mirror
+    // filter taps
+    DevBuf<int4> tap_d;
+    DevBuf<double> tap_w;
+    int ntaps = 0;
+    double taps_r = -1.0;
+    int taps_variant = -1;
+    // CUDA graphs of PCG chunks
+    cudaGraphExec_t g32 = nullptr, g64 = nullptr;
+    int chunk = 32;
+
+    // SIMP state
+    bool simp_begun = false;
+    am_simp_config cfg{};
+    double n_design = 0.0;
+    int iter = 0;
+};
+
+namespace {
+
+am_status sync_scalars(am_problem *P) {
+    CK(cudaMemcpyAsync(P->Sh, P->S, sizeof(Scalars), cudaMemcpyDeviceToHost, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    return AM_OK;
+}
+
+am_status ensure_vectors(am_problem *P, bool fp64) {
+    const size_t nv = 3 * (size_t)P->L.cs;
+    CK(P->r64.alloc(nv));
+    CK(P->xw64.alloc(nv));
+    CK(P->vstage.alloc(std::max<size_t>(nv, (size_t)P->N)));
+    CK(P->dinv64.alloc(P->L.cs));
+    CK(P->dinv32.alloc(P->L.cs));
+    CK(P->mask.alloc(P->L.cs));
+    CK(P->nofix.alloc(P->L.cs));
+    if (fp64) {
+        CK(P->p64a.alloc(nv));
+        CK(P->p64b.alloc(nv));
+        CK(P->q64v.alloc(nv));
+    } else {
+        CK(P->x32.alloc(nv));
+        CK(P->r32.alloc(nv));
+        CK(P->p32a.alloc(nv));
+        CK(P->p32b.alloc(nv));
+        CK(P->q32v.alloc(nv));
+    }
+    const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), P->nblocks_vec, 152 * 16});
+    CK(P->partial.alloc(np));
+    return AM_OK;
+}
+
+am_status ensure_elements(am_problem *P) {
+    const size_t ne = (size_t)P->L.nel;
+    CK(P->rho.alloc(ne));
+    CK(P->rho_new.alloc(ne));
+    CK(P->rho_f.alloc(ne));
+    CK(P->s64.alloc(ne));
+    CK(P->s32.alloc(ne));
+    CK(P->ce.alloc(ne));
+    CK(P->dc.alloc(ne));
+    CK(P->dcf.alloc(ne));
+    CK(P->design.alloc(ne));
+    CK(P->estage.alloc(ne));
+    return AM_OK;
+}
+
+// Uploads a host element array (host layout) into dst (internal layout).
+am_status upload_elem(am_problem *P, const double *host, double *dst, int layout) {
+    CK(cudaMemcpyAsync(P->estage.p, host, sizeof(double) * P->L.nel, cudaMemcpyHostToDevice, P->st));
+    CK(elem_to_dev<double>(P->L, P->estage.p, dst, layout, P->st));
+    return AM_OK;
+}
+am_status download_elem(am_problem *P, const double *src, double *host, int layout) {
+    CK(elem_from_dev<double>(P->L, src, P->estage.p, layout, P->st));
+    CK(cudaMemcpyAsync(host, P->estage.p, sizeof(double) * P->L.nel, cudaMemcpyDeviceToHost, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    return AM_OK;
+}
+
+am_status build_taps(am_problem *P, double r, int variant) {
+    if (P->taps_r == r && P->taps_variant == variant) return AM_OK;
+    if (!(r > 0.0) || r > 6.0) return fail(AM_ERR_INVALID_ARG, "filter_radius must be in (0, 6]");
+    const int R = (int)std::ceil(r);
+    std::vector<int4> d;
+    std::vector<double> w;
+    double tot = 0.0;
+    // CPP: neighbour search order dz, dy, dx (topology_optimizer.cpp:76-101),
+    // weight max(0, r - dist) for dist <= r.  PY: full (2R+1)^3 box of r - dist
+    // for dist <= r, normalised by the sum (topopt.py:135-151).
+    for (int dz = -R; dz <= R; ++dz)
+        for (int dy = -R; dy <= R; ++dy)
+            for (int dx = -R; dx <= R; ++dx) {
+                const double dist = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
+                if (dist <= r) {
+                    const double wt = variant == 0 ? std::max(0.0, r - dist) : r - dist;
+                    if (variant == 1 && wt == 0.0) continue;
+                    d.push_back(make_int4(dx, dy, dz, 0));
+                    w.push_back(wt);
+                    tot += wt;
+                }
+            }
+    if (variant == 1) {
+        // the reference sums the kernel over the box in C order (x, y, z) before
+        // normalising; the zero entries do not change the sum
+        double t2 = 0.0;
+        for (int a = 0; a < 2 * R + 1; ++a)
+            for (int b = 0; b < 2 * R + 1; ++b)
+                for (int c = 0; c < 2 * R + 1; ++c) {
+                    const double dist =
+                        std::sqrt((double)((a - R) * (a - R) + (b - R) * (b - R) + (c - R) * (c - R)));
+                    if (dist <= r) t2 += r - dist;
+                }
+        for (auto &x : w) x /= t2;
+    }
+    (void)tot;
+    CK(P->tap_d.alloc(d.size()));
+    CK(P->tap_w.alloc(w.size()));
+    CK(cudaMemcpyAsync(P->tap_d.p, d.data(), d.size() * sizeof(int4), cudaMemcpyHostToDevice, P->st));
+    CK(cudaMemcpyAsync(P->tap_w.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    P->ntaps = (int)d.size();
+    P->taps_r = r;
+    P->taps_variant = variant;
+    return AM_OK;
+}
+
+Taps taps_of(am_problem *P) { return Taps{P->tap_d.p, P->tap_w.p, P->ntaps}; }
+
+// Element scales + Jacobi diagonal for the density currently in `rho_dev`.
+am_status setup_operator(am_problem *P, const am_simp_config &c, const double *rho_dev) {
+    const int variant = c.variant;
+    const int8_t *g = (variant == AM_VARIANT_PY && !P->grid_host.empty()) ? P->grid.p : nullptr;
+    CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st));
+    return AM_OK;
+}
+
+am_status setup_mask(am_problem *P, int lc) {
+    const uint8_t *fb = (lc >= 0 && lc < (int)P->cases.size()) ? P->cases[lc].fixed_bits.p : nullptr;
+    CK(diag_mask(P->L, P->s64.p, P->ke00, fb, P->dinv64.p, P->dinv32.p, P->mask.p, P->st));
+    return AM_OK;
+}
+
+// ||F||^2 over the free DOFs of case lc (mask already built)
+am_status free_rhs_norm(am_problem *P, int lc, double *bnorm2) {
+    const LoadCaseDev &C = P->cases[lc];
+    CK(masked_sqnorm(C.f_idx.p, C.f_val.p, C.f_nnz, P->L.cs, P->mask.p, &P->S->res_rr, P->st));
+    CKS(sync_scalars(P));
+    *bnorm2 = P->Sh->res_rr;
+    return AM_OK;
+}
+
+template <typename T>
+am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
+    cudaGraph_t g = nullptr;
+    const KuLaunch &K = std::is_same<T, float>::value ? P->plan32 : P->plan64;
+    T *x, *r, *pa, *pb, *q;
+    const T *dinv, *s;
+    Modal<T> M;
+    if constexpr (std::is_same<T, float>::value) {
+        x = P->x32.p; r = P->r32.p; pa = P->p32a.p; pb = P->p32b.p; q = P->q32v.p;
+        dinv = P->dinv32.p; s = P->s32.p; M = P->M32;
+    } else {
+        x = P->xw64.p; r = P->r64.p; pa = P->p64a.p; pb = P->p64b.p; q = P->q64v.p;
+        dinv = P->dinv64.p; s = P->s64.p; M = P->M64;
+    }
+    const long long launches_before = launch_count();
+    CK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < P->chunk; ++k) {
+        T *pin = (k & 1) ? pb : pa;
+        T *pout = (k & 1) ? pa : pb;
+        cudaError_t e1 = ku_pcg<T>(K, P->L, M, s, pin, r, dinv, P->mask.p, q, pout, P->partial.p, P->S, P->st);
+        cudaError_t e2 = pcg_update<T>(P->L, x, r, pout, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            cudaStreamEndCapture(P->st, &g);
+            if (g) cudaGraphDestroy(g);
+            return fail(AM_ERR_CUDA, std::string("PCG capture: ") +
+                                         cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        }
+    }
+    CK(cudaStreamEndCapture(P->st, &g));
+    count_launches(launches_before - launch_count());  // captured, not executed
+    cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(AM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    return AM_OK;
+}
+
+// Runs PCG chunks until S->done.  Returns the iteration count in *its.
+template <typename T>
+am_status run_pcg(am_problem *P, int *its, int *status) {
+    cudaGraphExec_t *gx = std::is_same<T, float>::value ? &P->g32 : &P->g64;
+    if (!*gx) CKS(build_pcg_graph<T>(P, gx));
+    CKS(sync_scalars(P));
+    // every chunk either advances the iteration count or ends the solve; the
+    // host bound below only catches a solver state that stops advancing
+    const long long max_chunks = (long long)P->Sh->maxit / P->chunk + 4;
+    long long chunks = 0;
+    while (!P->Sh->done) {
+        if (++chunks > max_chunks) return fail(AM_ERR_TIMEOUT, "PCG did not terminate within its iteration cap");
+        CK(cudaGraphLaunch(*gx, P->st));
+        count_launches(2LL * P->chunk);
+        CKS(sync_scalars(P));
+    }
+    *its = P->Sh->it;
+    *status = P->Sh->status;
+    return AM_OK;
+}
+
+struct SolveOut {
+    int iterations = 0, outer = 0, converged = 0;
+    double residual = 0.0, time_s = 0.0;
+};
+
+// Solves K(s) u = F_lc on the free DOFs.  Operator (s64/s32, dinv, mask) must be
+// set up.  Result in P->cases[lc].x64; ce filled when want_ce.
+am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_ce, SolveOut &o) {
+    const double t0 = now_s();
+    LoadCaseDev &C = P->cases[lc];
+    const bool fp64 = c.precision == AM_PREC_FP64;
+    CKS(ensure_vectors(P, fp64));
+    CK(C.x64.alloc(3 * (size_t)P->L.cs));
+    if (!c.warm_start || !C.have_x) CK(cudaMemsetAsync(C.x64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
+    C.have_x = true;
+    double bnorm2 = 0.0;
+    CKS(free_rhs_norm(P, lc, &bnorm2));
+    o = SolveOut{};
+    if (!(bnorm2 > 0.0)) {
+        // rhs is zero on the free DOFs: u = 0 (Eigen returns x = 0 for b = 0)
+        CK(cudaMemsetAsync(C.x64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
+        if (want_ce) CK(cudaMemsetAsync(P->ce.p, 0, sizeof(double) * P->L.nel, P->st));
+        o.converged = 1;
+        o.time_s = now_s() - t0;
+        return AM_OK;
+    }
+    const double tol = c.cg_tol;
+    const int maxit = c.cg_max_iterations > 0 ? c.cg_max_iterations : 100000;
+    if (fp64) {
+        CK(cudaMemcpyAsync(P->xw64.p, C.x64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
+        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p,
+                    P->r64.p, nullptr, P->partial.p, P->S, P->st));
+        CK(pcg_start<double>(P->L, P->r64.p, P->dinv64.p, tol, bnorm2, maxit, P->partial.p, P->S,
+                             P->nblocks_vec, P->st));
+        int its = 0, stt = 0;
+        CKS(run_pcg<double>(P, &its, &stt));
+        CK(cudaMemcpyAsync(C.x64.p, P->xw64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
+        // true FP64 residual (+ element energies) at the accepted solution
+        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
+                    want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+        CKS(sync_scalars(P));
+        o.iterations = its;
+        o.outer = 1;
+        o.residual = std::sqrt(P->Sh->res_rr / bnorm2);
+        o.converged = (stt == ST_CONVERGED) ? 1 : 0;
+        if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the PCG iteration");
+    } else {
+        const int max_outer = c.max_outer > 0 ? c.max_outer : 50;
+        const double inner = c.inner_tol > 0.0 ? c.inner_tol : 1e-4;
+        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
+                    want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+        CKS(sync_scalars(P));
+        double rel = std::sqrt(P->Sh->res_rr / bnorm2);
+        int total = 0, outer = 0;
+        bool nan = !std::isfinite(rel);
+        while (!nan && rel > tol && outer < max_outer && total < maxit) {
+            CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
+            // inner target: the requested reduction, but no further than needed
+            const double want = std::max(inner, 0.5 * tol / rel);
+            CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, want, 0.0, maxit - total, P->partial.p, P->S,
+                                P->nblocks_vec, P->st));
+            int its = 0, stt = 0;
+            CKS(run_pcg<float>(P, &its, &stt));
+            total += its;
+            ++outer;
+            if (stt == ST_NAN) {
+                nan = true;
+                break;
+            }
+            CK(dc_accumulate(P->L, C.x64.p, P->x32.p, P->S, P->nblocks_vec, P->st));
+            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p,
+                        P->r64.p, want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+            CKS(sync_scalars(P));
+            const double nrel = std::sqrt(P->Sh->res_rr / bnorm2);
+            if (!std::isfinite(nrel)) {
+                nan = true;
+                break;
+            }
+            if (its == 0 && nrel >= rel) break;  // no progress possible
+            rel = nrel;
+        }
+        if (nan) return fail(AM_ERR_NAN_DETECTED, "NaN in the mixed-precision solve");
+        o.iterations = total;
+        o.outer = outer;
+        o.residual = rel;
+        o.converged = rel <= tol ? 1 : 0;
+    }
+    o.time_s = now_s() - t0;
+    return AM_OK;
+}
+
+// OC update of P->rho (design mask P->design / `design`) with filtered
+// sensitivities `dcf` into P->rho_new; results in P->Sh after the sync.
+am_status run_oc(am_problem *P, bool f64, int variant, double move, double rho_min, double vf, double n_design,
+                 const double *rho, const double *dcf, const uint8_t *design, double *rho_new) {
+    const size_t ne = (size_t)P->L.nel;
+    if (f64) {
+        CK(P->oc_a64.alloc(ne)); CK(P->oc_lo64.alloc(ne)); CK(P->oc_hi64.alloc(ne));
+    } else {
+        CK(P->oc_a32.alloc(ne)); CK(P->oc_lo32.alloc(ne)); CK(P->oc_hi32.alloc(ne));
+    }
+    OcBuffers B{P->L.nel, P->oc_a64.p, P->oc_lo64.p, P->oc_hi64.p, P->oc_a32.p, P->oc_lo32.p, P->oc_hi32.p};
+    CK(oc_prepare(B, rho, dcf, move, f64, variant, P->S, P->st));
+    for (int k = 0; k < 100; ++k)
+        CK(oc_pass(B, design, f64, variant, rho_min, vf, n_design, P->partial.p, P->S, P->nblocks_vec, P->st));
+    CK(oc_final(B, design, f64, variant, rho_min, rho, rho_new, P->partial.p, P->S, P->nblocks_vec, P->st));
+    CKS(sync_scalars(P));
+    return AM_OK;
+}
+
+am_status check_problem(am_problem *P) {
+    if (!P) return fail(AM_ERR_INVALID_ARG, "null problem");
+    CK(cudaSetDevice(P->device));
+    return AM_OK;
+}
+
+am_status check_cfg(am_problem *P, const am_simp_config *c) {
+    if (!c) return fail(AM_ERR_INVALID_ARG, "null config");
+    if (c->variant != AM_VARIANT_CPP && c->variant != AM_VARIANT_PY)
+        return fail(AM_ERR_INVALID_ARG, "unknown variant");
+    if (c->precision != AM_PREC_FP64 && c->precision != AM_PREC_MIXED)
+        return fail(AM_ERR_INVALID_ARG, "unknown precision");
+    if (c->layout != AM_LAYOUT_ZFASTEST && c->layout != AM_LAYOUT_XFASTEST)
+        return fail(AM_ERR_INVALID_ARG, "unknown layout");
+    if (c->preconditioner != AM_PRECOND_JACOBI)
+        return fail(AM_ERR_INVALID_ARG, "preconditioner not available in this build");
+    if (!(c->volume_fraction > 0.0 && c->volume_fraction <= 1.0))
+        return fail(AM_ERR_INVALID_ARG, "volume_fraction must be in (0, 1]");
+    if (!(c->penalty >= 1.0) || !(c->move_limit > 0.0) || !(c->rho_min >= 0.0) || !(c->E_min >= 0.0))
+        return fail(AM_ERR_INVALID_ARG, "need penalty >= 1, move_limit > 0, rho_min >= 0, E_min >= 0");
+    if (!(c->cg_tol > 0.0)) return fail(AM_ERR_INVALID_ARG, "cg_tol must be > 0");
+    (void)P;
+    return AM_OK;
+}
+
+// Walsh-basis constants of the unit-modulus hex8 cube of edge h (ku.cuh).
+Modal<double> modal_constants(double E, double nu, double h) {
+    const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double mu = E / (2.0 * (1.0 + nu));
+    const double a = h / 2.0;
+    return Modal<double>{lam, mu, a / 8.0, a / 24.0, a / 72.0, a / 72.0 * (lam + 4.0 * mu)};
+}
+
+// Entry (row, col) of KE, evaluated with the same operator the kernels apply.
+double element_stiffness_host(const Modal<double> &M, int row, int col) {
+    double u[3][8] = {}, y[3][8];
+    u[col % 3][col / 3] = 1.0;
+    hex8_apply<double>(u, y, M, 1.0, nullptr);
+    return y[row % 3][row / 3];
+}
+
+}  // namespace
+
+// ============================================================================
+// extern "C" ABI
+// ============================================================================
+extern "C" {
+
+const char *am_status_string(am_status s) {
+    switch (s) {
+        case AM_OK: return "AM_OK";
+        case AM_ERR_INVALID_ARG: return "AM_ERR_INVALID_ARG";
+        case AM_ERR_SIZE_MISMATCH: return "AM_ERR_SIZE_MISMATCH";
+        case AM_ERR_DOF_OUT_OF_RANGE: return "AM_ERR_DOF_OUT_OF_RANGE";
+        case AM_ERR_NOT_CONVERGED: return "AM_ERR_NOT_CONVERGED";
+        case AM_ERR_NAN_DETECTED: return "AM_ERR_NAN_DETECTED";
+        case AM_ERR_SINGULAR: return "AM_ERR_SINGULAR";
+        case AM_ERR_CUDA: return "AM_ERR_CUDA";
+        case AM_ERR_TIMEOUT: return "AM_ERR_TIMEOUT";
+        case AM_ERR_OOM: return "AM_ERR_OOM";
+        case AM_ERR_NO_DEVICE: return "AM_ERR_NO_DEVICE";
+    }
+    return "AM_ERR_UNKNOWN";
+}
+
+const char *am_last_error(void) { return g_last_error.c_str(); }
+
+int am_is_available(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n > 0;
+}
+
+am_status am_device_info(int *sm_count, size_t *free_bytes, size_t *total_bytes) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, dev));
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return AM_OK;
+}
+
+void am_simp_config_default(am_simp_config *c, int variant) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->variant = variant;
+    c->volume_fraction = 0.25;
+    c->penalty = 3.0;
+    c->filter_radius = 2.0;
+    c->move_limit = 0.2;
+    c->rho_min = 0.01;
+    c->E_min = variant == AM_VARIANT_CPP ? 1e-6 : 1e-9;
+    c->convergence_tol = 0.01;
+    c->max_iterations = 100;
+    c->precision = AM_PREC_MIXED;
+    c->preconditioner = AM_PRECOND_JACOBI;
+    c->cg_tol = 1e-6;
+    c->cg_max_iterations = 20000;
+    c->warm_start = 1;
+    c->inner_tol = 1e-4;
+    c->max_outer = 50;
+    c->layout = AM_LAYOUT_ZFASTEST;
+    c->verbose = 0;
+}
+
+am_status am_element_stiffness(double E, double nu, double h, double *ke) {
+    if (!ke) return fail(AM_ERR_INVALID_ARG, "null output");
+    if (!(h > 0.0) || !(E > 0.0) || !(nu > -1.0 && nu < 0.5))
+        return fail(AM_ERR_INVALID_ARG, "need h > 0, E > 0, -1 < nu < 0.5");
+    const Modal<double> M = modal_constants(E, nu, h);
+    for (int col = 0; col < 24; ++col) {
+        double u[3][8] = {}, y[3][8];
+        u[col % 3][col / 3] = 1.0;
+        hex8_apply<double>(u, y, M, 1.0, nullptr);
+        for (int row = 0; row < 24; ++row) ke[row * 24 + col] = y[row % 3][row / 3];
+    }
+    return AM_OK;
+}
+
+am_status am_problem_create(int nx, int ny, int nz, double h, double E0, double nu,
+                            const int8_t *grid, int layout, am_problem **out) {
+    if (!out) return fail(AM_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    if (nx < 1 || ny < 1 || nz < 1) return fail(AM_ERR_INVALID_ARG, "grid dimensions must be >= 1");
+    if (!(h > 0.0) || !(E0 > 0.0) || !(nu > -1.0 && nu < 0.5))
+        return fail(AM_ERR_INVALID_ARG, "need h > 0, E0 > 0, -1 < nu < 0.5");
+    if (layout != AM_LAYOUT_ZFASTEST && layout != AM_LAYOUT_XFASTEST)
+        return fail(AM_ERR_INVALID_ARG, "unknown layout");
+    if (!am_is_available()) return fail(AM_ERR_NO_DEVICE, "no CUDA device");
+    am_problem *P = new am_problem();
+    P->nx = nx; P->ny = ny; P->nz = nz;
+    P->h = h; P->E0 = E0; P->nu = nu;
+    cudaGetDevice(&P->device);
+    Layout &L = P->L;
+    L.nx = nx; L.ny = ny; L.nz = nz;
+    L.sx = ((nx + 1) + 3) / 4 * 4;
+    L.sxy = (long long)L.sx * (ny + 1);
+    L.cs = (L.sxy * (nz + 1) + 63) / 64 * 64;
+    L.nel = (long long)nx * ny * nz;
+    P->nn_ref = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+    P->N = 3 * P->nn_ref;
+    // Lame parameters of the unit-modulus material; K scales linearly with E0
+    // and the element scales carry E/E0, so the operator uses E = E0.
+    P->M64 = modal_constants(E0, nu, h);
+    const Modal<double> &M = P->M64;
+    P->M32 = Modal<float>{(float)M.lam, (float)M.mu, (float)M.c1, (float)M.c2, (float)M.c3, (float)M.c7};
+    // every diagonal entry of the cube KE equals KE[0][0]
+    P->ke00 = element_stiffness_host(M, 0, 0);
+    P->plan32 = ku_plan(L, false, 0);
+    P->plan64 = ku_plan(L, true, 0);
+    P->nblocks_vec = (int)std::max<long long>(1, std::min<long long>((3 * L.cs + 255) / 256, 152LL * 8));
+    cudaError_t e = ku_init_attributes();
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&P->S, sizeof(Scalars));
+    if (e == cudaSuccess) e = cudaMemset(P->S, 0, sizeof(Scalars));
+    if (e == cudaSuccess) e = cudaMallocHost(&P->Sh, sizeof(Scalars));
+    if (e != cudaSuccess) {
+        am_problem_destroy(P);
+        return fail(e == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,
+                    std::string("problem create: ") + cudaGetErrorString(e));
+    }
+    if (grid) {
+        std::vector<int8_t> g((size_t)L.nel);
+        for (long long ez = 0; ez < nz; ++ez)
+            for (long long ey = 0; ey < ny; ++ey)
+                for (long long ex = 0; ex < nx; ++ex) {
+                    const long long hidx = layout == AM_LAYOUT_ZFASTEST ? (ex * ny + ey) * nz + ez
+                                                                        : (ez * ny + ey) * nx + ex;
+                    const int8_t v = grid[hidx];
+                    if (v < -1 || v > 1) {
+                        am_problem_destroy(P);
+                        return fail(AM_ERR_INVALID_ARG, "grid values must be -1, 0 or 1");
+                    }
+                    g[(size_t)((ez * ny + ey) * nx + ex)] = v;
+                }
+        P->grid_host = g;
+        e = P->grid.alloc(g.size());
+        if (e == cudaSuccess) e = cudaMemcpy(P->grid.p, g.data(), g.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            am_problem_destroy(P);
+            return fail(AM_ERR_CUDA, std::string("grid upload: ") + cudaGetErrorString(e));
+        }
+    }
+    *out = P;
+    return AM_OK;
+}
+
+am_status am_problem_destroy(am_problem *P) {
+    if (!P) return AM_OK;
+    cudaSetDevice(P->device);
+    if (P->st) cudaStreamSynchronize(P->st);
+    if (P->g32) cudaGraphExecDestroy(P->g32);
+    if (P->g64) cudaGraphExecDestroy(P->g64);
+    for (auto &c : P->cases) {
+        c.F.release(); c.fixed_bits.release(); c.f_idx.release(); c.f_val.release(); c.x64.release();
+    }
+    DevBuf<double> *d64[] = {&P->rho, &P->rho_new, &P->rho_f, &P->s64, &P->ce, &P->dc, &P->dcf, &P->oc_a64, &P->oc_lo64, &P->oc_hi64,
+                             &P->estage, &P->dinv64, &P->r64, &P->xw64, &P->p64a, &P->p64b, &P->q64v,
+                             &P->vstage, &P->partial, &P->tap_w};
+    for (auto *b : d64) b->release();
+    P->oc_a32.release(); P->oc_lo32.release(); P->oc_hi32.release();
+    DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->r32, &P->p32a, &P->p32b, &P->q32v};
+    for (auto *b : d32) b->release();
+    P->design.release(); P->mask.release(); P->nofix.release(); P->grid.release(); P->tap_d.release();
+    if (P->S) cudaFree(P->S);
+    if (P->Sh) cudaFreeHost(P->Sh);
+    if (P->st) cudaStreamDestroy(P->st);
+    delete P;
+    return AM_OK;
+}
+
+am_status am_problem_set_loads(am_problem *P, int n_cases, const double *F, const int64_t *fixed,
+                               const int64_t *n_fixed) {
+    CKS(check_problem(P));
+    if (n_cases < 1 || !F) return fail(AM_ERR_INVALID_ARG, "need n_cases >= 1 and F");
+    if (!n_fixed) return fail(AM_ERR_INVALID_ARG, "need n_fixed");
+    for (auto &c : P->cases) {
+        c.F.release(); c.fixed_bits.release(); c.f_idx.release(); c.f_val.release(); c.x64.release();
+    }
+    P->cases.clear();
+    P->cases.resize(n_cases);
+    const long long N = P->N;
+    const Layout &L = P->L;
+    long long off = 0;
+    std::vector<uint8_t> bits((size_t)L.cs);
+    CK(P->vstage.alloc(std::max<size_t>(3 * (size_t)L.cs, (size_t)N)));
+    for (int c = 0; c < n_cases; ++c) {
+        LoadCaseDev &C = P->cases[c];
+        std::fill(bits.begin(), bits.end(), 0);
+        for (long long t = 0; t < n_fixed[c]; ++t) {
+            const long long d = fixed[off + t];
+            if (d < 0 || d >= N) return fail(AM_ERR_DOF_OUT_OF_RANGE, "Fixed DOF index out of range: " + std::to_string(d));
+            const long long n = d / 3;
+            const int comp = (int)(d % 3);
+            const int k = (int)(n % (P->nz + 1));
+            const long long tt = n / (P->nz + 1);
+            const int j = (int)(tt % (P->ny + 1)), i = (int)(tt / (P->ny + 1));
+            bits[(size_t)node_index(L, i, j, k)] |= (uint8_t)(1u << comp);
+        }
+        off += n_fixed[c];
+        const double *Fc = F + (size_t)c * N;
+        std::vector<long long> idx;
+        std::vector<double> val;
+        double b2 = 0.0;
+        for (long long d = 0; d < N; ++d) {
+            const double v = Fc[d];
+            if (!std::isfinite(v)) return fail(AM_ERR_NAN_DETECTED, "non-finite load entry");
+            if (v != 0.0) {
+                const long long n = d / 3;
+                const int comp = (int)(d % 3);
+                const int k = (int)(n % (P->nz + 1));
+                const long long tt = n / (P->nz + 1);
+                const int j = (int)(tt % (P->ny + 1)), i = (int)(tt / (P->ny + 1));
+                idx.push_back(comp * L.cs + node_index(L, i, j, k));
+                val.push_back(v);
+                b2 += v * v;
+            }
+        }
+        C.bnorm2_all = b2;
+        CK(C.F.alloc(3 * (size_t)L.cs));
+        CK(C.fixed_bits.alloc((size_t)L.cs));
+        CK(cudaMemcpyAsync(C.fixed_bits.p, bits.data(), bits.size(), cudaMemcpyHostToDevice, P->st));
+        CK(cudaMemcpyAsync(P->vstage.p, Fc, sizeof(double) * N, cudaMemcpyHostToDevice, P->st));
+        CK(dof_to_dev(L, P->vstage.p, C.F.p, P->st));
+        C.f_nnz = (int)idx.size();
+        CK(C.f_idx.alloc(std::max<size_t>(idx.size(), 1)));
+        CK(C.f_val.alloc(std::max<size_t>(val.size(), 1)));
+        if (!idx.empty()) {
+            CK(cudaMemcpyAsync(C.f_idx.p, idx.data(), idx.size() * sizeof(long long), cudaMemcpyHostToDevice, P->st));
+            CK(cudaMemcpyAsync(C.f_val.p, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice, P->st));
+        }
+        CK(cudaStreamSynchronize(P->st));
+    }
+    return AM_OK;
+}
+
+am_status am_ku_apply(am_problem *P, const am_simp_config *cfg, const double *rho, const double *u,
+                      double *y, int precision) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!rho || !u || !y) return fail(AM_ERR_INVALID_ARG, "null array");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, precision == AM_PREC_FP64));
+    CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    CKS(setup_operator(P, *cfg, P->rho.p));
+    CK(cudaMemcpyAsync(P->vstage.p, u, sizeof(double) * P->N, cudaMemcpyHostToDevice, P->st));
+    if (precision == AM_PREC_FP64) {
+        CK(dof_to_dev(P->L, P->vstage.p, P->xw64.p, P->st));
+        CK(ku_plain<double>(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, P->r64.p, P->st));
+        CK(dev_to_dof(P->L, P->r64.p, P->vstage.p, P->st));
+    } else {
+        CK(dof_to_dev_t<float>(P->L, P->vstage.p, P->x32.p, P->st));
+        CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->x32.p, P->r32.p, P->st));
+        CK(dev_to_dof_t<float>(P->L, P->r32.p, P->vstage.p, P->st));
+    }
+    CK(cudaMemcpyAsync(y, P->vstage.p, sizeof(double) * P->N, cudaMemcpyDeviceToHost, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    return AM_OK;
+}
+
+am_status am_solve(am_problem *P, const am_simp_config *cfg, const double *rho, int load_case,
+                   double *u_out, am_solve_stats *stats) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!rho) return fail(AM_ERR_INVALID_ARG, "null density");
+    if (load_case < 0 || load_case >= (int)P->cases.size())
+        return fail(AM_ERR_INVALID_ARG, "load case not set");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, cfg->precision == AM_PREC_FP64));
+    CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    CKS(setup_operator(P, *cfg, P->rho.p));
+    CKS(setup_mask(P, load_case));
+    SolveOut o;
+    CKS(solve_case(P, *cfg, load_case, false, o));
+    if (u_out) {
+        CK(dev_to_dof(P->L, P->cases[load_case].x64.p, P->vstage.p, P->st));
+        CK(cudaMemcpyAsync(u_out, P->vstage.p, sizeof(double) * P->N, cudaMemcpyDeviceToHost, P->st));
+        CK(cudaStreamSynchronize(P->st));
+    }
+    if (stats) {
+        stats->iterations = o.iterations;
+        stats->outer_iterations = o.outer;
+        stats->residual = o.residual;
+        stats->converged = o.converged;
+        stats->solve_time_s = o.time_s;
+        stats->max_displacement = 0.0;
+        stats->min_displacement = 0.0;
+        if (u_out) {
+            double mx = -INFINITY, mn = INFINITY;
+            for (long long i = 0; i < P->N; ++i) {
+                mx = std::max(mx, u_out[i]);
+                mn = std::min(mn, u_out[i]);
+            }
+            stats->max_displacement = mx;
+            stats->min_displacement = mn;
+        }
+    }
+    return AM_OK;
+}
+
+am_status am_sensitivities(am_problem *P, const am_simp_config *cfg, const double *rho,
+                           const double *u, double *dc, double *ce, double *compliance) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!rho || !u) return fail(AM_ERR_INVALID_ARG, "null array");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, true));
+    CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    CKS(setup_operator(P, *cfg, P->rho.p));
+    CKS(setup_mask(P, -1));
+    CK(cudaMemcpyAsync(P->vstage.p, u, sizeof(double) * P->N, cudaMemcpyHostToDevice, P->st));
+    CK(dof_to_dev(P->L, P->vstage.p, P->xw64.p, P->st));
+    // r64 <- 0 - K u (discarded); ce filled
+    CK(cudaMemsetAsync(P->p64a.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
+    CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, P->p64a.p, P->dinv64.p, P->mask.p, P->r64.p,
+                P->ce.p, P->partial.p, P->S, P->st));
+    // design mask: CPP all elements; PY grid == 0
+    if (cfg->variant == AM_VARIANT_PY) {
+        std::vector<uint8_t> dm((size_t)P->L.nel, 1);
+        if (!P->grid_host.empty())
+            for (size_t e = 0; e < dm.size(); ++e) dm[e] = P->grid_host[e] == 0;
+        CK(cudaMemcpyAsync(P->design.p, dm.data(), dm.size(), cudaMemcpyHostToDevice, P->st));
+        CK(cudaStreamSynchronize(P->st));
+    }
+    CK(sensitivities(P->L, P->rho.p, P->ce.p, P->s64.p, P->design.p, cfg->variant, cfg->penalty, P->dc.p, 0,
+                     P->partial.p, P->S, P->st));
+    CKS(sync_scalars(P));
+    if (compliance) *compliance = P->Sh->comp_energy;
+    if (dc) CKS(download_elem(P, P->dc.p, dc, cfg->layout));
+    if (ce) CKS(download_elem(P, P->ce.p, ce, cfg->layout));
+    return AM_OK;
+}
+
+am_status am_filter(am_problem *P, const am_simp_config *cfg, int which, const double *x,
+                    const double *rho, double *out) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!x || !out || (which == 0 && !rho)) return fail(AM_ERR_INVALID_ARG, "null array");
+    if (which != 0 && which != 1) return fail(AM_ERR_INVALID_ARG, "which must be 0 or 1");
+    CKS(ensure_elements(P));
+    CKS(build_taps(P, cfg->filter_radius, which));
+    CKS(upload_elem(P, x, P->dc.p, cfg->layout));
+    if (which == 0) CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    const bool f64 = cfg->precision == AM_PREC_FP64;
+    if (which == 0) {
+        CK(f64 ? filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st)
+               : filter_cpp<float>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));
+    } else {
+        CK(f64 ? filter_py<double>(P->L, taps_of(P), P->dc.p, nullptr, P->dcf.p, 0, 0.0, P->st)
+               : filter_py<float>(P->L, taps_of(P), P->dc.p, nullptr, P->dcf.p, 0, 0.0, P->st));
+    }
+    CKS(download_elem(P, P->dcf.p, out, cfg->layout));
+    return AM_OK;
+}
+
+am_status am_oc_update(am_problem *P, const am_simp_config *cfg, const double *rho, const double *dc,
+                       const uint8_t *design, double *rho_new, double *max_change, int *passes) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!rho || !dc || !design || !rho_new) return fail(AM_ERR_INVALID_ARG, "null array");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, true));
+    CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    CKS(upload_elem(P, dc, P->dcf.p, cfg->layout));
+    CK(cudaMemcpyAsync(P->estage.p, design, (size_t)P->L.nel, cudaMemcpyHostToDevice, P->st));
+    CK(elem_to_dev<uint8_t>(P->L, (const uint8_t *)P->estage.p, P->design.p, cfg->layout, P->st));
+    long long nd = 0;
+    for (long long e = 0; e < P->L.nel; ++e) nd += design[e] ? 1 : 0;
+    double n_design = (double)nd;
+    if (cfg->variant == AM_VARIANT_CPP && nd == 0) n_design = (double)P->L.nel;
+    const bool f64 = cfg->precision == AM_PREC_FP64;
+    CKS(run_oc(P, f64, cfg->variant, cfg->move_limit, cfg->rho_min, cfg->volume_fraction, n_design, P->rho.p,
+               P->dcf.p, P->design.p, P->rho_new.p));
+    if (max_change) *max_change = P->Sh->oc_change;
+    if (passes) *passes = P->Sh->oc_pass;
+    CKS(download_elem(P, P->rho_new.p, rho_new, cfg->layout));
+    return AM_OK;
+}
+
+am_status am_simp_begin(am_problem *P, const am_simp_config *cfg, const double *rho0) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (P->cases.empty()) return fail(AM_ERR_INVALID_ARG, "loads not set");
+    if (cfg->max_iterations < 0) return fail(AM_ERR_INVALID_ARG, "max_iterations < 0");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, cfg->precision == AM_PREC_FP64));
+    P->cfg = *cfg;
+    const long long nel = P->L.nel;
+    std::vector<double> r0((size_t)nel);
+    if (rho0) {
+        CKS(upload_elem(P, rho0, P->rho.p, cfg->layout));
+        CK(cudaMemcpyAsync(r0.data(), P->rho.p, sizeof(double) * nel, cudaMemcpyDeviceToHost, P->st));
+        CK(cudaStreamSynchronize(P->st));
+    } else {
+        for (long long e = 0; e < nel; ++e) {
+            const int g = P->grid_host.empty() ? 0 : P->grid_host[(size_t)e];
+            // PY: uniform volume_fraction (topopt.py:124); CPP: am_topopt.cpp:562-572
+            if (cfg->variant == AM_VARIANT_PY || g == 0) r0[(size_t)e] = cfg->volume_fraction;
+            else r0[(size_t)e] = g == 1 ? 1.0 : cfg->rho_min;
+        }
+        CK(cudaMemcpyAsync(P->rho.p, r0.data(), sizeof(double) * nel, cudaMemcpyHostToDevice, P->st));
+    }
+    // design mask: CPP from the initial density (topology_optimizer.cpp:419-428),
+    // PY grid == 0 (topopt.py:127)
+    std::vector<uint8_t> dm((size_t)nel);
+    long long nd = 0;
+    for (long long e = 0; e < nel; ++e) {
+        bool d;
+        if (cfg->variant == AM_VARIANT_CPP) d = r0[(size_t)e] > cfg->rho_min + 1e-6 && r0[(size_t)e] < 0.99;
+        else d = P->grid_host.empty() ? true : P->grid_host[(size_t)e] == 0;
+        dm[(size_t)e] = d;
+        nd += d;
+    }
+    P->n_design = (cfg->variant == AM_VARIANT_CPP && nd == 0) ? (double)nel : (double)nd;
+    CK(cudaMemcpyAsync(P->design.p, dm.data(), dm.size(), cudaMemcpyHostToDevice, P->st));
+    CKS(build_taps(P, cfg->filter_radius, cfg->variant == AM_VARIANT_CPP ? 0 : 1));
+    for (auto &c : P->cases) c.have_x = false;
+    CK(cudaStreamSynchronize(P->st));
+    P->simp_begun = true;
+    P->iter = 0;
+    return AM_OK;
+}
+
+am_status am_simp_step(am_problem *P, am_iteration_result *res) {
+    CKS(check_problem(P));
+    if (!P->simp_begun) return fail(AM_ERR_INVALID_ARG, "am_simp_begin not called");
+    const am_simp_config &c = P->cfg;
+    const bool f64 = c.precision == AM_PREC_FP64;
+    am_iteration_result R{};
+    double t0 = now_s();
+    const double *rho_asm = P->rho.p;
+    if (c.variant == AM_VARIANT_PY) {
+        // density pre-filter + clip (topopt.py:302-303)
+        CK(f64 ? filter_py<double>(P->L, taps_of(P), P->rho.p, nullptr, P->rho_f.p, 1, c.rho_min, P->st)
+               : filter_py<float>(P->L, taps_of(P), P->rho.p, nullptr, P->rho_f.p, 1, c.rho_min, P->st));
+        rho_asm = P->rho_f.p;
+    }
+    CKS(setup_operator(P, c, rho_asm));
+    CK(cudaStreamSynchronize(P->st));
+    double t1 = now_s();
+    R.assembly_time_s = t1 - t0;
+    double comp = 0.0;
+    int total_its = 0, total_outer = 0, conv = 1;
+    double worst_res = 0.0;
+    double t_solve = 0.0, t_sens = 0.0;
+    for (int lc = 0; lc < (int)P->cases.size(); ++lc) {
+        if (c.variant == AM_VARIANT_CPP && lc > 0) break;  // the C++ loop takes one F
+        double ts = now_s();
+        CKS(setup_mask(P, lc));
+        SolveOut o;
+        CKS(solve_case(P, c, lc, true, o));
+        total_its += o.iterations;
+        total_outer += o.outer;
+        conv = conv && o.converged;
+        worst_res = std::max(worst_res, o.residual);
+        double te = now_s();
+        t_solve += te - ts;
+        CK(sensitivities(P->L, rho_asm, P->ce.p, P->s64.p, P->design.p, c.variant, c.penalty, P->dc.p,
+                         lc > 0 ? 1 : 0, P->partial.p, P->S, P->st));
+        CK(sparse_dot(P->cases[lc].f_idx.p, P->cases[lc].f_val.p, P->cases[lc].f_nnz, P->cases[lc].x64.p,
+                      &P->S->comp_fu, P->st));
+        CKS(sync_scalars(P));
+        if (c.variant == AM_VARIANT_CPP) comp = P->Sh->comp_fu;
+        t_sens += now_s() - te;
+    }
+    if (c.variant == AM_VARIANT_PY) comp = P->Sh->comp_energy;
+    R.compliance = comp;
+    R.compliance_energy = P->Sh->comp_energy;
+    R.solve_time_s = t_solve;
+    R.sensitivity_time_s = t_sens;
+    R.solver_iterations = total_its;
+    R.solver_outer_iterations = total_outer;
+    R.solver_residual = worst_res;
+    R.solver_converged = conv;
+    double tu = now_s();
+    // filter (topology_optimizer.cpp:351 / topopt.py:363)
+    if (c.variant == AM_VARIANT_CPP) {
+        CK(f64 ? filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st)
+               : filter_cpp<float>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));
+    } else {
+        CK(f64 ? filter_py<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, 2, 0.0, P->st)
+               : filter_py<float>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, 2, 0.0, P->st));
+    }
+    // OC update
+    CKS(run_oc(P, f64, c.variant, c.move_limit, c.rho_min, c.volume_fraction, P->n_design, P->rho.p, P->dcf.p,
+               P->design.p, P->rho_new.p));
+    std::swap(P->rho.p, P->rho_new.p);
+    std::swap(P->rho.n, P->rho_new.n);
+    R.update_time_s = now_s() - tu;
+    R.max_density_change = P->Sh->oc_change;
+    R.volume_fraction = P->Sh->oc_volume;
+    R.oc_passes = P->Sh->oc_pass;
+    ++P->iter;
+    if (res) *res = R;
+    return AM_OK;
+}
+
+long long am_launch_count(void) { return launch_count(); }
+
+am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, double *avg_ms, double *min_ms) {
+    CKS(check_problem(P));
+    if (!P->simp_begun || P->iter < 1) return fail(AM_ERR_INVALID_ARG, "run am_simp_step at least once first");
+    if (reps < 1) return fail(AM_ERR_INVALID_ARG, "reps must be >= 1");
+    CKS(ensure_vectors(P, false));
+    CKS(sync_scalars(P));
+    const Scalars saved = *P->Sh;
+    Scalars run = saved;
+    run.done = 0;
+    run.beta = 0.5;
+    run.alpha = 1e-3;
+    run.thr = 0.0;
+    run.maxit = 1 << 30;
+    run.it = 0;
+    CK(cudaMemcpyAsync(P->S, &run, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
+    DevBuf<uint8_t> flush;
+    const size_t flush_bytes = 512ull << 20;
+    if (flush_l2) CK(flush.alloc(flush_bytes));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double tot = 0.0, mn = 1e30;
+    for (int k = 0; k < reps; ++k) {
+        if (flush_l2) CK(cudaMemsetAsync(flush.p, k & 0xff, flush_bytes, P->st));
+        CK(cudaMemcpyAsync(&P->S->done, &run.done, sizeof(int), cudaMemcpyHostToDevice, P->st));
+        CK(cudaEventRecord(e0, P->st));
+        switch (which) {
+            case 0:
+                CK(ku_pcg<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->r32.p, P->dinv32.p, P->mask.p,
+                                 P->q32v.p, P->p32b.p, P->partial.p, P->S, P->st));
+                break;
+            case 1:
+                CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->cases[0].x64.p, P->cases[0].F.p, P->dinv64.p,
+                            P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
+                break;
+            case 2:
+                CK(pcg_update<float>(P->L, P->x32.p, P->r32.p, P->p32b.p, P->q32v.p, P->dinv32.p, P->partial.p,
+                                     P->S, P->nblocks_vec, P->st));
+                break;
+            case 3:
+                CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->q32v.p, P->st));
+                break;
+            default:
+                return fail(AM_ERR_INVALID_ARG, "unknown kernel id");
+        }
+        CK(cudaEventRecord(e1, P->st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        tot += ms;
+        mn = std::min(mn, (double)ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    flush.release();
+    CK(cudaMemcpyAsync(P->S, &saved, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    if (avg_ms) *avg_ms = tot / reps;
+    if (min_ms) *min_ms = mn;
+    return AM_OK;
+}
+
+am_status am_problem_layout(am_problem *P, long long *nodes, long long *elements, long long *vector_stride,
+                            int *ku_tiles) {
+    CKS(check_problem(P));
+    if (nodes) *nodes = P->nn_ref;
+    if (elements) *elements = P->L.nel;
+    if (vector_stride) *vector_stride = P->L.cs;
+    if (ku_tiles) *ku_tiles = P->plan32.ntiles();
+    return AM_OK;
+}
+
+am_status am_simp_get_density(am_problem *P, double *rho_out) {
+    CKS(check_problem(P));
+    if (!P->simp_begun) return fail(AM_ERR_INVALID_ARG, "am_simp_begin not called");
+    if (!rho_out) return fail(AM_ERR_INVALID_ARG, "null output");
+    return download_elem(P, P->rho.p, rho_out, P->cfg.layout);
+}
+
+am_status am_simp_run(am_problem *P, const am_simp_config *cfg, const double *rho0, double *rho_out,
+                      double *compliance_hist, double *volume_hist, double *change_hist,
+                      int *iterations, int *converged) {
+    CKS(am_simp_begin(P, cfg, rho0));
+    int it = 0;
+    int conv = 0;
+    for (; it < cfg->max_iterations; ++it) {
+        am_iteration_result R;
+        CKS(am_simp_step(P, &R));
+        if (compliance_hist) compliance_hist[it] = R.compliance;
+        if (volume_hist) volume_hist[it] = R.volume_fraction;
+        if (change_hist) change_hist[it] = R.max_density_change;
+        if (cfg->verbose)
+            std::printf("%6d %14.4e %10.3f %12.2e %10d\n", it, R.compliance, R.volume_fraction,
+                        R.max_density_change, R.solver_iterations);
+        if (R.max_density_change < cfg->convergence_tol) {
+            conv = 1;
+            ++it;
+            break;
+        }
+    }
+    if (iterations) *iterations = it;
+    if (converged) *converged = conv;
+    if (rho_out) CKS(am_simp_get_density(P, rho_out));
+    return AM_OK;
+}
+
+}  // extern "C"

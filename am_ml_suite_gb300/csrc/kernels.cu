@@ -1,0 +1,867 @@
+// kernels.cu -- the kernels of the GB300 SIMP engine other than the tiled K*u
+// body (ku.cuh), plus the launchers declared in kernels.cuh.
+#include <algorithm>
+#include <atomic>
+
+#include "kernels.cuh"
+#include "ku.cuh"
+
+namespace amk {
+
+static inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Host-side count of kernel launches issued by this library (graph launches add
+// the kernel nodes they contain, see count_launches).
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(); }
+void count_launches(long long n) { g_launches += n; }
+static inline cudaError_t counted(cudaError_t e) {
+    if (e == cudaSuccess) ++g_launches;
+    return e;
+}
+
+// ============================================================================
+// K*u launch plans and launchers
+// ============================================================================
+KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint) {
+    KuLaunch K;
+    K.tx = 32;
+    K.ty = fp64 ? 4 : 8;
+    const long long cols = (long long)div_up(L.nx + 1, K.tx) * div_up(L.ny + 1, K.ty);
+    int tz = tz_hint;
+    if (tz <= 0) {
+        // enough tiles for ~4 waves of resident CTAs, but chunks of >= 8 planes
+        const long long want = 152LL * 8;
+        tz = (int)std::max<long long>(8, (long long)(L.nz + 1) * cols / want);
+        tz = std::min(tz, L.nz + 1);
+    }
+    K.tz = tz;
+    K.tiles_x = div_up(L.nx + 1, K.tx);
+    K.tiles_y = div_up(L.ny + 1, K.ty);
+    K.tiles_z = div_up(L.nz + 1, K.tz);
+    return K;
+}
+
+template <typename T, int TX, int TY, int MODE>
+static cudaError_t set_ku_attr() {
+    using Sh = KuShape<TX, TY>;
+    return cudaFuncSetAttribute(ku_tile_kernel<T, TX, TY, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Sh::template smem_bytes<T>());
+}
+
+cudaError_t ku_init_attributes() {
+    cudaError_t e;
+#define AMK_ATTR(T, X, Y, M) \
+    if ((e = set_ku_attr<T, X, Y, M>()) != cudaSuccess) return e;
+    AMK_ATTR(float, 32, 8, KU_PLAIN)
+    AMK_ATTR(float, 32, 8, KU_PCG)
+    AMK_ATTR(float, 32, 4, KU_PLAIN)
+    AMK_ATTR(float, 32, 4, KU_PCG)
+    AMK_ATTR(double, 32, 8, KU_PLAIN)
+    AMK_ATTR(double, 32, 8, KU_PCG)
+    AMK_ATTR(double, 32, 8, KU_RESID)
+    AMK_ATTR(double, 32, 4, KU_PLAIN)
+    AMK_ATTR(double, 32, 4, KU_PCG)
+    AMK_ATTR(double, 32, 4, KU_RESID)
+#undef AMK_ATTR
+    return cudaSuccess;
+}
+
+template <typename T, int TX, int TY, int MODE>
+static cudaError_t launch_ku(const KuLaunch &K, KuArgs<T> &a, cudaStream_t st) {
+    using Sh = KuShape<TX, TY>;
+    const size_t smem = Sh::template smem_bytes<T>();
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tiles_z = K.tiles_z;
+    a.tz = K.tz;
+    ku_tile_kernel<T, TX, TY, MODE><<<K.ntiles(), Sh::NT, smem, st>>>(a);
+    return counted(cudaGetLastError());
+}
+
+template <typename T, int MODE>
+static cudaError_t dispatch_ku(const KuLaunch &K, KuArgs<T> &a, cudaStream_t st) {
+    if (K.tx == 32 && K.ty == 8) return launch_ku<T, 32, 8, MODE>(K, a, st);
+    if (K.tx == 32 && K.ty == 4) return launch_ku<T, 32, 4, MODE>(K, a, st);
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
+                     T *y, cudaStream_t st) {
+    KuArgs<T> a{};
+    a.L = L;
+    a.M = M;
+    a.s = s;
+    a.u = u;
+    a.y = y;
+    return dispatch_ku<T, KU_PLAIN>(K, a, st);
+}
+
+template <typename T>
+cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s,
+                   const T *p_prev, const T *r, const T *dinv, const uint8_t *mask, T *q, T *p_out,
+                   double *partial, Scalars *S, cudaStream_t st) {
+    KuArgs<T> a{};
+    a.L = L;
+    a.M = M;
+    a.s = s;
+    a.u = p_prev;
+    a.r = r;
+    a.dinv = dinv;
+    a.mask = mask;
+    a.y = q;
+    a.p_out = p_out;
+    a.partial = partial;
+    a.S = S;
+    return dispatch_ku<T, KU_PCG>(K, a, st);
+}
+
+cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
+                     const double *x, const double *f, const double *dinv, const uint8_t *mask,
+                     double *r, double *ce, double *partial, Scalars *S, cudaStream_t st) {
+    KuArgs<double> a{};
+    a.L = L;
+    a.M = M;
+    a.s = s;
+    a.u = x;
+    a.f = f;
+    a.dinv = dinv;
+    a.mask = mask;
+    a.y = r;
+    a.ce = ce;
+    a.energy = ce != nullptr;
+    a.partial = partial;
+    a.S = S;
+    return dispatch_ku<double, KU_RESID>(K, a, st);
+}
+
+template cudaError_t ku_plain<float>(const KuLaunch &, const Layout &, const Modal<float> &,
+                                     const float *, const float *, float *, cudaStream_t);
+template cudaError_t ku_plain<double>(const KuLaunch &, const Layout &, const Modal<double> &,
+                                      const double *, const double *, double *, cudaStream_t);
+template cudaError_t ku_pcg<float>(const KuLaunch &, const Layout &, const Modal<float> &,
+                                   const float *, const float *, const float *, const float *,
+                                   const uint8_t *, float *, float *, double *, Scalars *,
+                                   cudaStream_t);
+template cudaError_t ku_pcg<double>(const KuLaunch &, const Layout &, const Modal<double> &,
+                                    const double *, const double *, const double *,
+                                    const double *, const uint8_t *, double *, double *, double *,
+                                    Scalars *, cudaStream_t);
+
+// ============================================================================
+// PCG vector kernels
+// ============================================================================
+constexpr int VEC_THREADS = 256;
+
+// flat loop over the 3 component planes; dinv indexed by node = i mod cs
+template <typename T>
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                      const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
+                      Scalars *S) {
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag;
+    if (S->done) return;
+    const T alpha = (T)S->alpha;
+    const long long cs = L.cs;
+    Acc<T> a0, a1;
+    // one node per thread and step, its three component planes
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)gridDim.x * blockDim.x) {
+        const T d = dinv[n];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long i = n + c * cs;
+            const T xi = x[i] + alpha * p[i];
+            const T ri = r[i] - alpha * q[i];
+            x[i] = xi;
+            r[i] = ri;
+            a0.add_prod(ri, ri);
+            a1.add_prod(ri, d * ri);
+        }
+    }
+    double v[2] = {a0.value(), a1.value()};
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = v[0];
+        partial[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last(&S->cnt_upd, &last_flag)) return;
+    double tot[2];
+    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) {
+        const double rr = tot[0], rz = tot[1];
+        S->it += 1;
+        S->rr = rr;
+        if (!isfinite(rr) || !isfinite(rz)) {
+            S->status = ST_NAN;
+            S->done = 1;
+        } else if (rr < S->thr) {
+            S->status = ST_CONVERGED;
+            S->done = 1;
+        } else if (S->it >= S->maxit) {
+            S->status = ST_MAXIT;
+            S->done = 1;
+        }
+        S->beta = (S->rz != 0.0) ? rz / S->rz : 0.0;
+        S->rz = rz;
+        S->cnt_upd = 0;
+    }
+}
+
+template <typename T>
+cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *p, const T *q, const T *dinv,
+                       double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    pcg_update_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, p, q, dinv, partial, S);
+    return counted(cudaGetLastError());
+}
+template cudaError_t pcg_update<float>(const Layout &, float *, float *, const float *,
+                                       const float *, const float *, double *, Scalars *, int,
+                                       cudaStream_t);
+template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *,
+                                        const double *, const double *, double *, Scalars *, int,
+                                        cudaStream_t);
+
+template <typename T>
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_start_kernel(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double tol,
+                     double bnorm2, int maxit, double *partial, Scalars *S) {
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag;
+    const long long cs = L.cs;
+    Acc<T> a0, a1;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)gridDim.x * blockDim.x) {
+        const T d = dinv[n];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T ri = r[n + c * cs];
+            a0.add_prod(ri, ri);
+            a1.add_prod(ri, d * ri);
+        }
+    }
+    double v[2] = {a0.value(), a1.value()};
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = v[0];
+        partial[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last(&S->cnt_upd, &last_flag)) return;
+    double tot[2];
+    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) {
+        S->rr = tot[0];
+        S->rz = tot[1];
+        S->thr = tol * tol * (bnorm2 > 0.0 ? bnorm2 : tot[0]);
+        S->beta = 0.0;
+        S->alpha = 0.0;
+        S->it = 0;
+        S->maxit = maxit;
+        S->status = ST_RUNNING;
+        S->done = 0;
+        if (!isfinite(tot[0])) {
+            S->status = ST_NAN;
+            S->done = 1;
+        } else if (tot[0] < S->thr || tot[0] == 0.0) {
+            S->status = ST_CONVERGED;
+            S->done = 1;
+        } else if (maxit <= 0) {
+            S->status = ST_MAXIT;
+            S->done = 1;
+        }
+        S->cnt_upd = 0;
+    }
+}
+
+template <typename T>
+cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double tol, double bnorm2,
+                      int maxit, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    pcg_start_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, r, dinv, tol, bnorm2, maxit, partial, S);
+    return counted(cudaGetLastError());
+}
+template cudaError_t pcg_start<float>(const Layout &, const float *, const float *, double, double,
+                                      int, double *, Scalars *, int, cudaStream_t);
+template cudaError_t pcg_start<double>(const Layout &, const double *, const double *, double,
+                                       double, int, double *, Scalars *, int, cudaStream_t);
+
+__global__ void dc_inner_init_kernel(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
+                                     float *__restrict__ x32, const Scalars *S) {
+    const double inv = S->res_rr > 0.0 ? 1.0 / sqrt(S->res_rr) : 0.0;
+    const long long n = 3 * L.cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        r32[i] = (float)(r64[i] * inv);
+        x32[i] = 0.f;
+    }
+}
+cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
+                          const Scalars *S, int nblocks, cudaStream_t st) {
+    dc_inner_init_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, r64, r32, x32, S);
+    return counted(cudaGetLastError());
+}
+
+__global__ void dc_accumulate_kernel(Layout L, double *__restrict__ x64, const float *__restrict__ x32,
+                                     const Scalars *S) {
+    const double sc = sqrt(S->res_rr);
+    const long long n = 3 * L.cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        x64[i] = fma(sc, (double)x32[i], x64[i]);
+}
+cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
+                          int nblocks, cudaStream_t st) {
+    dc_accumulate_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, x64, x32, S);
+    return counted(cudaGetLastError());
+}
+
+// ============================================================================
+// set-up kernels
+// ============================================================================
+__device__ __forceinline__ double pow_fast(double x, double p) {
+    // integer exponents in [0, 8] by repeated multiplication, else pow
+    if (p == floor(p) && p >= 0.0 && p <= 8.0) {
+        const int k = (int)p;
+        double r = 1.0;
+        for (int i = 0; i < k; ++i) r *= x;
+        return r;
+    }
+    return pow(x, p);
+}
+
+__global__ void scales_kernel(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
+                              int variant, double p, double emin, double rho_min, double E,
+                              double *__restrict__ s64, float *__restrict__ s32) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int g = grid ? grid[e] : 0;
+        const double r = rho[e];
+        double v;
+        if (variant == 0) {
+            if (g == -1 || r < rho_min) v = 0.0;
+            else if (g == 1) v = 1.0;
+            else v = emin + pow_fast(r, p) * (1.0 - emin);
+        } else {
+            if (g == -1) v = 0.0;
+            else if (g == 1) v = 1.0;
+            else v = (emin + pow_fast(r, p) * (E - emin)) / E;
+        }
+        if (s64) s64[e] = v;
+        if (s32) s32[e] = (float)v;
+    }
+}
+cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int variant, double p,
+                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st) {
+    const int nb = std::max(1, std::min(div_up(L.nel, 256), 152 * 16));
+    scales_kernel<<<nb, 256, 0, st>>>(L, rho, grid, variant, p, emin, rho_min, E, s64, s32);
+    return counted(cudaGetLastError());
+}
+
+__global__ void diag_mask_kernel(Layout L, const double *__restrict__ s, double d0,
+                                 const uint8_t *__restrict__ fixed_bits, double *__restrict__ dinv64,
+                                 float *__restrict__ dinv32, uint8_t *__restrict__ mask) {
+    const long long nn = L.sxy * (L.nz + 1);
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
+         n += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(n / L.sxy);
+        const long long rem = n - (long long)iz * L.sxy;
+        const int iy = (int)(rem / L.sx), ix = (int)(rem - (long long)iy * L.sx);
+        if (ix > L.nx) continue;  // padding column
+        double acc = 0.0;
+        for (int dz = -1; dz <= 0; ++dz) {
+            const int ez = iz + dz;
+            if (ez < 0 || ez >= L.nz) continue;
+            for (int dy = -1; dy <= 0; ++dy) {
+                const int ey = iy + dy;
+                if (ey < 0 || ey >= L.ny) continue;
+                for (int dx = -1; dx <= 0; ++dx) {
+                    const int ex = ix + dx;
+                    if (ex < 0 || ex >= L.nx) continue;
+                    acc += s[elem_index(L, ex, ey, ez)];
+                }
+            }
+        }
+        const double dg = d0 * acc;
+        const bool orphan = fabs(dg) < 1e-15;
+        uint8_t m = fixed_bits ? fixed_bits[n] : 0;
+        if (orphan) m = 7;
+        mask[n] = m;
+        const double di = orphan ? 0.0 : 1.0 / dg;
+        if (dinv64) dinv64[n] = di;
+        if (dinv32) dinv32[n] = (float)di;
+    }
+}
+cudaError_t diag_mask(const Layout &L, const double *s64, double d0, const uint8_t *fixed_bits,
+                      double *dinv64, float *dinv32, uint8_t *mask, cudaStream_t st) {
+    const long long nn = L.sxy * (L.nz + 1);
+    const int nb = std::max(1, std::min(div_up(nn, 256), 152 * 16));
+    diag_mask_kernel<<<nb, 256, 0, st>>>(L, s64, d0, fixed_bits, dinv64, dinv32, mask);
+    return counted(cudaGetLastError());
+}
+
+// ============================================================================
+// layout conversions
+// ============================================================================
+template <typename T>
+__global__ void dof_to_dev_kernel(Layout L, const double *__restrict__ src, T *__restrict__ dst) {
+    const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
+         n += (long long)gridDim.x * blockDim.x) {
+        // n enumerates reference node ids (i slowest, k fastest)
+        const int k = (int)(n % (L.nz + 1));
+        const long long t = n / (L.nz + 1);
+        const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
+        const long long d = node_index(L, i, j, k);
+        dst[d] = (T)src[3 * n];
+        dst[d + L.cs] = (T)src[3 * n + 1];
+        dst[d + 2 * L.cs] = (T)src[3 * n + 2];
+    }
+}
+template <typename T>
+__global__ void dev_to_dof_kernel(Layout L, const T *__restrict__ src, double *__restrict__ dst) {
+    const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
+         n += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(n % (L.nz + 1));
+        const long long t = n / (L.nz + 1);
+        const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
+        const long long d = node_index(L, i, j, k);
+        dst[3 * n] = (double)src[d];
+        dst[3 * n + 1] = (double)src[d + L.cs];
+        dst[3 * n + 2] = (double)src[d + 2 * L.cs];
+    }
+}
+template <typename T>
+cudaError_t dof_to_dev_t(const Layout &L, const double *src, T *dst, cudaStream_t st) {
+    const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    dof_to_dev_kernel<T><<<std::max(1, std::min(div_up(nn, 256), 152 * 16)), 256, 0, st>>>(L, src, dst);
+    return counted(cudaGetLastError());
+}
+template <typename T>
+cudaError_t dev_to_dof_t(const Layout &L, const T *src, double *dst, cudaStream_t st) {
+    const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    dev_to_dof_kernel<T><<<std::max(1, std::min(div_up(nn, 256), 152 * 16)), 256, 0, st>>>(L, src, dst);
+    return counted(cudaGetLastError());
+}
+template cudaError_t dof_to_dev_t<float>(const Layout &, const double *, float *, cudaStream_t);
+template cudaError_t dof_to_dev_t<double>(const Layout &, const double *, double *, cudaStream_t);
+template cudaError_t dev_to_dof_t<float>(const Layout &, const float *, double *, cudaStream_t);
+template cudaError_t dev_to_dof_t<double>(const Layout &, const double *, double *, cudaStream_t);
+cudaError_t dof_to_dev(const Layout &L, const double *src, double *dst, cudaStream_t st) {
+    return dof_to_dev_t<double>(L, src, dst, st);
+}
+cudaError_t dev_to_dof(const Layout &L, const double *src, double *dst, cudaStream_t st) {
+    return dev_to_dof_t<double>(L, src, dst, st);
+}
+
+template <typename T>
+__global__ void elem_conv_kernel(Layout L, const T *__restrict__ src, T *__restrict__ dst, int layout,
+                                 int to_dev) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        // e enumerates internal (x-fastest) elements
+        const int ex = (int)(e % L.nx);
+        const long long t = e / L.nx;
+        const int ey = (int)(t % L.ny), ez = (int)(t / L.ny);
+        const long long h = layout == 0 ? ((long long)ex * L.ny + ey) * L.nz + ez : e;
+        if (to_dev) dst[e] = src[h];
+        else dst[h] = src[e];
+    }
+}
+template <typename T>
+cudaError_t elem_to_dev(const Layout &L, const T *src, T *dst, int layout, cudaStream_t st) {
+    elem_conv_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(L, src, dst,
+                                                                                         layout, 1);
+    return counted(cudaGetLastError());
+}
+template <typename T>
+cudaError_t elem_from_dev(const Layout &L, const T *src, T *dst, int layout, cudaStream_t st) {
+    elem_conv_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(L, src, dst,
+                                                                                         layout, 0);
+    return counted(cudaGetLastError());
+}
+template cudaError_t elem_to_dev<double>(const Layout &, const double *, double *, int, cudaStream_t);
+template cudaError_t elem_to_dev<int8_t>(const Layout &, const int8_t *, int8_t *, int, cudaStream_t);
+template cudaError_t elem_to_dev<uint8_t>(const Layout &, const uint8_t *, uint8_t *, int, cudaStream_t);
+template cudaError_t elem_from_dev<double>(const Layout &, const double *, double *, int, cudaStream_t);
+
+// ============================================================================
+// filters
+// ============================================================================
+template <typename T>
+__global__ void filter_cpp_kernel(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw,
+                                  int ntaps, const double *__restrict__ x, const double *__restrict__ rho,
+                                  double *__restrict__ out) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int ex = (int)(e % L.nx);
+        const long long t = e / L.nx;
+        const int ey = (int)(t % L.ny), ez = (int)(t / L.ny);
+        T num = T(0), den = T(0);
+        for (int k = 0; k < ntaps; ++k) {
+            const int4 d = td[k];
+            const int xx = ex + d.x, yy = ey + d.y, zz = ez + d.z;
+            if (xx < 0 || xx >= L.nx || yy < 0 || yy >= L.ny || zz < 0 || zz >= L.nz) continue;
+            const long long n = elem_index(L, xx, yy, zz);
+            const T w = (T)tw[k];
+            const T rn = (T)rho[n];
+            num += w * rn * (T)x[n];
+            den += w * rn;
+        }
+        out[e] = (den > T(1e-15)) ? (double)(num / den) : x[e];
+    }
+}
+template <typename T>
+cudaError_t filter_cpp(const Layout &L, const Taps &tp, const double *x, const double *rho,
+                       double *out, cudaStream_t st) {
+    filter_cpp_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(
+        L, tp.d, tp.w, tp.n, x, rho, out);
+    return counted(cudaGetLastError());
+}
+template cudaError_t filter_cpp<float>(const Layout &, const Taps &, const double *, const double *,
+                                       double *, cudaStream_t);
+template cudaError_t filter_cpp<double>(const Layout &, const Taps &, const double *, const double *,
+                                        double *, cudaStream_t);
+
+__device__ __forceinline__ int reflect_idx(int i, int n) {
+    const int period = 2 * n;
+    int m = i % period;
+    if (m < 0) m += period;
+    return (m >= n) ? period - 1 - m : m;
+}
+
+template <typename T>
+__global__ void filter_py_kernel(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw,
+                                 int ntaps, const double *__restrict__ x, const double *__restrict__ rho,
+                                 double *__restrict__ out, int mode, double lo) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int ex = (int)(e % L.nx);
+        const long long t = e / L.nx;
+        const int ey = (int)(t % L.ny), ez = (int)(t / L.ny);
+        T acc = T(0);
+        for (int k = 0; k < ntaps; ++k) {
+            const int4 d = td[k];
+            const long long n = elem_index(L, reflect_idx(ex + d.x, L.nx), reflect_idx(ey + d.y, L.ny),
+                                           reflect_idx(ez + d.z, L.nz));
+            T v = (T)x[n];
+            if (mode == 2) v = (T)(x[n] * rho[n]);
+            acc += (T)tw[k] * v;
+        }
+        double o = (double)acc;
+        if (mode == 1) o = npmin(npmax(o, lo), 1.0);
+        else if (mode == 2) o = o / npmax(rho[e], 1e-3);
+        out[e] = o;
+    }
+}
+template <typename T>
+cudaError_t filter_py(const Layout &L, const Taps &tp, const double *x, const double *rho,
+                      double *out, int mode, double lo, cudaStream_t st) {
+    filter_py_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(
+        L, tp.d, tp.w, tp.n, x, rho, out, mode, lo);
+    return counted(cudaGetLastError());
+}
+template cudaError_t filter_py<float>(const Layout &, const Taps &, const double *, const double *,
+                                      double *, int, double, cudaStream_t);
+template cudaError_t filter_py<double>(const Layout &, const Taps &, const double *, const double *,
+                                       double *, int, double, cudaStream_t);
+
+// ============================================================================
+// sensitivities
+// ============================================================================
+__global__ void __launch_bounds__(256)
+    sens_kernel(Layout L, const double *__restrict__ rho, const double *__restrict__ ce,
+                const double *__restrict__ s, const uint8_t *__restrict__ design, int variant,
+                double p, double *__restrict__ dc, int accumulate, double *partial, Scalars *S) {
+    __shared__ double red[256 / 32];
+    __shared__ int last_flag;
+    double en = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const double c = ce[e];
+        en = fma(s[e], c, en);  // void elements have s = 0
+        if (variant == 0) {
+            dc[e] = -p * pow_fast(rho[e], p - 1.0) * c;
+        } else {
+            double d = design[e] ? -p * pow_fast(rho[e], p - 1.0) * c : 0.0;
+            if (d != d) d = 0.0;
+            dc[e] = accumulate ? dc[e] + d : d;
+        }
+    }
+    double v[1] = {en};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v[0];
+    if (!arrive_last(&S->cnt_misc, &last_flag)) return;
+    double tot[1];
+    reduce_partials<1>(partial, gridDim.x, 1, tot, red);
+    if (threadIdx.x == 0) {
+        S->comp_energy = accumulate ? S->comp_energy + tot[0] : tot[0];
+        S->cnt_misc = 0;
+    }
+}
+cudaError_t sensitivities(const Layout &L, const double *rho, const double *ce, const double *s,
+                          const uint8_t *design, int variant, double p, double *dc, int accumulate,
+                          double *partial, Scalars *S, cudaStream_t st) {
+    const int nb = std::max(1, std::min(div_up(L.nel, 256), 152 * 8));
+    sens_kernel<<<nb, 256, 0, st>>>(L, rho, ce, s, design, variant, p, dc, accumulate, partial, S);
+    return counted(cudaGetLastError());
+}
+
+__global__ void sparse_dot_kernel(const long long *idx, const double *val, int n, const double *u,
+                                  double *out) {
+    __shared__ double red[256 / 32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(val[i], u[idx[i]], acc);
+    double v[1] = {acc};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) *out = v[0];
+}
+cudaError_t sparse_dot(const long long *idx, const double *val, int n, const double *u,
+                       double *out, cudaStream_t st) {
+    sparse_dot_kernel<<<1, 256, 0, st>>>(idx, val, n, u, out);
+    return counted(cudaGetLastError());
+}
+
+__global__ void masked_sqnorm_kernel(const long long *idx, const double *val, int n, long long cs,
+                                     const uint8_t *mask, double *out) {
+    __shared__ double red[256 / 32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const long long d = idx[i];
+        const int comp = (int)(d / cs);
+        const long long node = d - comp * cs;
+        if (!((mask[node] >> comp) & 1u)) acc = fma(val[i], val[i], acc);
+    }
+    double v[1] = {acc};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) *out = v[0];
+}
+cudaError_t masked_sqnorm(const long long *idx, const double *val, int n, long long cs,
+                          const uint8_t *mask, double *out, cudaStream_t st) {
+    masked_sqnorm_kernel<<<1, 256, 0, st>>>(idx, val, n, cs, mask, out);
+    return counted(cudaGetLastError());
+}
+
+// ============================================================================
+// OC bisection (topology_optimizer.cpp:205-287 / topopt.py:200-264)
+//
+// Per element the update is max(rmin, max(rho - m, min(1, min(rho + m, rho Be))))
+// with Be = sqrt(-dc / (lmid + eps)).  It is evaluated as a * t with
+// a = rho sqrt(-dc) (once per update) and t = 1/sqrt(lmid + eps) (once per pass),
+// and the bounds rho -/+ m are precomputed, so a pass reads 3 values per element
+// and writes nothing; the density is written once with the last pass's t.
+// FP64 mode does the pass in FP64.  Mixed mode does it in double-float
+// arithmetic on the FP32 pipes (FP64 is ~1/64 of FP32 on GB300): an FP32 pass
+// shifts the bisection volume enough to flip its branch decisions, a
+// double-float pass keeps ~48 significant bits like the FP64 reference.
+// ============================================================================
+__device__ __forceinline__ float2 df_of(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    const float s = p + e;
+    return make_float2(s, e - (s - p));
+}
+__device__ __forceinline__ bool df_lt(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+__device__ __forceinline__ bool df_nan(float2 a) { return a.x != a.x; }
+
+struct OcPrepArgs {
+    long long nel;
+    const double *rho, *dc;
+    double *a64, *lo64, *hi64;
+    float2 *a32, *lo32, *hi32;
+    double move;
+    int fp64, variant;
+    Scalars *S;
+};
+
+__global__ void oc_prepare_kernel(OcPrepArgs A) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const double r = A.rho[e];
+        const double a = r * sqrt(-A.dc[e]);
+        const double lo = r - A.move, hi = r + A.move;
+        if (A.fp64) {
+            A.a64[e] = a;
+            A.lo64[e] = lo;
+            A.hi64[e] = hi;
+        } else {
+            A.a32[e] = df_of(a);
+            A.lo32[e] = df_of(lo);
+            A.hi32[e] = df_of(hi);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Scalars *S = A.S;
+        const double l1 = A.variant == 0 ? 1e-20 : 1e-9;
+        const double l2 = A.variant == 0 ? 1e20 : 1e9;
+        const double eps = A.variant == 0 ? 1e-20 : 1e-10;
+        S->l1 = l1;
+        S->l2 = l2;
+        S->oc_t = 1.0 / sqrt(0.5 * (l1 + l2) + eps);
+        S->oc_t_last = S->oc_t;
+        S->oc_pass = 0;
+        S->oc_done = 0;
+        S->oc_variant = A.variant;
+    }
+}
+cudaError_t oc_prepare(const OcBuffers &B, const double *rho, const double *dc, double move, int fp64,
+                       int variant, Scalars *S, cudaStream_t st) {
+    OcPrepArgs a{B.nel, rho, dc, B.a64, B.lo64, B.hi64, B.a32, B.lo32, B.hi32, move, fp64, variant, S};
+    oc_prepare_kernel<<<std::max(1, std::min(div_up(B.nel, 256), 152 * 16)), 256, 0, st>>>(a);
+    return counted(cudaGetLastError());
+}
+
+template <typename T>
+__device__ __forceinline__ T oc_clamp(T c, T lo, T hi, T rmin, int variant) {
+    if (variant == 0) return cmax<T>(rmin, cmax<T>(lo, cmin<T>(T(1), cmin<T>(hi, c))));
+    return npmax<T>(rmin, npmax<T>(lo, npmin<T>(T(1), npmin<T>(hi, c))));
+}
+
+// the same chain on double-float values
+__device__ __forceinline__ float2 oc_clamp_df(float2 c, float2 lo, float2 hi, float2 rmin, int variant) {
+    const float2 one = make_float2(1.f, 0.f);
+    if (variant == 0) {
+        float2 m = df_lt(c, hi) ? c : hi;       // std::min(hi, c)
+        m = df_lt(m, one) ? m : one;             // std::min(1, m)
+        m = df_lt(lo, m) ? m : lo;               // std::max(lo, m)
+        return df_lt(rmin, m) ? m : rmin;        // std::max(rmin, m)
+    }
+    if (df_nan(c) || df_nan(lo) || df_nan(hi)) return make_float2(__int_as_float(0x7fc00000), 0.f);
+    float2 m = df_lt(c, hi) ? c : hi;
+    m = df_lt(m, one) ? m : one;
+    m = df_lt(m, lo) ? lo : m;
+    return df_lt(m, rmin) ? rmin : m;
+}
+
+__device__ __forceinline__ void oc_stop_check(Scalars *S, double cur, double vf, int variant) {
+    const double lmid = 0.5 * (S->l1 + S->l2);
+    S->oc_cur = cur;
+    S->oc_t_last = S->oc_t;
+    if (cur > vf) S->l1 = lmid;
+    else S->l2 = lmid;
+    S->oc_pass += 1;
+    const double l1 = S->l1, l2 = S->l2;
+    bool stop;
+    if (variant == 0) {
+        stop = (l2 - l1) / (l1 + l2) < 1e-4;
+    } else {
+        const double den = (l1 + l2) > 1e-10 ? (l1 + l2) : 1e-10;
+        stop = (l1 + l2 < 1e-12) || ((l2 - l1) / den <= 1e-3);
+    }
+    if (stop || S->oc_pass >= 100) S->oc_done = 1;
+    const double eps = variant == 0 ? 1e-20 : 1e-10;
+    S->oc_t = 1.0 / sqrt(0.5 * (l1 + l2) + eps);
+}
+
+struct OcPassArgs {
+    OcBuffers B;
+    const uint8_t *design;
+    int fp64, variant;
+    double rho_min, vf, n_design;
+    double *partial;
+    Scalars *S;
+};
+
+// One bisection pass: volume of the design elements at the current t.
+__global__ void __launch_bounds__(256) oc_pass_kernel(OcPassArgs A) {
+    __shared__ double red[256 / 32];
+    __shared__ int last_flag;
+    Scalars *S = A.S;
+    if (S->oc_done) return;
+    const double t = S->oc_t;
+    double vol64 = 0.0;
+    DF vol{0.f, 0.f};
+    if (A.fp64) {
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+             e += (long long)gridDim.x * blockDim.x) {
+            if (!A.design[e]) continue;
+            vol64 += oc_clamp<double>(A.B.a64[e] * t, A.B.lo64[e], A.B.hi64[e], A.rho_min, A.variant);
+        }
+    } else {
+        const float2 tdf = df_of(t), rmin = df_of(A.rho_min);
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+             e += (long long)gridDim.x * blockDim.x) {
+            if (!A.design[e]) continue;
+            const float2 v = oc_clamp_df(df_mul(A.B.a32[e], tdf), A.B.lo32[e], A.B.hi32[e], rmin, A.variant);
+            df_add(vol, v.x);
+            vol.lo += v.y;
+        }
+        vol64 = df_value(vol);
+    }
+    double v[1] = {vol64};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) A.partial[blockIdx.x] = v[0];
+    if (!arrive_last(&S->cnt_oc, &last_flag)) return;
+    double tot[1];
+    reduce_partials<1>(A.partial, gridDim.x, 1, tot, red);
+    if (threadIdx.x == 0) {
+        oc_stop_check(S, tot[0] / A.n_design, A.vf, A.variant);
+        S->cnt_oc = 0;
+    }
+}
+cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min, double vf,
+                    double n_design, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    OcPassArgs a{B, design, fp64, variant, rho_min, vf, n_design, partial, S};
+    oc_pass_kernel<<<nblocks, 256, 0, st>>>(a);
+    return counted(cudaGetLastError());
+}
+
+// Density of the last executed pass, max |change| and the design-mask mean.
+__global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const double *__restrict__ rho,
+                                                       double *__restrict__ rho_new) {
+    __shared__ double red[2 * (256 / 32)];
+    __shared__ int last_flag;
+    Scalars *S = A.S;
+    const double t = S->oc_t_last;
+    const float2 tdf = df_of(t), rmin = df_of(A.rho_min);
+    double mc = 0.0, vs = 0.0, cnt = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+         e += (long long)gridDim.x * blockDim.x) {
+        const double r0 = rho[e];
+        double v = r0;
+        if (A.design[e]) {
+            if (S->oc_pass == 0) v = r0;  // no pass ran (cannot happen with the reference bounds)
+            else if (A.fp64) v = oc_clamp<double>(A.B.a64[e] * t, A.B.lo64[e], A.B.hi64[e], A.rho_min, A.variant);
+            else v = df_to(oc_clamp_df(df_mul(A.B.a32[e], tdf), A.B.lo32[e], A.B.hi32[e], rmin, A.variant));
+            vs += v;
+            cnt += 1.0;
+        }
+        rho_new[e] = v;
+        mc = fmax(mc, fabs(v - r0));
+    }
+    const double m = block_max(mc, red);
+    double s2[2] = {vs, cnt};
+    block_sum<2>(s2, red);
+    if (threadIdx.x == 0) {
+        A.partial[3 * blockIdx.x] = m;
+        A.partial[3 * blockIdx.x + 1] = s2[0];
+        A.partial[3 * blockIdx.x + 2] = s2[1];
+    }
+    if (!arrive_last(&S->cnt_oc, &last_flag)) return;
+    if (threadIdx.x == 0) {
+        double mm = 0.0, ss = 0.0, cc = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+            mm = fmax(mm, __ldcg(A.partial + 3 * b));
+            ss += __ldcg(A.partial + 3 * b + 1);
+            cc += __ldcg(A.partial + 3 * b + 2);
+        }
+        S->oc_change = mm;
+        S->oc_volume = cc > 0.0 ? ss / cc : ss / (double)A.B.nel;
+        S->cnt_oc = 0;
+    }
+}
+cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min,
+                     const double *rho, double *rho_new, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    OcPassArgs a{B, design, fp64, variant, rho_min, 0.0, 1.0, partial, S};
+    oc_final_kernel<<<nblocks, 256, 0, st>>>(a, rho, rho_new);
+    return counted(cudaGetLastError());
+}
+
+}  // namespace amk

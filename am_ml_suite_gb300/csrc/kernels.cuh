@@ -1,0 +1,129 @@
+// kernels.cuh -- host-visible launchers of the GB300 SIMP engine kernels.
+// Every launcher enqueues on `st` and returns the launch error (no host sync).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "am_common.cuh"
+
+namespace amk {
+
+// kernel launches issued so far (graph replays add their kernel-node count)
+long long launch_count();
+void count_launches(long long n);
+
+// ---- tiled K*u (ku.cuh) ----------------------------------------------------
+struct KuLaunch {
+    int tx, ty;  // owned node columns per tile (one of the compiled shapes)
+    int tz;      // node planes per tile
+    int tiles_x, tiles_y, tiles_z;
+    int ntiles() const { return tiles_x * tiles_y * tiles_z; }
+};
+KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint);
+
+template <typename T>
+cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
+                     T *y, cudaStream_t st);
+// q = mask(K p), p = dinv r + beta p_prev (beta from S), partial p.q -> S->alpha
+template <typename T>
+cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s,
+                   const T *p_prev, const T *r, const T *dinv, const uint8_t *mask, T *q, T *p_out,
+                   double *partial, Scalars *S, cudaStream_t st);
+// r = mask(f - K x) in FP64 with r.r, r.dinv.r -> S->res_rr / res_rz; optional ce.
+cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
+                     const double *x, const double *f, const double *dinv, const uint8_t *mask,
+                     double *r, double *ce, double *partial, Scalars *S, cudaStream_t st);
+
+// ---- PCG vector kernels ------------------------------------------------------
+// x += alpha p; r -= alpha q; rr, rz -> S (beta, convergence, iteration count)
+template <typename T>
+cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *p, const T *q, const T *dinv,
+                       double *partial, Scalars *S, int nblocks, cudaStream_t st);
+// PCG start from r (already masked): rr, rz -> S; thr = tol^2 * bnorm2 (or * rr if
+// bnorm2 <= 0); beta = 0; it = 0; done if converged already.
+template <typename T>
+cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double tol, double bnorm2,
+                      int maxit, double *partial, Scalars *S, int nblocks, cudaStream_t st);
+// r32 = r64 / sqrt(S->res_rr), x32 = 0 (inner start of the defect correction)
+cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
+                          const Scalars *S, int nblocks, cudaStream_t st);
+// x64 += sqrt(S->res_rr) * x32
+cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
+                          int nblocks, cudaStream_t st);
+
+// ---- set-up kernels ------------------------------------------------------------
+// element scales from a device density (internal layout).  variant 0 (CPP):
+// grid -1 or rho < rho_min -> 0, grid 1 -> 1, else emin + rho^p (1 - emin);
+// variant 1 (PY): grid -1 -> 0, grid 1 -> 1, else (emin + rho^p (E - emin))/E.
+cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int variant, double p,
+                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st);
+// per-node inverse diagonal (KE[0][0] * sum of the adjacent scales), orphan DOFs
+// (|diag| < 1e-15) joined to the constrained bits of `fixed_bits`.
+cudaError_t diag_mask(const Layout &L, const double *s64, double d0, const uint8_t *fixed_bits,
+                      double *dinv64, float *dinv32, uint8_t *mask, cudaStream_t st);
+
+// ---- layout conversions --------------------------------------------------------
+// reference DOF order <-> device component planes
+cudaError_t dof_to_dev(const Layout &L, const double *src, double *dst, cudaStream_t st);
+cudaError_t dev_to_dof(const Layout &L, const double *src, double *dst, cudaStream_t st);
+template <typename T>
+cudaError_t dof_to_dev_t(const Layout &L, const double *src, T *dst, cudaStream_t st);
+template <typename T>
+cudaError_t dev_to_dof_t(const Layout &L, const T *src, double *dst, cudaStream_t st);
+// element array in host layout (0 z-fastest, 1 x-fastest) <-> internal x-fastest
+template <typename T>
+cudaError_t elem_to_dev(const Layout &L, const T *src, T *dst, int layout, cudaStream_t st);
+template <typename T>
+cudaError_t elem_from_dev(const Layout &L, const T *src, T *dst, int layout, cudaStream_t st);
+
+// ---- filters ---------------------------------------------------------------------
+struct Taps {
+    const int4 *d;       // (dx, dy, dz, 0)
+    const double *w;     // weight
+    int n;
+};
+// CPP: out = sum w rho_n x_n / sum w rho_n (neighbours in the grid), x if den <= 1e-15
+template <typename T>
+cudaError_t filter_cpp(const Layout &L, const Taps &tp, const double *x, const double *rho,
+                       double *out, cudaStream_t st);
+// PY: out = sum w x_n[reflect] ; mode 0 plain, 1 clip(out, lo, 1), 2 x := x*rho and
+// out /= max(rho, 1e-3)
+template <typename T>
+cudaError_t filter_py(const Layout &L, const Taps &tp, const double *x, const double *rho,
+                      double *out, int mode, double lo, cudaStream_t st);
+
+// ---- sensitivities -----------------------------------------------------------------
+// dc = -p rho^(p-1) ce over all elements (CPP) or design elements (PY, accumulated
+// into dc with NaN -> 0); energy = sum s ce over non-void elements -> S->comp_energy
+// (accumulate = 1 adds to S->comp_energy); fu = sum F.u over the listed DOFs.
+cudaError_t sensitivities(const Layout &L, const double *rho, const double *ce, const double *s,
+                          const uint8_t *design, int variant, double p, double *dc, int accumulate,
+                          double *partial, Scalars *S, cudaStream_t st);
+cudaError_t sparse_dot(const long long *idx, const double *val, int n, const double *u,
+                       double *out, cudaStream_t st);
+// sum of val^2 over the listed entries whose DOF is not masked (||F||^2 on the free DOFs)
+cudaError_t masked_sqnorm(const long long *idx, const double *val, int n, long long cs,
+                          const uint8_t *mask, double *out, cudaStream_t st);
+// sets the shared-memory attributes of every compiled K*u kernel (call once,
+// outside stream capture)
+cudaError_t ku_init_attributes();
+
+// ---- OC ------------------------------------------------------------------------------
+// Per-element terms of the OC update: a = rho sqrt(-dc), lo = rho - move,
+// hi = rho + move, in FP64 (fp64 mode) or as double-float pairs (mixed).
+struct OcBuffers {
+    long long nel;
+    double *a64, *lo64, *hi64;
+    float2 *a32, *lo32, *hi32;
+};
+// computes the terms and resets the bisection state (l1, l2, t, pass, done)
+cudaError_t oc_prepare(const OcBuffers &B, const double *rho, const double *dc, double move, int fp64,
+                       int variant, Scalars *S, cudaStream_t st);
+// one bisection pass: design volume at the current multiplier -> l1 / l2, stop test
+cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min, double vf,
+                    double n_design, double *partial, Scalars *S, int nblocks, cudaStream_t st);
+// new density with the last pass's multiplier, max |change|, design-mask mean -> S
+cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min,
+                     const double *rho, double *rho_new, double *partial, Scalars *S, int nblocks, cudaStream_t st);
+
+}  // namespace amk

@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""SIMP iterations/s and PCG solve ms at relative residual 1e-6 on GB300.
+
+Workload (default ``bracket192``): the 192x96x96 bracket -- 1,769,472 hex8
+elements, 5,447,811 DOF, E0 = 1, nu = 0.3, E_min = 1e-9, p = 3, vf = 0.3,
+rmin = 2.0 cone sensitivity filter, move 0.2, clamped x = 0 face, a passive void
+cylinder (radius 16 voxels through y, axis at the x-z centre, rho = 0) and four
+passive solid 6x6 bolt-pad columns (full height, inset 6 voxels from the x-y
+corners, rho = 1), 3 point loads on the top face at seeded random nodes
+(numpy default_rng(2)), magnitude U(0.5, 1.5), direction uniform on the sphere.
+K*u in FP32 inside an FP64 defect-correction loop to rel-res 1e-6, Jacobi PCG.
+
+One step = one SIMP iteration (solve, sensitivities, filter, OC update).
+``value``: iterations/s over the timed steps with the state resident in HBM.
+``e2e``: the same metric through the public C ABI from host buffers
+(``am_problem_set_loads`` + ``am_simp_run`` for W+K iterations, density
+downloaded).  The working set of a step (solver vectors + element arrays,
+~300 MB) exceeds the 129 MB L2, so no explicit flush is needed between steps;
+the roofline probe of the dominant kernel flushes L2 before each launch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (shape, rmin, vf, description)
+    "bracket192": ((192, 96, 96), 2.0, 0.3, "192x96x96 bracket, void cylinder r=16 through y, 4 bolt-pad columns, "
+                                            "3 seeded point loads on the top face"),
+    "cantilever256": ((256, 128, 128), 2.5, 0.25, "256x128x128 cantilever, -z load 1 on the central 32x32 patch of x=max"),
+    "cantilever48": ((48, 24, 12), 1.5, 0.3, "48x24x12 cantilever, -z unit line load along x=48, z=6"),
+}
+
+
+def build_workload(name):
+    shape, rmin, vf, desc = WORKLOADS[name]
+    nx, ny, nz = shape
+    N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    node = lambda i, j, k: (i * (ny + 1) + j) * (nz + 1) + k  # noqa: E731
+    base = np.array([node(0, j, k) for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(N)
+    rho0 = np.full(shape, vf)
+    if name == "bracket192":
+        i = np.arange(nx)[:, None, None] + 0.5
+        k = np.arange(nz)[None, None, :] + 0.5
+        cyl = (i - nx / 2) ** 2 + (k - nz / 2) ** 2 <= 16.0 ** 2
+        rho0 = np.where(np.broadcast_to(cyl, shape), 0.0, rho0)
+        for x0 in (6, nx - 12):
+            for y0 in (6, ny - 12):
+                rho0[x0:x0 + 6, y0:y0 + 6, :] = 1.0
+        rng = np.random.default_rng(2)
+        ij = rng.integers(0, [nx + 1, ny + 1], size=(3, 2))
+        mag = rng.uniform(0.5, 1.5, size=3)
+        d = rng.normal(size=(3, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        for (a, b), m, v in zip(ij, mag, d):
+            F[3 * node(int(a), int(b), nz) + np.arange(3)] += m * v
+    elif name == "cantilever256":
+        c0j, c0k = ny // 2 - 16, nz // 2 - 16
+        nodes = [node(nx, j, k) for j in range(c0j, c0j + 33) for k in range(c0k, c0k + 33)]
+        F[3 * np.array(nodes) + 2] = -1.0 / len(nodes)
+    else:
+        line = [node(nx, j, nz // 2) for j in range(ny + 1)]
+        F[3 * np.array(line) + 2] = -1.0 / len(line)
+    return dict(shape=shape, rmin=rmin, vf=vf, F=F, fixed=fixed, rho0=rho0, desc=desc)
+
+
+def simp_config(nat, W, max_iterations=100):
+    return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
+                              rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
+                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=1e-4)
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[3:7]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ku_traffic_per_launch(W, nodes, elements):
+    """DRAM bytes per launch of the fused FP32 PCG K*u from the committed ncu
+    summary (measured on a smaller case, scaled by nodes), or None."""
+    p = os.path.join(ROOT, "profiles", "ku_pcg_fp32_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d["dram_bytes_per_launch"] * nodes / d["nodes"]
+
+
+def cpu_baseline(W, steps_gpu_its, pcg_iters_sample=20):
+    """The CPU restatement (oracle, OpenMP on all host cores): CSR assembly,
+    `pcg_iters_sample` Jacobi-PCG iterations, sensitivities, filter, OC of one
+    C++-variant SIMP iteration on the full workload.  The iteration rate is
+    extrapolated with the PCG iteration count per SIMP iteration of the GPU run
+    (same method, same tolerance)."""
+    import oracle as O
+
+    prm = O.make_params(volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2, rho_min=0.01,
+                        E_min=1e-9)
+    t0 = time.time()
+    times, threads = O.baseline_sample(W["shape"], prm, W["rho0"].ravel(), W["F"], W["fixed"], pcg_iters_sample)
+    wall = time.time() - t0
+    per_iter = (times["assembly"] + times["pcg_setup"] + steps_gpu_its * times["pcg_iteration"] +
+                times["sensitivities"] + times["filter"] + times["oc"])
+    return {"value": 1.0 / per_iter, "unit": "SIMP iters/s", "cores": threads, "kind": "port",
+            "sample": (f"one C++-variant SIMP iteration of the FP64 CPU restatement on the full workload: "
+                       f"CSR assembly + {pcg_iters_sample} Jacobi-PCG iterations timed (s/PCG-it "
+                       f"{times['pcg_iteration']:.4f}), extrapolated to {steps_gpu_its:.0f} PCG iterations per SIMP "
+                       f"iteration; sample wall {wall:.1f} s"),
+            "phases_s": times}
+
+
+def run_reference(args, W):
+    import oracle as O  # noqa: F401
+
+    # bounded sample per step: one timed sample of the CPU restatement per step
+    vals = []
+    sample = None
+    its = float(os.environ.get("AM_BENCH_PCG_ITS", "2000"))
+    for _ in range(max(1, args.warmup)):
+        cpu_baseline(W, its, 5)
+    t0 = time.time()
+    for _ in range(args.steps):
+        cb = cpu_baseline(W, its, 10)
+        vals.append(cb["value"])
+        sample = cb
+    wall = time.time() - t0
+    value = statistics.median(vals)
+    line = {"metric": "SIMP iters/s @ rel-res 1e-6 (Jacobi PCG)", "value": value, "unit": "SIMP iters/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "shape": list(W["shape"]), "description": W["desc"]},
+            "cpu_baseline": {"value": value, "unit": "SIMP iters/s", "cores": sample["cores"], "kind": "port",
+                             "sample": sample["sample"]},
+            "e2e": {"value": value, "unit": "SIMP iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # one independent replica per GPU (the single-domain path does not shard):
+        # pin this process to its GPU before the CUDA runtime starts
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    W = build_workload(args.workload)
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, W)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    from am_ml_suite_gb300 import _build, _native as nat
+
+    _build.build()
+    nat.load()
+    if not nat.is_available():
+        raise SystemExit("no CUDA device: the GB300 arm needs a GPU")
+    shape = W["shape"]
+    cfg = simp_config(nat, W)
+
+    # ---- device-resident timed region --------------------------------------
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([W["F"]], [W["fixed"]])
+    p.simp_begin(cfg, W["rho0"])
+    warm = [p.simp_step() for _ in range(args.warmup)]
+    lay = p.layout()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    l0 = nat.launch_count()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        res = [p.simp_step() for _ in range(args.steps)]  # each step ends with a device sync
+        t1 = time.perf_counter()
+    l1 = nat.launch_count()
+    elapsed = t1 - t0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps / elapsed
+    pcg_ms = 1000.0 * statistics.mean(r.solve_time_s for r in res)
+    pcg_its = statistics.mean(r.solver_iterations for r in res)
+
+    # ---- roofline of the dominant kernel (fused FP32 PCG K*u) ---------------
+    nodes, nel = lay["nodes"], lay["elements"]
+    ku_ms, ku_min = p.bench_kernel(0, reps=20, flush_l2=True)
+    # reads p, r (3 x 4 B each per node), dinv (4 B), mask (1 B), scale (4 B per
+    # element); writes p, q (3 x 4 B each per node)
+    alg_bytes = 53 * nodes + 4 * nel
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (ku_ms * 1e-3) / 1e9
+    traffic = ku_traffic_per_launch(W, nodes, nel)
+    res_ms, _ = p.bench_kernel(1, reps=5, flush_l2=True)
+    upd_ms, _ = p.bench_kernel(2, reps=20, flush_l2=True)
+    p.close()
+
+    # ---- end to end through the C ABI from host buffers ---------------------
+    e2e = None
+    if not args.no_e2e:
+        total = args.warmup + args.steps
+        ecfg = simp_config(nat, W, max_iterations=total)
+        try:
+            import torch
+
+            def pinned(a, dtype):
+                t = torch.empty(a.size, dtype=dtype, pin_memory=True)
+                arr = t.numpy()
+                arr[:] = a.ravel()
+                return arr, t
+
+            F_h, _tF = pinned(W["F"], torch.float64)
+            fx_h, _tx = pinned(W["fixed"].astype(np.int64), torch.int64)
+            r0_h, _tr = pinned(W["rho0"], torch.float64)
+            out_h, _to = pinned(np.zeros(nel), torch.float64)
+        except Exception:
+            F_h, fx_h, r0_h, out_h = W["F"], W["fixed"].astype(np.int64), W["rho0"].ravel(), np.zeros(nel)
+        q = nat.Problem(shape, 1.0, 1.0, 0.3)
+        te0 = time.perf_counter()
+        q.set_loads([F_h], [fx_h])
+        r = q.simp_run(ecfg, r0_h)
+        out_h[:] = r["density"]
+        te1 = time.perf_counter()
+        q.close()
+        h2d = F_h.nbytes + fx_h.nbytes + r0_h.nbytes
+        d2h = out_h.nbytes + 3 * 8 * total
+        e2e = {"value": world * total / (te1 - te0), "unit": "SIMP iters/s",
+               "h2d_bytes_per_step": int(h2d / total), "d2h_bytes_per_step": int(d2h / total),
+               "iterations": total, "wall_s": te1 - te0,
+               "note": "am_problem_set_loads + am_simp_run from host buffers, cold start included"}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(W, pcg_its)
+
+    if rank == 0:
+        line = {
+            "metric": "SIMP iters/s @ rel-res 1e-6 (Jacobi PCG); PCG solve ms in pcg_solve_ms",
+            "value": value, "unit": "SIMP iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 K*u + f64 defect correction",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
+                       "description": W["desc"], "precision": "mixed", "preconditioner": "jacobi",
+                       "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probe flushes L2",
+                       "parallelism": f"replicas x{world}"},
+            "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,
+            "solver_residual_max": max(r.solver_residual for r in res),
+            "compliance_last": res[-1].compliance,
+            "roofline": {"bound": "hbm", "kernel": "ku_tile_kernel<float,32,8,PCG> (fused p-update + K*p + p.q)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                         "avg_ms": ku_ms, "min_ms": ku_min},
+            "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_fp64": res_ms, "pcg_update_fp32": upd_ms},
+            "gpu_launches": int(l1 - l0),
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,231 @@
+/*
+ * am_gpu.h -- C ABI of the GB300 (sm_103a) SIMP topology-optimisation engine.
+ *
+ * Drop-in for the solver entry points of the reference engine
+ * (ettoremiglioranza1012/AM_ML_suite):
+ *   C++  TopologyOptimizer       cpp_engine/include/am/topology_optimizer.hpp:132-169
+ *        GlobalAssembler         cpp_engine/include/am/global_assembler.hpp:113-131
+ *        LinearSolver            cpp_engine/include/am/linear_solver.hpp:132-172
+ *   Py   SIMPOptimizer.run       src/am/numerical/topopt.py:94-133, 266-411
+ *        fem.solve_fem etc.      src/am/numerical/fem.py:175-383
+ * Inputs are a voxel domain plus load cases; outputs are the density field and
+ * the compliance / volume histories.  Every entry point takes caller-owned HOST
+ * buffers unless its name ends in _device; device memory lives in the opaque
+ * handle.  No entry point throws; each returns an am_status.
+ *
+ * Layout of host arrays:
+ *   densities / grids: AM_LAYOUT_ZFASTEST  e = i*ny*nz + j*nz + k  (C-order (nx,ny,nz);
+ *                      fem.py and global_assembler.hpp:162-164), or
+ *                      AM_LAYOUT_XFASTEST  e = k*nx*ny + j*nx + i  (topology_optimizer.hpp:218-232,
+ *                      am_topopt.cpp:167-171)
+ *   DOF vectors (F, u): 3*(i*(ny+1)*(nz+1) + j*(nz+1) + k) + d  (fem.py:168-170,
+ *                      global_assembler.cpp:45-50)
+ *   grid values: -1 void, 0 design, 1 fixed solid (geometry.py:16-30)
+ */
+#ifndef AM_GPU_H
+#define AM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference throws std::invalid_argument
+ * (global_assembler.cpp:73-83, linear_solver.cpp:59-63), std::out_of_range
+ * (linear_solver.cpp:69-73) and Python ValueError (fem.py:296-319); a solve that
+ * does not converge is a warning plus converged=false (linear_solver.cpp:175-180),
+ * which here is AM_OK with the converged flag cleared in the stats. */
+typedef enum am_status {
+    AM_OK = 0,
+    AM_ERR_INVALID_ARG = 1,
+    AM_ERR_SIZE_MISMATCH = 2,
+    AM_ERR_DOF_OUT_OF_RANGE = 3,
+    AM_ERR_NOT_CONVERGED = 4,
+    AM_ERR_NAN_DETECTED = 5,
+    AM_ERR_SINGULAR = 6,
+    AM_ERR_CUDA = 7,
+    AM_ERR_TIMEOUT = 8,
+    AM_ERR_OOM = 9,
+    AM_ERR_NO_DEVICE = 10
+} am_status;
+
+enum { AM_LAYOUT_ZFASTEST = 0, AM_LAYOUT_XFASTEST = 1 };
+
+/* Which reference loop the SIMP entry points follow.
+ * AM_VARIANT_CPP: TopologyOptimizer (topology_optimizer.cpp:294-520): relative E_min,
+ *   elements with rho < rho_min skipped in the stiffness (global_assembler.cpp:147-149),
+ *   design mask from the initial density, filter sum w rho dc / sum w rho
+ *   (:168-198), OC bisection 1e-20/1e20 to 1e-4 (:205-287), compliance u.F.
+ * AM_VARIANT_PY: SIMPOptimizer (topopt.py:266-411): absolute E_min, void/fixed grid
+ *   cells, density pre-filter + normalised reflect-mode cone filter, OC bisection
+ *   1e-9/1e9 to 1e-3, compliance sum of element energies, several load cases. */
+enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
+
+/* AM_PREC_FP64: every kernel in FP64 (the parity mode).
+ * AM_PREC_MIXED: FP32 K*u and PCG inside an FP64 defect-correction loop; FP64 for
+ *   dot products (double-float accumulation), alpha/beta, the outer residual
+ *   r = f - K u, compliance and the OC volume sums. */
+enum { AM_PREC_FP64 = 0, AM_PREC_MIXED = 1 };
+
+enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1 };
+
+/* SIMP configuration: SIMPConfig (topology_optimizer.hpp:49-59) + SIMPParams
+ * (topopt.py:30-52) + the solver knobs of SolverConfig (linear_solver.hpp:66-75). */
+typedef struct am_simp_config {
+    double volume_fraction;   /* target volume fraction */
+    double penalty;           /* SIMP exponent p */
+    double filter_radius;     /* rmin in elements */
+    double move_limit;
+    double rho_min;
+    double E_min;             /* relative (CPP) or absolute in units of E0 (PY) */
+    double convergence_tol;   /* max |delta rho| */
+    int max_iterations;
+    int variant;              /* AM_VARIANT_* */
+    int precision;            /* AM_PREC_* */
+    int preconditioner;       /* AM_PRECOND_* */
+    double cg_tol;            /* relative residual ||f - K u|| / ||f|| of every solve */
+    int cg_max_iterations;    /* cap on (inner) PCG iterations per solve */
+    int warm_start;           /* 1: each solve starts from the previous displacement */
+    double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve */
+    int max_outer;            /* MIXED: cap on defect-correction steps */
+    int layout;               /* AM_LAYOUT_* of density arrays */
+    int verbose;
+} am_simp_config;
+
+/* Per-solve statistics (SolveStats, linear_solver.hpp:48-56). */
+typedef struct am_solve_stats {
+    int iterations;           /* PCG iterations (sum of inner iterations in MIXED) */
+    int outer_iterations;     /* defect-correction steps (MIXED), 1 in FP64 */
+    double residual;          /* final ||f - K u|| / ||f||, computed in FP64 */
+    int converged;
+    double solve_time_s;
+    double max_displacement;
+    double min_displacement;
+} am_solve_stats;
+
+/* IterationResult (topology_optimizer.hpp:65-74) plus the extra fields of this engine. */
+typedef struct am_iteration_result {
+    double compliance;         /* CPP: u.F ; PY: sum over load cases of element energies */
+    double compliance_energy;  /* sum_e scale_e u_e^T KE u_e (both variants) */
+    double volume_fraction;    /* mean density over the design mask after the update */
+    double max_density_change;
+    int solver_iterations;
+    int solver_outer_iterations;
+    double solver_residual;
+    int solver_converged;
+    int oc_passes;             /* bisection passes of the OC update */
+    double assembly_time_s;    /* scale / diagonal set-up (no global K is assembled) */
+    double solve_time_s;
+    double sensitivity_time_s;
+    double update_time_s;      /* filter + OC */
+} am_iteration_result;
+
+typedef struct am_problem am_problem;
+
+/* Human-readable status name; detail of the last error of this thread. */
+const char *am_status_string(am_status s);
+const char *am_last_error(void);
+
+/* Library / device information.  get_max_threads of the missing Python binding
+ * (notebook cells 23-24) maps to the SM count; is_available to a usable device. */
+int am_is_available(void);
+am_status am_device_info(int *sm_count, size_t *free_bytes, size_t *total_bytes);
+
+/* 24x24 row-major element stiffness of a cube of edge h, material (E, nu), as
+ * applied by the kernels (the 2x2x2-Gauss KE of ElementKernel::computeStiffness
+ * element_kernel.cpp:155-179 / get_element_stiffness_matrix fem.py:43-135;
+ * node order element_kernel.cpp:41-50). */
+am_status am_element_stiffness(double E, double nu, double h, double *ke);
+
+/* Fills cfg with the defaults of the chosen variant (SIMPConfig defaults for CPP,
+ * SIMPParams defaults for PY), MIXED precision, Jacobi, cg_tol 1e-6. */
+void am_simp_config_default(am_simp_config *cfg, int variant);
+
+/* Creates a problem on the current CUDA device: nx*ny*nz cubic elements of edge h,
+ * isotropic material (E0, nu).  grid (nullable = all design) uses `layout`.
+ * Replaces TopologyOptimizer::TopologyOptimizer (topology_optimizer.cpp:16-53). */
+am_status am_problem_create(int nx, int ny, int nz, double h, double E0, double nu,
+                            const int8_t *grid, int layout, am_problem **out);
+am_status am_problem_destroy(am_problem *p);
+
+/* Load cases: F is n_cases x N (N = 3 (nx+1)(ny+1)(nz+1)), fixed is the
+ * concatenation of the constrained DOFs of each case, n_fixed[c] entries for
+ * case c.  Replaces LoadCase.get_force_vector / get_constrained_dofs
+ * (loads.py:125-156) and the F / fixed_dofs arguments of TopologyOptimizer::run.
+ * A DOF index outside [0, N) -> AM_ERR_DOF_OUT_OF_RANGE. */
+am_status am_problem_set_loads(am_problem *p, int n_cases, const double *F,
+                               const int64_t *fixed, const int64_t *n_fixed);
+
+/* y = K(rho) u for the unconstrained operator (the assembled K of
+ * GlobalAssembler::assemble global_assembler.cpp:61-222 / fem.py:175-248, applied
+ * matrix-free).  precision AM_PREC_FP64 or AM_PREC_MIXED (FP32 K*u). */
+am_status am_ku_apply(am_problem *p, const am_simp_config *cfg, const double *rho,
+                      const double *u, double *y, int precision);
+
+/* Solves K(rho) u = F_case with the constrained and orphan DOFs eliminated
+ * (LinearSolver::solveWithBCs linear_solver.cpp:186-203; solve_fem fem.py:251-325).
+ * u_out (nullable) receives u in the reference DOF order. */
+am_status am_solve(am_problem *p, const am_simp_config *cfg, const double *rho, int load_case,
+                   double *u_out, am_solve_stats *stats);
+
+/* Element energies ce = u_e^T KE u_e, sensitivities dc = -p rho^(p-1) ce (CPP:
+ * every element, topology_optimizer.cpp:126-161; PY: design elements only,
+ * topopt.py:158-198) and the compliance sum_e scale_e ce (fem.py:328-383). */
+am_status am_sensitivities(am_problem *p, const am_simp_config *cfg, const double *rho,
+                           const double *u, double *dc, double *ce, double *compliance);
+
+/* Filters.  which = 0: C++ sensitivity filter sum w rho dc / sum w rho
+ * (topology_optimizer.cpp:60-119,168-198), x = dc, rho used;
+ * which = 1: Python normalised cone convolution, reflect boundary
+ * (topopt.py:135-156), rho ignored. */
+am_status am_filter(am_problem *p, const am_simp_config *cfg, int which, const double *x,
+                    const double *rho, double *out);
+
+/* OC update of the chosen variant (topology_optimizer.cpp:205-287 /
+ * topopt.py:200-264).  design[e] != 0 marks design elements.  Outputs the new
+ * density, max |change| and the bisection pass count. */
+am_status am_oc_update(am_problem *p, const am_simp_config *cfg, const double *rho,
+                       const double *dc, const uint8_t *design, double *rho_new,
+                       double *max_change, int *passes);
+
+/* Full SIMP run (TopologyOptimizer::run topology_optimizer.cpp:391-520 /
+ * SIMPOptimizer.run topopt.py:266-411).  rho0 (nullable: volume_fraction
+ * everywhere, CPP keeps fixed / void cells at 1 / rho_min) in cfg->layout.
+ * Histories need room for cfg->max_iterations entries; change_hist nullable. */
+am_status am_simp_run(am_problem *p, const am_simp_config *cfg, const double *rho0,
+                      double *rho_out, double *compliance_hist, double *volume_hist,
+                      double *change_hist, int *iterations, int *converged);
+
+/* Stepwise form of the same loop on device-resident state:
+ * am_simp_begin uploads rho0 and builds the design mask / filter;
+ * am_simp_step runs one iteration (TopologyOptimizer::runIteration
+ * topology_optimizer.cpp:294-384); am_simp_get_density downloads rho. */
+am_status am_simp_begin(am_problem *p, const am_simp_config *cfg, const double *rho0);
+am_status am_simp_step(am_problem *p, am_iteration_result *res);
+am_status am_simp_get_density(am_problem *p, double *rho_out);
+
+/* ---- measurement (no counterpart in the reference, whose timers are the
+ * std::chrono phase times of IterationResult, topology_optimizer.hpp:65-74) ---- */
+
+/* Kernel launches this library has issued so far (CUDA-graph replays add the
+ * kernel nodes they contain). */
+long long am_launch_count(void);
+
+/* Times `reps` single launches of one kernel on the problem's stream with CUDA
+ * events (after at least one am_simp_step, on the state it left): which = 0 the
+ * fused FP32 PCG K*u, 1 the FP64 residual K*u, 2 the FP32 PCG vector update,
+ * 3 the plain FP32 K*u.  flush_l2 != 0 overwrites a 512 MB buffer before each
+ * launch so the kernel reads from HBM.  Solver state is restored afterwards. */
+am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
+
+/* Sizes of the device layout: reference node count, element count, the padded
+ * component stride of a device vector, and the K*u tile count. */
+am_status am_problem_layout(am_problem *p, long long *nodes, long long *elements, long long *vector_stride,
+                            int *ku_tiles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AM_GPU_H */

@@ -266,3 +266,24 @@ def simp_py(shape, h, E, nu, prm, grid, F_list, fixed_list):
                            _p(vh, _dp), _p(dh, _dp), ctypes.byref(conv))
     return dict(density=out.reshape(shape), compliance=ch[:it], volume=vh[:it], change=dh[:it],
                 iterations=it, converged=bool(conv.value))
+
+
+def baseline_sample(shape, prm, rho, F, fixed, pcg_iters=20):
+    """Times one C++-variant SIMP iteration of the CPU restatement (CSR assembly,
+    `pcg_iters` Jacobi-PCG iterations, sensitivities, filter, OC).  Returns
+    (times dict in seconds, threads)."""
+    L = lib()
+    if not hasattr(L, "_bs_set"):
+        L.orc_baseline_sample.argtypes = ([ctypes.c_int] * 3 + [ctypes.POINTER(SimpParams), _dp, _dp, _i64p,
+                                          ctypes.c_int64, ctypes.c_int, _dp])
+        L.orc_baseline_sample.restype = ctypes.c_int
+        L._bs_set = True
+    nx, ny, nz = shape
+    rho = _f64(rho).ravel()
+    F = _f64(F)
+    fixed = np.ascontiguousarray(fixed, dtype=np.int64)
+    t = np.zeros(6)
+    th = L.orc_baseline_sample(nx, ny, nz, ctypes.byref(prm), _p(rho, _dp), _p(F, _dp), _p(fixed, _i64p),
+                               fixed.size, int(pcg_iters), _p(t, _dp))
+    keys = ["assembly", "pcg_setup", "pcg_iteration", "sensitivities", "filter", "oc"]
+    return dict(zip(keys, t.tolist())), th

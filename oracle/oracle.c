@@ -708,3 +708,98 @@ int orc_simp_py(int nx, int ny, int nz, double h, double E, double nu,
     free(u); free(design); free(cons);
     return it;
 }
+
+static double wtime(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
+int orc_baseline_sample(int nx, int ny, int nz, const orc_simp_params *prm, const double *rho,
+                        const double *F, const int64_t *fixed, int64_t n_fixed, int pcg_iters,
+                        double *times) {
+    const int64_t nel = (int64_t)nx * ny * nz;
+    const int64_t N = 3 * (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+    double ke[576];
+    orc_ke(1.0, 0.3, 1.0, ke);
+    double *s = malloc(sizeof(double) * nel);
+    double *u = calloc(N, sizeof(double));
+    double *ce = malloc(sizeof(double) * nel);
+    double *dc = malloc(sizeof(double) * nel);
+    double *dcf = malloc(sizeof(double) * nel);
+    double *r2 = malloc(sizeof(double) * nel);
+    uint8_t *design = malloc(nel);
+    uint8_t *cons = malloc(N);
+    mark_fixed(N, fixed, n_fixed, cons);
+    int64_t nd = 0;
+    for (int64_t e = 0; e < nel; ++e) {
+        design[e] = (uint8_t)(rho[e] > prm->rho_min + 1e-6 && rho[e] < 0.99);
+        nd += design[e];
+    }
+    /* assembly */
+    double t0 = wtime();
+    orc_scales(0, nel, NULL, rho, prm->penalty, prm->E_min, prm->rho_min, 1.0, s);
+    const int64_t nnz = orc_csr_nnz(nx, ny, nz);
+    int64_t *rowptr = malloc(sizeof(int64_t) * (N + 1));
+    int32_t *col = malloc(sizeof(int32_t) * nnz);
+    double *val = malloc(sizeof(double) * nnz);
+    orc_csr_build(nx, ny, nz, ke, s, rowptr, col, val);
+    double t1 = wtime();
+    /* PCG: set-up (diagonal, initial residual) and `pcg_iters` iterations */
+    double *dinv = malloc(sizeof(double) * N), *r = malloc(sizeof(double) * N);
+    double *z = malloc(sizeof(double) * N), *p = malloc(sizeof(double) * N), *q = malloc(sizeof(double) * N);
+    orc_diag(nx, ny, nz, ke, s, dinv);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) {
+        const int fx = cons[i] || fabs(dinv[i]) < 1e-15;
+        dinv[i] = fx ? 0.0 : 1.0 / dinv[i];
+        r[i] = fx ? 0.0 : F[i];
+        z[i] = dinv[i] * r[i];
+        p[i] = z[i];
+    }
+    double rz = dot(N, r, z);
+    double t2 = wtime();
+    for (int it = 0; it < pcg_iters; ++it) {
+        orc_csr_spmv(N, rowptr, col, val, p, q);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; ++i)
+            if (cons[i]) q[i] = 0.0;
+        const double alpha = rz / dot(N, p, q);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; ++i) {
+            u[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+            z[i] = dinv[i] * r[i];
+        }
+        const double rzn = dot(N, r, z);
+        const double beta = rzn / rz;
+        rz = rzn;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; ++i) p[i] = z[i] + beta * p[i];
+        (void)dot(N, r, r);
+    }
+    double t3 = wtime();
+    orc_element_energy(nx, ny, nz, ke, u, ce);
+    for (int64_t e = 0; e < nel; ++e) dc[e] = -prm->penalty * pow(rho[e], prm->penalty - 1.0) * ce[e];
+    double t4 = wtime();
+    orc_filter_cpp(nx, ny, nz, prm->filter_radius, dc, rho, dcf);
+    double t5 = wtime();
+    memcpy(r2, rho, sizeof(double) * nel);
+    (void)orc_oc_cpp(nel, r2, dcf, design, nd, prm->volume_fraction, prm->move_limit, prm->rho_min, NULL);
+    double t6 = wtime();
+    times[0] = t1 - t0;
+    times[1] = t2 - t1;
+    times[2] = pcg_iters > 0 ? (t3 - t2) / pcg_iters : 0.0;
+    times[3] = t4 - t3;
+    times[4] = t5 - t4;
+    times[5] = t6 - t5;
+    free(s); free(u); free(ce); free(dc); free(dcf); free(r2); free(design); free(cons);
+    free(rowptr); free(col); free(val); free(dinv); free(r); free(z); free(p); free(q);
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

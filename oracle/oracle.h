@@ -141,6 +141,16 @@ int orc_simp_py(int nx, int ny, int nz, double h, double E, double nu,
                 double *rho_out, double *compliance_hist, double *volume_hist,
                 double *change_hist, int *converged);
 
+/* Timed sample of one C++-variant SIMP iteration of the CPU restatement, for the
+ * CPU baseline: CSR assembly of K (the reference re-assembles every iteration,
+ * topology_optimizer.cpp:309-315), `pcg_iters` Jacobi-PCG iterations on the CSR
+ * matrix, sensitivities, the C++ filter and the OC update.  times[0..5] =
+ * scales+assembly, PCG set-up, mean time of one PCG iteration, sensitivities,
+ * filter, OC (seconds).  Returns the OpenMP thread count used. */
+int orc_baseline_sample(int nx, int ny, int nz, const orc_simp_params *prm, const double *rho,
+                        const double *F, const int64_t *fixed, int64_t n_fixed, int pcg_iters,
+                        double *times);
+
 #ifdef __cplusplus
 }
 #endif

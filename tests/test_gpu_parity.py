@@ -1,0 +1,273 @@
+"""Parity of the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances (from the engine's accuracy contract):
+  FP64 K*u, filters, OC, sensitivities: <= 1e-12 relative / absolute
+  FP32 K*u: <= 2e-6 relative to max|y|
+  solves: displacement relative error <= 1e-6 against an FP64 tight solve
+  SIMP: per-iteration compliance <= 1e-6 relative, densities <= 1e-4 max-abs
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from am_ml_suite_gb300 import _native as nat
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 1, 1), (2, 3, 5), (7, 5, 4), (33, 9, 10), (31, 8, 17), (48, 24, 12)]
+
+
+def _random_case(shape, seed, with_grid=True):
+    rng = np.random.default_rng(seed)
+    grid = rng.choice(np.array([-1, 0, 0, 0, 1], np.int8), size=shape) if with_grid else np.zeros(shape, np.int8)
+    rho = rng.uniform(0.01, 1.0, size=shape)
+    return rng, grid, rho
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_ku_fp64_and_fp32(shape):
+    rng, grid, rho = _random_case(shape, 1)
+    nx, ny, nz = shape
+    N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    u = rng.normal(size=N)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=grid)
+    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9)
+    s = O.scales(1, rho.ravel(), grid.ravel(), 3.0, 1e-9, 0.0, 1.0)
+    ref = O.ku(shape, O.ke(), s, u)
+    y64 = p.ku(cfg, rho, u, nat.PREC_FP64)
+    y32 = p.ku(cfg, rho, u, nat.PREC_MIXED)
+    scale = max(np.abs(ref).max(), 1e-300)
+    assert np.abs(y64 - ref).max() <= 1e-13 * scale
+    assert np.abs(y32 - ref).max() <= 2e-6 * scale
+
+
+def test_ku_cpp_scale_rule():
+    """C++ rule: rho < rho_min skipped, relative E_min, grid ignored."""
+    shape = (9, 6, 5)
+    rng, _, rho = _random_case(shape, 2)
+    rho[rho < 0.2] = 1e-4
+    nx, ny, nz = shape
+    u = rng.normal(size=3 * (nx + 1) * (ny + 1) * (nz + 1))
+    p = nat.Problem(shape, 0.5, 2.0, 0.25)
+    cfg = nat.default_config(nat.VARIANT_CPP, E_min=1e-6, rho_min=1e-3)
+    s = O.scales(0, rho.ravel(), None, 3.0, 1e-6, 1e-3, 1.0)
+    ref = O.ku(shape, O.ke(2.0, 0.25, 0.5), s, u)
+    y = p.ku(cfg, rho, u, nat.PREC_FP64)
+    assert np.abs(y - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_ku_matches_reference_assembled_csr(golden):
+    shape = tuple(golden["ku_shape"])
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=golden["ku_grid"])
+    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9)
+    y = p.ku(cfg, golden["ku_rho"], golden["ku_u"], nat.PREC_FP64)
+    assert np.abs(y - golden["ku_y"]).max() <= 1e-13 * np.abs(golden["ku_y"]).max()
+
+
+def _cantilever(shape):
+    nx, ny, nz = shape
+    N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(N)
+    line = [nx * (ny + 1) * (nz + 1) + j * (nz + 1) + nz // 2 for j in range(ny + 1)]
+    F[3 * np.array(line) + 2] = -1.0 / len(line)
+    return F, fixed
+
+
+@pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
+def test_solve_matches_oracle(golden, precision):
+    shape = tuple(golden["solve_shape"])
+    grid = golden["solve_grid"]
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=grid)
+    p.set_loads([golden["solve_F"]], [golden["solve_fixed"]])
+    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9, precision=precision, cg_tol=1e-9, warm_start=0)
+    u, st = p.solve(cfg, golden["solve_rho"])
+    ref = golden["solve_u"]
+    assert st.converged and st.residual <= 1e-9
+    assert np.linalg.norm(u - ref) / np.linalg.norm(ref) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
+def test_solve_cfg1_simp_density(precision):
+    """48x24x12 cantilever at a SIMP-like density field, rel-res 1e-6."""
+    shape = (48, 24, 12)
+    rng = np.random.default_rng(5)
+    rho = np.clip(rng.uniform(0.0, 1.0, size=shape) ** 2, 0.01, 1.0)
+    F, fixed = _cantilever(shape)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, E_min=1e-9, rho_min=0.0, precision=precision, cg_tol=1e-6,
+                             warm_start=0)
+    u, st = p.solve(cfg, rho)
+    s = O.scales(0, rho.ravel(), None, 3.0, 1e-9, 0.0, 1.0)
+    ref, _, _ = O.pcg(shape, O.ke(), s, fixed, F, tol=1e-12)
+    assert st.converged and st.residual <= 1e-6
+    # relative residual 1e-6 bounds the displacement error by the conditioning;
+    # check the residual of the returned u with the oracle operator as well
+    r = F - O.ku(shape, O.ke(), s, u)
+    r[fixed] = 0.0
+    assert np.linalg.norm(r) / np.linalg.norm(F) <= 1.05e-6
+    assert abs(F @ u - F @ ref) / abs(F @ ref) <= 1e-6
+
+
+def test_sensitivities(golden):
+    shape = tuple(golden["oc_py_shape"])
+    grid = golden["oc_py_grid"]
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=grid)
+    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9, penalty=3.0)
+    dc, ce, c = p.sensitivities(cfg, golden["sens_rho"], golden["sens_u"])
+    ref = golden["sens_dc"].ravel()
+    assert np.abs(dc - ref).max() <= 1e-12 * np.abs(ref).max()
+    ce_ref = O.element_energy(shape, O.ke(), golden["sens_u"])
+    assert np.abs(ce - ce_ref).max() <= 1e-12 * ce_ref.max()
+
+
+@pytest.mark.parametrize("shape", [(7, 5, 4), (33, 9, 10), (2, 3, 5)])
+@pytest.mark.parametrize("r", [1.5, 2.5])
+def test_filters(shape, r):
+    rng = np.random.default_rng(7)
+    x = -rng.uniform(0, 3, size=shape)
+    rho = rng.uniform(0.01, 1, size=shape)
+    p = nat.Problem(shape)
+    for prec, tol in ((nat.PREC_FP64, 1e-12), (nat.PREC_MIXED, 2e-6)):
+        cfg = nat.default_config(nat.VARIANT_CPP, filter_radius=r, precision=prec)
+        out = p.filter(cfg, 0, x, rho)
+        ref = O.filter_cpp(shape, r, x, rho)
+        assert np.abs(out - ref).max() <= tol * np.abs(ref).max()
+        out = p.filter(cfg, 1, x)
+        ref = O.filter_py(shape, r, x)
+        assert np.abs(out - ref).max() <= tol * np.abs(ref).max()
+
+
+def test_filter_py_golden(golden):
+    for r in (1.5, 2.5):
+        x = golden[f"filter_py_r{r}_x"]
+        p = nat.Problem(x.shape)
+        out = p.filter(nat.default_config(nat.VARIANT_PY, filter_radius=r, precision=nat.PREC_FP64), 1, x)
+        assert np.abs(out - golden[f"filter_py_r{r}_y"].ravel()).max() < 1e-14
+
+
+@pytest.mark.parametrize("variant", [nat.VARIANT_CPP, nat.VARIANT_PY])
+def test_oc_fp64(variant):
+    shape = (17, 9, 6)
+    rng = np.random.default_rng(11)
+    rho = rng.uniform(0.02, 0.95, size=shape)
+    dc = -rng.uniform(0.0, 5.0, size=shape) * rho
+    design = rng.uniform(size=shape) < 0.8
+    p = nat.Problem(shape)
+    cfg = nat.default_config(variant, volume_fraction=0.3, move_limit=0.2, rho_min=0.01, precision=nat.PREC_FP64)
+    out, mc, passes = p.oc_update(cfg, rho, dc, design)
+    if variant == nat.VARIANT_CPP:
+        ref, rmc, rpasses = O.oc_cpp(rho, dc, design, 0.3, 0.2, 0.01)
+        assert mc == pytest.approx(rmc, abs=1e-12)
+    else:
+        ref, rpasses = O.oc_py(rho, dc, design, 0.3, 0.2, 0.01)
+    assert passes == rpasses
+    assert np.abs(out - ref).max() <= 1e-12
+    # mixed precision: double-float per-element update on the FP32 pipes
+    cfg.precision = nat.PREC_MIXED
+    out32, _, p32 = p.oc_update(cfg, rho, dc, design)
+    assert p32 == rpasses
+    assert np.abs(out32 - ref).max() <= 1e-12
+
+
+def test_oc_py_golden(golden):
+    grid = golden["oc_py_grid"]
+    p = nat.Problem(grid.shape)
+    cfg = nat.default_config(nat.VARIANT_PY, volume_fraction=0.3, move_limit=0.2, rho_min=0.01,
+                             precision=nat.PREC_FP64)
+    out, _, _ = p.oc_update(cfg, golden["oc_py_rho"], golden["oc_py_dc"], grid == 0)
+    assert np.abs(out - golden["oc_py_out"].ravel()).max() < 1e-14
+
+
+def test_simp_py_golden_history(golden):
+    """Python SIMP 8x4x4, 5 iterations: the reference's own history."""
+    shape = tuple(golden["simp_py_shape"])
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=np.zeros(shape, np.int8))
+    p.set_loads([golden["simp_py_F"]], [golden["simp_py_fixed"]])
+    cfg = nat.default_config(nat.VARIANT_PY, volume_fraction=0.3, filter_radius=1.5, max_iterations=5,
+                             convergence_tol=0.0, E_min=1e-9, precision=nat.PREC_FP64, cg_tol=1e-11)
+    r = p.simp_run(cfg)
+    assert r["iterations"] == 5
+    assert np.allclose(r["compliance"], golden["simp_py_compliance"], rtol=1e-8)
+    assert np.allclose(r["volume"], golden["simp_py_volume"], rtol=1e-10)
+    assert np.abs(r["density"] - golden["simp_py_density"].ravel()).max() < 1e-8
+
+
+def test_simp_py_two_load_cases(golden):
+    shape = tuple(golden["simp_py_shape"])
+    fx = golden["simp_py_fixed"]
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=np.zeros(shape, np.int8))
+    p.set_loads([golden["simp_py_F"], golden["simp_py2_F2"]], [fx, fx])
+    cfg = nat.default_config(nat.VARIANT_PY, volume_fraction=0.35, filter_radius=1.5, max_iterations=3,
+                             convergence_tol=0.0, E_min=1e-9, precision=nat.PREC_FP64, cg_tol=1e-11)
+    r = p.simp_run(cfg)
+    assert np.allclose(r["compliance"], golden["simp_py2_compliance"], rtol=1e-8)
+    assert np.abs(r["density"] - golden["simp_py2_density"].ravel()).max() < 1e-8
+
+
+@pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
+def test_simp_cpp_cfg1_vs_oracle(precision):
+    """Config 1 (48x24x12, E_min 1e-9, vf 0.3, rmin 1.5, move 0.2): 10 OC iterations,
+    per-iteration compliance <= 1e-6 relative and densities <= 1e-4 against the
+    FP64 oracle solved to 1e-12."""
+    shape = (48, 24, 12)
+    F, fixed = _cantilever(shape)
+    iters = 10
+    prm = O.make_params(volume_fraction=0.3, filter_radius=1.5, move_limit=0.2, rho_min=0.01, E_min=1e-9,
+                        convergence_tol=0.0, max_iterations=iters, cg_tol=1e-12, warm_start=1)
+    ref = O.simp_cpp(shape, 1.0, 1.0, 0.3, prm, np.full(shape, 0.3), F, fixed)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, volume_fraction=0.3, filter_radius=1.5, move_limit=0.2,
+                             rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=iters,
+                             precision=precision, cg_tol=1e-8)
+    r = p.simp_run(cfg, np.full(shape, 0.3))
+    assert r["iterations"] == iters
+    rel = np.abs(r["compliance"] - ref["compliance"]) / ref["compliance"]
+    assert rel.max() <= 1e-6, rel
+    assert np.abs(r["density"] - ref["density"].ravel()).max() <= 1e-4
+
+
+def test_errors():
+    with pytest.raises(nat.AmError) as e:
+        nat.Problem((0, 2, 2))
+    assert e.value.name == "AM_ERR_INVALID_ARG"
+    p = nat.Problem((2, 2, 2))
+    N = p.N
+    with pytest.raises(nat.AmError) as e:
+        p.set_loads([np.zeros(N)], [np.array([N + 5])])
+    assert e.value.name == "AM_ERR_DOF_OUT_OF_RANGE"
+    with pytest.raises(nat.AmError) as e:
+        p.simp_step()
+    assert e.value.name == "AM_ERR_INVALID_ARG"
+    F = np.zeros(N)
+    F[-1] = np.nan
+    with pytest.raises(nat.AmError) as e:
+        p.set_loads([F], [np.array([0])])
+    assert e.value.name == "AM_ERR_NAN_DETECTED"
+
+
+def test_zero_load_and_all_void():
+    shape = (3, 3, 3)
+    p = nat.Problem(shape, grid=np.full(shape, -1, np.int8))
+    N = p.N
+    F = np.zeros(N)
+    F[-1] = 1.0
+    p.set_loads([F], [np.arange(3)])
+    cfg = nat.default_config(nat.VARIANT_PY, precision=nat.PREC_FP64)
+    u, st = p.solve(cfg, np.full(shape, 0.5))
+    # every DOF is an orphan -> no free DOF -> u = 0 (fem.py:287-289)
+    assert np.all(u == 0.0) and st.converged
+
+
+def test_determinism():
+    shape = (33, 9, 10)
+    rng, grid, rho = _random_case(shape, 3)
+    u = rng.normal(size=3 * 34 * 10 * 11)
+    p = nat.Problem(shape, grid=grid)
+    cfg = nat.default_config(nat.VARIANT_PY)
+    a = p.ku(cfg, rho, u, nat.PREC_FP64)
+    b = p.ku(cfg, rho, u, nat.PREC_FP64)
+    assert np.array_equal(a, b)
