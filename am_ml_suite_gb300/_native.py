@@ -68,6 +68,7 @@ class SolveStats(ctypes.Structure):
         ("solve_time_s", ctypes.c_double),
         ("max_displacement", ctypes.c_double),
         ("min_displacement", ctypes.c_double),
+        ("fp64_iterations", ctypes.c_int),
     ]
 
 
@@ -86,6 +87,7 @@ class IterationResult(ctypes.Structure):
         ("solve_time_s", ctypes.c_double),
         ("sensitivity_time_s", ctypes.c_double),
         ("update_time_s", ctypes.c_double),
+        ("solver_fp64_iterations", ctypes.c_int),
     ]
 
 
@@ -299,7 +301,7 @@ class Problem:
                                      ctypes.byref(mn)), "am_bench_kernel")
         return avg.value, mn.value
 
-    def layout(self):
+    def layout_info(self):
         n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
         t = ctypes.c_int(0)
         check(load().am_problem_layout(self.handle, ctypes.byref(n), ctypes.byref(e), ctypes.byref(cs),

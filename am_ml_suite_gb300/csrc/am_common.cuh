@@ -43,7 +43,10 @@ struct Modal {
 struct Scalars {
     // PCG
     double rz, rr, pq, alpha, beta, thr;
-    int it, maxit, done, status;      // status: 0 ok, 1 converged, 2 max it, 3 breakdown, 4 nan
+    double rz_prev;     // r.z of the previous iteration (beta after a residual replacement)
+    double thr_update;  // mixed precision: recursive |r|^2 that triggers a reliable update
+    int it, maxit, done, status;      // status: 0 ok, 1 converged, 2 max it, 3 breakdown, 4 nan,
+                                      // 5 reliable update due
     // residual kernel results
     double res_rr, res_rz, energy;
     // OC bisection
@@ -52,11 +55,14 @@ struct Scalars {
     double oc_change, oc_volume;
     // sensitivities
     double comp_fu, comp_energy;
+    // outer flexible CG (FP64): z.r, z.q, alpha, beta, p.q, r.r
+    double o_zr, o_zq, o_alpha, o_beta, o_pq, o_rr;
+    int o_status, pad1;
     // last-block counters (one per kernel family so overlapping uses never clash)
-    unsigned int cnt_ku, cnt_upd, cnt_oc, cnt_misc;
+    unsigned int cnt_ku, cnt_upd, cnt_oc, cnt_misc, cnt_fcg, pad2;
 };
 
-enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4 };
+enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4, ST_UPDATE = 5 };
 
 // Double-float accumulator: an unevaluated sum hi + lo of two floats.  Products of
 // FP32 operands are added exactly (FMA error term) and the running sum keeps ~48

@@ -26,6 +26,12 @@ am_status fail(am_status s, const std::string &msg) {
     return s;
 }
 
+}  // namespace
+
+void amk::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+namespace {
+
 #define CK(call)                                                                            \
     do {                                                                                    \
         cudaError_t e_ = (call);                                                            \
@@ -283,10 +289,9 @@ am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
     const long long launches_before = launch_count();
     CK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < P->chunk; ++k) {
-        T *pin = (k & 1) ? pb : pa;
-        T *pout = (k & 1) ? pa : pb;
-        cudaError_t e1 = ku_pcg<T>(K, P->L, M, s, pin, r, dinv, P->mask.p, q, pout, P->partial.p, P->S, P->st);
-        cudaError_t e2 = pcg_update<T>(P->L, x, r, pout, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
+        // the p ping-pong member is chosen on the device from the parity of S->it
+        cudaError_t e1 = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
+        cudaError_t e2 = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
         if (e1 != cudaSuccess || e2 != cudaSuccess) {
             cudaStreamEndCapture(P->st, &g);
             if (g) cudaGraphDestroy(g);
@@ -324,7 +329,7 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
 }
 
 struct SolveOut {
-    int iterations = 0, outer = 0, converged = 0;
+    int iterations = 0, outer = 0, converged = 0, fp64_iterations = 0;
     double residual = 0.0, time_s = 0.0;
 };
 
@@ -355,7 +360,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         CK(cudaMemcpyAsync(P->xw64.p, C.x64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p,
                     P->r64.p, nullptr, P->partial.p, P->S, P->st));
-        CK(pcg_start<double>(P->L, P->r64.p, P->dinv64.p, tol, bnorm2, maxit, P->partial.p, P->S,
+        CK(pcg_start<double>(P->L, P->r64.p, P->dinv64.p, tol * tol * bnorm2, 0.0, maxit, 0, P->partial.p, P->S,
                              P->nblocks_vec, P->st));
         int its = 0, stt = 0;
         CKS(run_pcg<double>(P, &its, &stt));
@@ -370,8 +375,15 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         o.converged = (stt == ST_CONVERGED) ? 1 : 0;
         if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the PCG iteration");
     } else {
-        const int max_outer = c.max_outer > 0 ? c.max_outer : 50;
-        const double inner = c.inner_tol > 0.0 ? c.inner_tol : 1e-4;
+        // Mixed precision: flexible CG in FP64 (FP64 K*u, vectors and dot
+        // products, so the accepted iterate has the energy-norm quality of FP64 CG
+        // at the same residual) preconditioned by an FP32 Jacobi-PCG inner solve
+        // z = M(r) that reduces its residual by inner_tol (or stops at its cap).
+        CKS(ensure_vectors(P, true));
+        const int max_outer = c.max_outer > 0 ? c.max_outer : 200;
+        const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.1;
+        const int inner_cap = std::max(50, maxit / 4);
+        CK(cudaMemsetAsync(&P->S->o_status, 0, sizeof(int), P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
                     want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
         CKS(sync_scalars(P));
@@ -379,32 +391,50 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         int total = 0, outer = 0;
         bool nan = !std::isfinite(rel);
         while (!nan && rel > tol && outer < max_outer && total < maxit) {
+            // z = M(r): FP32 PCG on K z = r from zero
             CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
-            // inner target: the requested reduction, but no further than needed
-            const double want = std::max(inner, 0.5 * tol / rel);
-            CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, want, 0.0, maxit - total, P->partial.p, P->S,
-                                P->nblocks_vec, P->st));
+            CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, -(inner_red * inner_red), 0.0,
+                                std::min(inner_cap, maxit - total), 0, P->partial.p, P->S, P->nblocks_vec, P->st));
             int its = 0, stt = 0;
             CKS(run_pcg<float>(P, &its, &stt));
-            total += its;
-            ++outer;
             if (stt == ST_NAN) {
                 nan = true;
                 break;
             }
-            CK(dc_accumulate(P->L, C.x64.p, P->x32.p, P->S, P->nblocks_vec, P->st));
-            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p,
-                        P->r64.p, want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+            total += its;
+            // outer step
+            CK(fcg_dots(P->L, P->x32.p, P->r64.p, P->q64v.p, outer == 0 ? 1 : 0, P->partial.p, P->S,
+                        P->nblocks_vec, P->st));
+            CK(fcg_direction(P->L, P->x32.p, P->p64a.p, P->S, P->nblocks_vec, P->st));
+            CK(ku_dot(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p, P->S,
+                      P->st));
+            CK(fcg_update(P->L, C.x64.p, P->r64.p, P->p64a.p, P->q64v.p, P->partial.p, P->S, P->nblocks_vec,
+                          P->st));
             CKS(sync_scalars(P));
-            const double nrel = std::sqrt(P->Sh->res_rr / bnorm2);
-            if (!std::isfinite(nrel)) {
+            ++outer;
+            if (P->Sh->o_status == ST_NAN || !std::isfinite(P->Sh->o_rr)) {
                 nan = true;
                 break;
             }
-            if (its == 0 && nrel >= rel) break;  // no progress possible
-            rel = nrel;
+            rel = std::sqrt(P->Sh->o_rr / bnorm2);
+            if (c.verbose >= 2)
+                std::printf("  outer %d: inner %d (total %d) rel-res %.3e\n", outer, its, total, rel);
+            if (rel <= tol) {
+                // accept on the recomputed FP64 residual (and element energies)
+                CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p,
+                            P->r64.p, want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+                CKS(sync_scalars(P));
+                rel = std::sqrt(P->Sh->res_rr / bnorm2);
+            }
         }
         if (nan) return fail(AM_ERR_NAN_DETECTED, "NaN in the mixed-precision solve");
+        if (want_ce && rel > tol) {
+            // not converged: element energies of the returned iterate
+            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
+                        P->ce.p, P->partial.p, P->S, P->st));
+            CKS(sync_scalars(P));
+            rel = std::sqrt(P->Sh->res_rr / bnorm2);
+        }
         o.iterations = total;
         o.outer = outer;
         o.residual = rel;
@@ -536,8 +566,8 @@ void am_simp_config_default(am_simp_config *c, int variant) {
     c->cg_tol = 1e-6;
     c->cg_max_iterations = 20000;
     c->warm_start = 1;
-    c->inner_tol = 1e-4;
-    c->max_outer = 50;
+    c->inner_tol = 0.1;
+    c->max_outer = 200;
     c->layout = AM_LAYOUT_ZFASTEST;
     c->verbose = 0;
 }
@@ -762,6 +792,7 @@ am_status am_solve(am_problem *P, const am_simp_config *cfg, const double *rho, 
         stats->residual = o.residual;
         stats->converged = o.converged;
         stats->solve_time_s = o.time_s;
+        stats->fp64_iterations = o.fp64_iterations;
         stats->max_displacement = 0.0;
         stats->min_displacement = 0.0;
         if (u_out) {
@@ -910,8 +941,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     const double *rho_asm = P->rho.p;
     if (c.variant == AM_VARIANT_PY) {
         // density pre-filter + clip (topopt.py:302-303)
-        CK(f64 ? filter_py<double>(P->L, taps_of(P), P->rho.p, nullptr, P->rho_f.p, 1, c.rho_min, P->st)
-               : filter_py<float>(P->L, taps_of(P), P->rho.p, nullptr, P->rho_f.p, 1, c.rho_min, P->st));
+        CK(filter_py<double>(P->L, taps_of(P), P->rho.p, nullptr, P->rho_f.p, 1, c.rho_min, P->st));
         rho_asm = P->rho_f.p;
     }
     CKS(setup_operator(P, c, rho_asm));
@@ -919,7 +949,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     double t1 = now_s();
     R.assembly_time_s = t1 - t0;
     double comp = 0.0;
-    int total_its = 0, total_outer = 0, conv = 1;
+    int total_its = 0, total_outer = 0, total_fp64 = 0, conv = 1;
     double worst_res = 0.0;
     double t_solve = 0.0, t_sens = 0.0;
     for (int lc = 0; lc < (int)P->cases.size(); ++lc) {
@@ -930,6 +960,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
         CKS(solve_case(P, c, lc, true, o));
         total_its += o.iterations;
         total_outer += o.outer;
+        total_fp64 += o.fp64_iterations;
         conv = conv && o.converged;
         worst_res = std::max(worst_res, o.residual);
         double te = now_s();
@@ -951,14 +982,16 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     R.solver_outer_iterations = total_outer;
     R.solver_residual = worst_res;
     R.solver_converged = conv;
+    R.solver_fp64_iterations = total_fp64;
     double tu = now_s();
-    // filter (topology_optimizer.cpp:351 / topopt.py:363)
+    // filter (topology_optimizer.cpp:351 / topopt.py:363), FP64 in every mode: the
+    // OC bisection is discrete, so an FP32 filter's rounding can flip one of its
+    // late branch decisions and move the density by ~1e-4 relative; the filter is
+    // well under 1% of a step.
     if (c.variant == AM_VARIANT_CPP) {
-        CK(f64 ? filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st)
-               : filter_cpp<float>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));
+        CK(filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));
     } else {
-        CK(f64 ? filter_py<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, 2, 0.0, P->st)
-               : filter_py<float>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, 2, 0.0, P->st));
+        CK(filter_py<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, 2, 0.0, P->st));
     }
     // OC update
     CKS(run_oc(P, f64, c.variant, c.move_limit, c.rho_min, c.volume_fraction, P->n_design, P->rho.p, P->dcf.p,
@@ -1004,16 +1037,16 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
         CK(cudaEventRecord(e0, P->st));
         switch (which) {
             case 0:
-                CK(ku_pcg<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->r32.p, P->dinv32.p, P->mask.p,
-                                 P->q32v.p, P->p32b.p, P->partial.p, P->S, P->st));
+                CK(ku_pcg<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p,
+                                 P->mask.p, P->q32v.p, P->partial.p, P->S, P->st));
                 break;
             case 1:
                 CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->cases[0].x64.p, P->cases[0].F.p, P->dinv64.p,
                             P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
                 break;
             case 2:
-                CK(pcg_update<float>(P->L, P->x32.p, P->r32.p, P->p32b.p, P->q32v.p, P->dinv32.p, P->partial.p,
-                                     P->S, P->nblocks_vec, P->st));
+                CK(pcg_update<float>(P->L, P->x32.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p, P->dinv32.p,
+                                     P->partial.p, P->S, P->nblocks_vec, P->st));
                 break;
             case 3:
                 CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->q32v.p, P->st));

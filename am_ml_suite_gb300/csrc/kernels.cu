@@ -5,6 +5,7 @@
 
 #include "kernels.cuh"
 #include "ku.cuh"
+#include "ku2.cuh"
 
 namespace amk {
 
@@ -23,22 +24,45 @@ static inline cudaError_t counted(cudaError_t e) {
 // ============================================================================
 // K*u launch plans and launchers
 // ============================================================================
-KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint) {
+KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms) {
     KuLaunch K;
-    K.tx = 32;
-    K.ty = fp64 ? 4 : 8;
-    const long long cols = (long long)div_up(L.nx + 1, K.tx) * div_up(L.ny + 1, K.ty);
-    int tz = tz_hint;
-    if (tz <= 0) {
-        // enough tiles for ~4 waves of resident CTAs, but chunks of >= 8 planes
-        const long long want = 152LL * 8;
-        tz = (int)std::max<long long>(8, (long long)(L.nz + 1) * cols / want);
-        tz = std::min(tz, L.nz + 1);
+    int ctas_per_sm;
+    if (fp64) {
+        K.tx = 32;
+        K.ty = 4;
+        K.warps = 0;
+        ctas_per_sm = 3;
+    } else {
+        K.warps = 8;
+        K.tx = Ku2Shape<8>::TX;
+        K.ty = Ku2Shape<8>::TY;
+        ctas_per_sm = 2;
     }
-    K.tz = tz;
     K.tiles_x = div_up(L.nx + 1, K.tx);
     K.tiles_y = div_up(L.ny + 1, K.ty);
-    K.tiles_z = div_up(L.nz + 1, K.tz);
+    const long long cols = (long long)K.tiles_x * K.tiles_y;
+    const int planes = L.nz + 1;
+    int tz = tz_hint;
+    if (tz <= 0) {
+        // time ~ waves x (planes per tile + 1 halo layer); pick the z chunking
+        // that minimises it (chunks of >= 4 planes)
+        const long long slots = (long long)sms * ctas_per_sm;
+        double best = 1e300;
+        tz = planes;
+        for (int chunks = 1; chunks <= planes; ++chunks) {
+            const int t = div_up(planes, chunks);
+            if (t < 4 && chunks > 1) break;
+            const long long tiles = cols * div_up(planes, t);
+            const double waves = (double)div_up(tiles, slots);
+            const double cost = waves * (t + 1);
+            if (cost < best - 1e-9) {
+                best = cost;
+                tz = t;
+            }
+        }
+    }
+    K.tz = std::min(std::max(tz, 1), planes);
+    K.tiles_z = div_up(planes, K.tz);
     return K;
 }
 
@@ -63,6 +87,8 @@ cudaError_t ku_init_attributes() {
     AMK_ATTR(double, 32, 4, KU_PLAIN)
     AMK_ATTR(double, 32, 4, KU_PCG)
     AMK_ATTR(double, 32, 4, KU_RESID)
+    AMK_ATTR(double, 32, 4, KU_DOT)
+    AMK_ATTR(double, 32, 8, KU_DOT)
 #undef AMK_ATTR
     return cudaSuccess;
 }
@@ -86,9 +112,33 @@ static cudaError_t dispatch_ku(const KuLaunch &K, KuArgs<T> &a, cudaStream_t st)
     return cudaErrorInvalidValue;
 }
 
+template <int MODE>
+static cudaError_t launch_ku2(const KuLaunch &K, Ku2Args &a, cudaStream_t st) {
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tiles_z = K.tiles_z;
+    a.tz = K.tz;
+    if (K.warps == 8) {
+        ku2_kernel<8, MODE><<<K.ntiles(), 256, 0, st>>>(a);
+        return counted(cudaGetLastError());
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <typename T>
 cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
                      T *y, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (K.warps > 0) {
+            Ku2Args a{};
+            a.L = L;
+            a.M = M;
+            a.s = s;
+            a.u = u;
+            a.y = y;
+            return launch_ku2<KU_PLAIN>(K, a, st);
+        }
+    }
     KuArgs<T> a{};
     a.L = L;
     a.M = M;
@@ -99,19 +149,36 @@ cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, cons
 }
 
 template <typename T>
-cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s,
-                   const T *p_prev, const T *r, const T *dinv, const uint8_t *mask, T *q, T *p_out,
-                   double *partial, Scalars *S, cudaStream_t st) {
+cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, T *pa, T *pb,
+                   const T *r, const T *dinv, const uint8_t *mask, T *q, double *partial, Scalars *S,
+                   cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (K.warps > 0) {
+            Ku2Args a{};
+            a.L = L;
+            a.M = M;
+            a.s = s;
+            a.pa = pa;
+            a.pb = pb;
+            a.r = r;
+            a.dinv = dinv;
+            a.mask = mask;
+            a.y = q;
+            a.partial = partial;
+            a.S = S;
+            return launch_ku2<KU_PCG>(K, a, st);
+        }
+    }
     KuArgs<T> a{};
     a.L = L;
     a.M = M;
     a.s = s;
-    a.u = p_prev;
+    a.pa = pa;
+    a.pb = pb;
     a.r = r;
     a.dinv = dinv;
     a.mask = mask;
     a.y = q;
-    a.p_out = p_out;
     a.partial = partial;
     a.S = S;
     return dispatch_ku<T, KU_PCG>(K, a, st);
@@ -136,49 +203,116 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
     return dispatch_ku<double, KU_RESID>(K, a, st);
 }
 
+cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
+                   const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st) {
+    KuArgs<double> a{};
+    a.L = L;
+    a.M = M;
+    a.s = s;
+    a.u = p;
+    a.mask = mask;
+    a.y = q;
+    a.partial = partial;
+    a.S = S;
+    return dispatch_ku<double, KU_DOT>(K, a, st);
+}
+
 template cudaError_t ku_plain<float>(const KuLaunch &, const Layout &, const Modal<float> &,
                                      const float *, const float *, float *, cudaStream_t);
 template cudaError_t ku_plain<double>(const KuLaunch &, const Layout &, const Modal<double> &,
                                       const double *, const double *, double *, cudaStream_t);
-template cudaError_t ku_pcg<float>(const KuLaunch &, const Layout &, const Modal<float> &,
-                                   const float *, const float *, const float *, const float *,
-                                   const uint8_t *, float *, float *, double *, Scalars *,
-                                   cudaStream_t);
-template cudaError_t ku_pcg<double>(const KuLaunch &, const Layout &, const Modal<double> &,
-                                    const double *, const double *, const double *,
-                                    const double *, const uint8_t *, double *, double *, double *,
-                                    Scalars *, cudaStream_t);
+template cudaError_t ku_pcg<float>(const KuLaunch &, const Layout &, const Modal<float> &, const float *,
+                                   float *, float *, const float *, const float *, const uint8_t *, float *,
+                                   double *, Scalars *, cudaStream_t);
+template cudaError_t ku_pcg<double>(const KuLaunch &, const Layout &, const Modal<double> &, const double *,
+                                    double *, double *, const double *, const double *, const uint8_t *,
+                                    double *, double *, Scalars *, cudaStream_t);
 
 // ============================================================================
 // PCG vector kernels
 // ============================================================================
 constexpr int VEC_THREADS = 256;
 
-// flat loop over the 3 component planes; dinv indexed by node = i mod cs
+// x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer the K*u
+// kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
 template <typename T>
 __global__ void __launch_bounds__(VEC_THREADS)
-    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
                       const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
                       Scalars *S) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag;
     if (S->done) return;
     const T alpha = (T)S->alpha;
+    const T *__restrict__ p = (S->it & 1) ? pa : pb;
     const long long cs = L.cs;
     Acc<T> a0, a1;
-    // one node per thread and step, its three component planes
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
-         n += (long long)gridDim.x * blockDim.x) {
-        const T d = dinv[n];
+    if constexpr (std::is_same<T, float>::value) {
+        // four nodes per thread and step (cs is a multiple of 64, rows 16-byte
+        // aligned): all 13 vector loads are issued before the 6 stores
+        const long long n4 = cs / 4;
+        for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4;
+             k += (long long)gridDim.x * blockDim.x) {
+            const float4 d = __ldg(reinterpret_cast<const float4 *>(dinv) + k);
+            float4 xv[3], rv[3], pv[3], qv[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const long long i = n + c * cs;
-            const T xi = x[i] + alpha * p[i];
-            const T ri = r[i] - alpha * q[i];
-            x[i] = xi;
-            r[i] = ri;
-            a0.add_prod(ri, ri);
-            a1.add_prod(ri, d * ri);
+            for (int c = 0; c < 3; ++c) {
+                const long long i = k + c * n4;
+                xv[c] = reinterpret_cast<const float4 *>(x)[i];
+                rv[c] = reinterpret_cast<const float4 *>(r)[i];
+                pv[c] = __ldg(reinterpret_cast<const float4 *>(p) + i);
+                qv[c] = __ldg(reinterpret_cast<const float4 *>(q) + i);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                xv[c].x = fmaf(alpha, pv[c].x, xv[c].x);
+                xv[c].y = fmaf(alpha, pv[c].y, xv[c].y);
+                xv[c].z = fmaf(alpha, pv[c].z, xv[c].z);
+                xv[c].w = fmaf(alpha, pv[c].w, xv[c].w);
+                rv[c].x = fmaf(-alpha, qv[c].x, rv[c].x);
+                rv[c].y = fmaf(-alpha, qv[c].y, rv[c].y);
+                rv[c].z = fmaf(-alpha, qv[c].z, rv[c].z);
+                rv[c].w = fmaf(-alpha, qv[c].w, rv[c].w);
+                a0.add_prod(rv[c].x, rv[c].x);
+                a0.add_prod(rv[c].y, rv[c].y);
+                a0.add_prod(rv[c].z, rv[c].z);
+                a0.add_prod(rv[c].w, rv[c].w);
+                a1.add_prod(rv[c].x, d.x * rv[c].x);
+                a1.add_prod(rv[c].y, d.y * rv[c].y);
+                a1.add_prod(rv[c].z, d.z * rv[c].z);
+                a1.add_prod(rv[c].w, d.w * rv[c].w);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long i = k + c * n4;
+                reinterpret_cast<float4 *>(x)[i] = xv[c];
+                reinterpret_cast<float4 *>(r)[i] = rv[c];
+            }
+        }
+    } else {
+        // one node per thread and step, its three component planes
+        for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
+             n += (long long)gridDim.x * blockDim.x) {
+            const T d = dinv[n];
+            T xv[3], rv[3], pv[3], qv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long i = n + c * cs;
+                xv[c] = x[i];
+                rv[c] = r[i];
+                pv[c] = p[i];
+                qv[c] = q[i];
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long i = n + c * cs;
+                const T xi = xv[c] + alpha * pv[c];
+                const T ri = rv[c] - alpha * qv[c];
+                x[i] = xi;
+                r[i] = ri;
+                a0.add_prod(ri, ri);
+                a1.add_prod(ri, d * ri);
+            }
         }
     }
     double v[2] = {a0.value(), a1.value()};
@@ -194,39 +328,48 @@ __global__ void __launch_bounds__(VEC_THREADS)
         const double rr = tot[0], rz = tot[1];
         S->it += 1;
         S->rr = rr;
+        S->rz_prev = S->rz;
+        S->beta = (S->rz != 0.0) ? rz / S->rz : 0.0;
+        S->rz = rz;
         if (!isfinite(rr) || !isfinite(rz)) {
             S->status = ST_NAN;
             S->done = 1;
         } else if (rr < S->thr) {
             S->status = ST_CONVERGED;
             S->done = 1;
+        } else if (rr < S->thr_update) {
+            S->status = ST_UPDATE;
+            S->done = 1;
         } else if (S->it >= S->maxit) {
             S->status = ST_MAXIT;
             S->done = 1;
         }
-        S->beta = (S->rz != 0.0) ? rz / S->rz : 0.0;
-        S->rz = rz;
         S->cnt_upd = 0;
     }
 }
 
 template <typename T>
-cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *p, const T *q, const T *dinv,
+cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st) {
-    pcg_update_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, p, q, dinv, partial, S);
+    pcg_update_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, pa, pb, q, dinv, partial, S);
     return counted(cudaGetLastError());
 }
-template cudaError_t pcg_update<float>(const Layout &, float *, float *, const float *,
-                                       const float *, const float *, double *, Scalars *, int,
-                                       cudaStream_t);
-template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *,
-                                        const double *, const double *, double *, Scalars *, int,
-                                        cudaStream_t);
+template cudaError_t pcg_update<float>(const Layout &, float *, float *, const float *, const float *,
+                                       const float *, const float *, double *, Scalars *, int, cudaStream_t);
+template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *, const double *,
+                                        const double *, const double *, double *, Scalars *, int, cudaStream_t);
 
+// (Re)start of the PCG sequence from the residual in r: r.r, r.z -> S.
+// restart == 0: fresh sequence (beta = 0, it = 0).  restart == 1: the residual
+// was replaced by a recomputed one; the search direction is kept and
+// beta = r.z / (r.z of the previous iteration).  restart == 2: iteration count
+// kept, beta = 0 (steepest-descent restart after a breakdown).  thr: |r|^2 that ends the
+// sequence; upd_factor: a reliable update is requested when |r|^2 falls below
+// upd_factor * (this |r|^2) (0 disables).  maxit caps S->it.
 template <typename T>
 __global__ void __launch_bounds__(VEC_THREADS)
-    pcg_start_kernel(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double tol,
-                     double bnorm2, int maxit, double *partial, Scalars *S) {
+    pcg_start_kernel(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double thr,
+                     double upd_factor, int maxit, int restart, double *partial, Scalars *S) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag;
     const long long cs = L.cs;
@@ -252,11 +395,19 @@ __global__ void __launch_bounds__(VEC_THREADS)
     reduce_partials<2>(partial, gridDim.x, 2, tot, red);
     if (threadIdx.x == 0) {
         S->rr = tot[0];
+        if (restart == 1) {
+            S->beta = (S->rz_prev > 0.0) ? tot[1] / S->rz_prev : 0.0;
+        } else if (restart == 2) {
+            S->beta = 0.0;
+        } else {
+            S->beta = 0.0;
+            S->it = 0;
+            S->rz_prev = 0.0;
+        }
         S->rz = tot[1];
-        S->thr = tol * tol * (bnorm2 > 0.0 ? bnorm2 : tot[0]);
-        S->beta = 0.0;
+        S->thr = thr >= 0.0 ? thr : -thr * tot[0];  // negative: relative to this |r|^2
+        S->thr_update = upd_factor * tot[0];
         S->alpha = 0.0;
-        S->it = 0;
         S->maxit = maxit;
         S->status = ST_RUNNING;
         S->done = 0;
@@ -266,7 +417,7 @@ __global__ void __launch_bounds__(VEC_THREADS)
         } else if (tot[0] < S->thr || tot[0] == 0.0) {
             S->status = ST_CONVERGED;
             S->done = 1;
-        } else if (maxit <= 0) {
+        } else if (S->it >= maxit) {
             S->status = ST_MAXIT;
             S->done = 1;
         }
@@ -275,23 +426,23 @@ __global__ void __launch_bounds__(VEC_THREADS)
 }
 
 template <typename T>
-cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double tol, double bnorm2,
-                      int maxit, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
-    pcg_start_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, r, dinv, tol, bnorm2, maxit, partial, S);
+cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,
+                      int restart, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    pcg_start_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, r, dinv, thr, upd_factor, maxit, restart, partial, S);
     return counted(cudaGetLastError());
 }
-template cudaError_t pcg_start<float>(const Layout &, const float *, const float *, double, double,
-                                      int, double *, Scalars *, int, cudaStream_t);
-template cudaError_t pcg_start<double>(const Layout &, const double *, const double *, double,
-                                       double, int, double *, Scalars *, int, cudaStream_t);
+template cudaError_t pcg_start<float>(const Layout &, const float *, const float *, double, double, int, int,
+                                      double *, Scalars *, int, cudaStream_t);
+template cudaError_t pcg_start<double>(const Layout &, const double *, const double *, double, double, int, int,
+                                       double *, Scalars *, int, cudaStream_t);
 
 __global__ void dc_inner_init_kernel(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
                                      float *__restrict__ x32, const Scalars *S) {
-    const double inv = S->res_rr > 0.0 ? 1.0 / sqrt(S->res_rr) : 0.0;
+    (void)S;
     const long long n = 3 * L.cs;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        r32[i] = (float)(r64[i] * inv);
+        r32[i] = (float)r64[i];
         x32[i] = 0.f;
     }
 }
@@ -303,12 +454,100 @@ cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float 
 
 __global__ void dc_accumulate_kernel(Layout L, double *__restrict__ x64, const float *__restrict__ x32,
                                      const Scalars *S) {
-    const double sc = sqrt(S->res_rr);
+    (void)S;
     const long long n = 3 * L.cs;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
-        x64[i] = fma(sc, (double)x32[i], x64[i]);
+        x64[i] += (double)x32[i];
 }
+// ---- outer flexible CG (FP64), preconditioned by an inner solve z = M(r) ------
+// Flexible CG with one stored direction and the Polak-Ribiere beta
+// (Notay, SIAM J. Sci. Comput. 22 (2000)): beta = z_new.(r_new - r_old) / z_old.r_old,
+// and r_new - r_old = -alpha q, so beta = -alpha z_new.q / z_old.r_old.
+__global__ void __launch_bounds__(VEC_THREADS)
+    fcg_dots_kernel(Layout L, const float *__restrict__ z, const double *__restrict__ r,
+                    const double *__restrict__ q, int first, double *partial, Scalars *S) {
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag;
+    const long long n = 3 * L.cs;
+    double zr = 0.0, zq = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double zi = (double)z[i];
+        zr = fma(zi, r[i], zr);
+        if (!first) zq = fma(zi, q[i], zq);
+    }
+    double v[2] = {zr, zq};
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = v[0];
+        partial[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last(&S->cnt_fcg, &last_flag)) return;
+    double tot[2];
+    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) {
+        S->o_beta = (first || S->o_zr == 0.0) ? 0.0 : -S->o_alpha * tot[1] / S->o_zr;
+        S->o_zr = tot[0];
+        S->o_zq = tot[1];
+        S->cnt_fcg = 0;
+    }
+}
+cudaError_t fcg_dots(const Layout &L, const float *z, const double *r, const double *q, int first,
+                     double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+    fcg_dots_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, z, r, q, first, partial, S);
+    return counted(cudaGetLastError());
+}
+
+// p = z + beta p
+__global__ void fcg_direction_kernel(Layout L, const float *__restrict__ z, double *__restrict__ p,
+                                     const Scalars *S) {
+    const double beta = S->o_beta;
+    const long long n = 3 * L.cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        p[i] = beta == 0.0 ? (double)z[i] : fma(beta, p[i], (double)z[i]);
+}
+cudaError_t fcg_direction(const Layout &L, const float *z, double *p, const Scalars *S, int nblocks,
+                          cudaStream_t st) {
+    fcg_direction_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, z, p, S);
+    return counted(cudaGetLastError());
+}
+
+// x += alpha p; r -= alpha q; r.r -> S->o_rr
+__global__ void __launch_bounds__(VEC_THREADS)
+    fcg_update_kernel(Layout L, double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
+                      const double *__restrict__ q, double *partial, Scalars *S) {
+    __shared__ double red[VEC_THREADS / 32];
+    __shared__ int last_flag;
+    const double alpha = S->o_alpha;
+    const long long n = 3 * L.cs;
+    double rr = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double pi = p[i], qi = q[i], xi = x[i], ri = r[i];
+        x[i] = fma(alpha, pi, xi);
+        const double rn = fma(-alpha, qi, ri);
+        r[i] = rn;
+        rr = fma(rn, rn, rr);
+    }
+    double v[1] = {rr};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v[0];
+    if (!arrive_last(&S->cnt_fcg, &last_flag)) return;
+    double tot[1];
+    reduce_partials<1>(partial, gridDim.x, 1, tot, red);
+    if (threadIdx.x == 0) {
+        S->o_rr = tot[0];
+        S->cnt_fcg = 0;
+    }
+}
+cudaError_t fcg_update(const Layout &L, double *x, double *r, const double *p, const double *q, double *partial,
+                       Scalars *S, int nblocks, cudaStream_t st) {
+    fcg_update_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, p, q, partial, S);
+    return counted(cudaGetLastError());
+}
+
 cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
                           int nblocks, cudaStream_t st) {
     dc_accumulate_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, x64, x32, S);

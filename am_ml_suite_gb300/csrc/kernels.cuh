@@ -11,45 +11,64 @@ namespace amk {
 // kernel launches issued so far (graph replays add their kernel-node count)
 long long launch_count();
 void count_launches(long long n);
+// detail message returned by am_last_error() on this thread
+void set_last_error(const char *msg);
 
-// ---- tiled K*u (ku.cuh) ----------------------------------------------------
+// ---- tiled K*u (ku.cuh: FP64 / generic, ku2.cuh: FP32 warp-row form) --------
 struct KuLaunch {
     int tx, ty;  // owned node columns per tile (one of the compiled shapes)
     int tz;      // node planes per tile
     int tiles_x, tiles_y, tiles_z;
+    int warps;   // > 0: FP32 warp-row kernel (ku2.cuh) with this many warps
     int ntiles() const { return tiles_x * tiles_y * tiles_z; }
 };
-KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint);
+// fp64: ku.cuh shape for FP64; otherwise the FP32 warp-row kernel.  tz_hint <= 0
+// picks the z chunking from a wave-quantisation cost model (resident CTAs per SM
+// `ctas_per_sm`, `sms` multiprocessors).
+KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms = 152);
 
 template <typename T>
 cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
                      T *y, cudaStream_t st);
-// q = mask(K p), p = dinv r + beta p_prev (beta from S), partial p.q -> S->alpha
+// p = dinv r + beta p_prev, q = mask(K p), partial p.q -> S->alpha.  p_prev / p are
+// the ping-pong pair (pa, pb) chosen by the parity of S->it.
 template <typename T>
-cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s,
-                   const T *p_prev, const T *r, const T *dinv, const uint8_t *mask, T *q, T *p_out,
-                   double *partial, Scalars *S, cudaStream_t st);
+cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, T *pa, T *pb,
+                   const T *r, const T *dinv, const uint8_t *mask, T *q, double *partial, Scalars *S,
+                   cudaStream_t st);
 // r = mask(f - K x) in FP64 with r.r, r.dinv.r -> S->res_rr / res_rz; optional ce.
 cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
                      const double *x, const double *f, const double *dinv, const uint8_t *mask,
                      double *r, double *ce, double *partial, Scalars *S, cudaStream_t st);
 
 // ---- PCG vector kernels ------------------------------------------------------
-// x += alpha p; r -= alpha q; rr, rz -> S (beta, convergence, iteration count)
+// x += alpha p; r -= alpha q (p = the pair member written this iteration);
+// rr, rz -> S (beta, stop tests: converged / reliable update due / max it)
 template <typename T>
-cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *p, const T *q, const T *dinv,
+cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st);
-// PCG start from r (already masked): rr, rz -> S; thr = tol^2 * bnorm2 (or * rr if
-// bnorm2 <= 0); beta = 0; it = 0; done if converged already.
+// (re)start from the residual r (already masked); see pcg_start_kernel
 template <typename T>
-cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double tol, double bnorm2,
-                      int maxit, double *partial, Scalars *S, int nblocks, cudaStream_t st);
-// r32 = r64 / sqrt(S->res_rr), x32 = 0 (inner start of the defect correction)
+cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,
+                      int restart, double *partial, Scalars *S, int nblocks, cudaStream_t st);
+// r32 = r64, x32 = 0 (reliable update: the FP32 sequence continues from the
+// recomputed FP64 residual)
 cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
                           const Scalars *S, int nblocks, cudaStream_t st);
-// x64 += sqrt(S->res_rr) * x32
+// x64 += x32
 cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
                           int nblocks, cudaStream_t st);
+// outer flexible CG (FP64) with an inner preconditioner output z (FP32):
+// z.r, z.q -> beta (first: 0) ; p = z + beta p ; q = mask(K p), p.q -> alpha ;
+// x += alpha p, r -= alpha q, r.r
+cudaError_t fcg_dots(const Layout &L, const float *z, const double *r, const double *q, int first,
+                     double *partial, Scalars *S, int nblocks, cudaStream_t st);
+cudaError_t fcg_direction(const Layout &L, const float *z, double *p, const Scalars *S, int nblocks,
+                          cudaStream_t st);
+cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
+                   const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st);
+cudaError_t fcg_update(const Layout &L, double *x, double *r, const double *p, const double *q, double *partial,
+                       Scalars *S, int nblocks, cudaStream_t st);
 
 // ---- set-up kernels ------------------------------------------------------------
 // element scales from a device density (internal layout).  variant 0 (CPP):

@@ -22,7 +22,10 @@
 
 namespace amk {
 
-enum { KU_PLAIN = 0, KU_PCG = 1, KU_RESID = 2 };
+// PLAIN: y = K u.  PCG: p = dinv r + beta p_prev, q = mask(K p), p.q.  RESID:
+// r = mask(f - K u) in FP64.  DOT: q = mask(K u) and u.q (the FP64 matvec of the
+// outer flexible CG).
+enum { KU_PLAIN = 0, KU_PCG = 1, KU_RESID = 2, KU_DOT = 3 };
 
 template <typename T>
 struct KuArgs {
@@ -34,6 +37,8 @@ struct KuArgs {
     const double *f;       // RESID: right-hand side (FP64)
     T *y;                  // PLAIN: K u ; PCG: q = K p ; RESID: r = f - K u
     T *p_out;              // PCG: p = dinv r + beta p_prev
+    T *pa, *pb;            // PCG ping-pong pair: iteration it reads p[it & 1], writes the other
+                           // (it = S->it, so a solve can stop and resume at any parity)
     const uint8_t *mask;   // per-node constrained bits (bit c = DOF component c)
     double *partial;       // per-tile partial sums (2 per tile)
     double *ce;            // RESID with energy: u_e^T KE u_e per owned element
@@ -167,7 +172,14 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
     const int z1 = min(z0 + A.tz, L.nz + 1);
     const long long cs = L.cs;
     T beta = T(0);
-    if (MODE == KU_PCG) beta = (T)A.S->beta;
+    if (MODE == KU_PCG) {
+        beta = (T)A.S->beta;
+        if (A.pa) {
+            const bool odd = (A.S->it & 1) != 0;
+            A.u = odd ? A.pb : A.pa;
+            A.p_out = odd ? A.pa : A.pb;
+        }
+    }
 
     auto stage = [&](int iz, int slot) {
         T *dst = us + slot * 3 * NS;
@@ -282,7 +294,7 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
                     for (int c = 0; c < 3; ++c) A.y[n + c * cs] = val[c];
                 } else {
                     const unsigned m = A.mask[n];
-                    if (MODE == KU_PCG) {
+                    if (MODE == KU_PCG || MODE == KU_DOT) {
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             const T q = ((m >> c) & 1u) ? T(0) : val[c];
@@ -301,7 +313,7 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
                     }
                 }
             }
-            if (MODE == KU_PCG) {
+            if (MODE == KU_PCG || MODE == KU_DOT) {
                 const T *pn = us + ((ez + 1) & 1) * 3 * NS + (ly + 1) * SX + (lx + 1);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) pcur[c] = pn[c * NS];
@@ -331,6 +343,15 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
                 S->alpha = 0.0;
             } else {
                 S->alpha = S->rz / pq;
+            }
+        } else if (MODE == KU_DOT) {
+            const double pq = tot[0];
+            S->o_pq = pq;
+            if (!(pq > 0.0) || !isfinite(pq)) {
+                S->o_status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+                S->o_alpha = 0.0;
+            } else {
+                S->o_alpha = S->o_zr / pq;
             }
         } else {
             S->res_rr = tot[0];

@@ -82,7 +82,7 @@ def build_workload(name):
 def simp_config(nat, W, max_iterations=100):
     return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
-                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=1e-4)
+                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=0.1)
 
 
 class ClockSampler:
@@ -248,7 +248,7 @@ def main():
     p.set_loads([W["F"]], [W["fixed"]])
     p.simp_begin(cfg, W["rho0"])
     warm = [p.simp_step() for _ in range(args.warmup)]
-    lay = p.layout()
+    lay = p.layout_info()
     if world > 1:
         import torch.distributed as dist
 

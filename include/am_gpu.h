@@ -64,9 +64,10 @@ enum { AM_LAYOUT_ZFASTEST = 0, AM_LAYOUT_XFASTEST = 1 };
 enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
 
 /* AM_PREC_FP64: every kernel in FP64 (the parity mode).
- * AM_PREC_MIXED: FP32 K*u and PCG inside an FP64 defect-correction loop; FP64 for
- *   dot products (double-float accumulation), alpha/beta, the outer residual
- *   r = f - K u, compliance and the OC volume sums. */
+ * AM_PREC_MIXED: FP64 flexible CG (outer K*u, vectors, dots) preconditioned by FP32
+ *   Jacobi PCG inner solves (FP32 K*u, double-float dot accumulation); the outer
+ *   residual r = f - K u, compliance, filter and the OC volume sums in FP64 (the OC
+ *   per-element update in double-float). */
 enum { AM_PREC_FP64 = 0, AM_PREC_MIXED = 1 };
 
 enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1 };
@@ -88,8 +89,9 @@ typedef struct am_simp_config {
     double cg_tol;            /* relative residual ||f - K u|| / ||f|| of every solve */
     int cg_max_iterations;    /* cap on (inner) PCG iterations per solve */
     int warm_start;           /* 1: each solve starts from the previous displacement */
-    double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve */
-    int max_outer;            /* MIXED: cap on defect-correction steps */
+    double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve that
+                                 preconditions the FP64 flexible CG (0.1 by default) */
+    int max_outer;            /* MIXED: cap on outer FP64 flexible-CG iterations per solve */
     int layout;               /* AM_LAYOUT_* of density arrays */
     int verbose;
 } am_simp_config;
@@ -103,6 +105,7 @@ typedef struct am_solve_stats {
     double solve_time_s;
     double max_displacement;
     double min_displacement;
+    int fp64_iterations;      /* MIXED: FP64 PCG iterations after the FP32 sequence stagnated */
 } am_solve_stats;
 
 /* IterationResult (topology_optimizer.hpp:65-74) plus the extra fields of this engine. */
@@ -120,6 +123,7 @@ typedef struct am_iteration_result {
     double solve_time_s;
     double sensitivity_time_s;
     double update_time_s;      /* filter + OC */
+    int solver_fp64_iterations; /* MIXED: FP64 continuation iterations (FP32 stagnation) */
 } am_iteration_result;
 
 typedef struct am_problem am_problem;
@@ -224,6 +228,7 @@ am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, doub
  * component stride of a device vector, and the K*u tile count. */
 am_status am_problem_layout(am_problem *p, long long *nodes, long long *elements, long long *vector_stride,
                             int *ku_tiles);
+
 
 #ifdef __cplusplus
 }
