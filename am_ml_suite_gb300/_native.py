@@ -125,6 +125,9 @@ SIGNATURES = {
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "am_problem_layout": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                          ctypes.POINTER(ctypes.c_longlong), _ip]),
+    # device pointers are passed as c_void_p
+    "am_residual_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _LIB = None

@@ -229,6 +229,38 @@ am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, doub
 am_status am_problem_layout(am_problem *p, long long *nodes, long long *elements, long long *vector_stride,
                             int *ku_tiles);
 
+/* ---- allocation-free residual (no counterpart in the reference) ----------------
+ * For callers that cannot allocate device memory once they are running -- code
+ * inside another framework's fixed memory pool, allocation-free real-time or
+ * certified loops, plugins whose host owns every buffer -- and so cannot use the
+ * handle API above (am_problem_create allocates a workspace).
+ *
+ * Computes, in FP64 on the current device, r = f - K(scale) u with the
+ * constrained components of r set to 0, and rr = |r|^2, for an nx*ny*nz grid of
+ * cubic hex8 elements of edge h and material (E0, nu).  Every argument is a
+ * caller-owned DEVICE buffer in the compact layout:
+ *   u, f, r : three component planes of (nx+1)(ny+1)(nz+1) nodes each, node
+ *             (ix,iy,iz) at (iz*(ny+1) + iy)*(nx+1) + ix of its plane;
+ *   scale   : nx*ny*nz element stiffness factors, element (ex,ey,ez) at
+ *             (ez*ny + ey)*nx + ex (0 removes an element);
+ *   mask    : one byte per node, bit c set = component c constrained;
+ *   rr      : one double.
+ * The call is asynchronous on `stream` (a cudaStream_t, NULL = default stream);
+ * results are ready when the stream reaches that point.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: its scratch (per-tile partial sums and
+ * a block of solver scalars, 512 KB in total) is a file-scope __device__ array
+ * present on every device that loads the library until the process exits.  The
+ * first call on a device looks up that array's device address with the device
+ * current (this may load the library's device code); make the first call on each
+ * device before any stream capture.  Every call shares the scratch and the
+ * previous call's contents remain in it, so calls whose executions overlap on the
+ * GPU (different streams, or host threads) race; the call clears what must start
+ * at zero.  Limit: ceil((nx+1)/32) * ceil((ny+1)/4) <= 32768 (for example
+ * 1023 x 4095 x any nz); larger grids return AM_ERR_SIZE_MISMATCH before any
+ * device work.  Errors are read with am_last_error(). */
+am_status am_residual_noalloc(int nx, int ny, int nz, double h, double E0, double nu, const double *scale,
+                              const double *u, const double *f, const uint8_t *mask, double *r, double *rr,
+                              void *stream);
 
 #ifdef __cplusplus
 }
