@@ -342,6 +342,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
     CKS(ensure_vectors(P, fp64));
     CK(C.x64.alloc(3 * (size_t)P->L.cs));
     if (!c.warm_start || !C.have_x) CK(cudaMemsetAsync(C.x64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
+    else CK(zero_masked(P->L, P->mask.p, C.x64.p, P->nblocks_vec, P->st));  // DOFs orphaned since the last solve
     C.have_x = true;
     double bnorm2 = 0.0;
     CKS(free_rhs_norm(P, lc, &bnorm2));
@@ -458,7 +459,8 @@ am_status run_oc(am_problem *P, bool f64, int variant, double move, double rho_m
     CK(oc_prepare(B, rho, dcf, move, f64, variant, P->S, P->st));
     for (int k = 0; k < 100; ++k)
         CK(oc_pass(B, design, f64, variant, rho_min, vf, n_design, P->partial.p, P->S, P->nblocks_vec, P->st));
-    CK(oc_final(B, design, f64, variant, rho_min, rho, rho_new, P->partial.p, P->S, P->nblocks_vec, P->st));
+    CK(oc_final(B, design, f64, variant, rho_min, rho, dcf, move, rho_new, P->partial.p, P->S, P->nblocks_vec,
+                P->st));
     CKS(sync_scalars(P));
     return AM_OK;
 }

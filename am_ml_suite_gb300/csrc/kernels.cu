@@ -452,13 +452,17 @@ cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float 
     return counted(cudaGetLastError());
 }
 
-__global__ void dc_accumulate_kernel(Layout L, double *__restrict__ x64, const float *__restrict__ x32,
-                                     const Scalars *S) {
-    (void)S;
-    const long long n = 3 * L.cs;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        x64[i] += (double)x32[i];
+// x = 0 on the constrained / orphan components (bit c of mask[n] set)
+__global__ void zero_masked_kernel(Layout L, const uint8_t *__restrict__ mask, double *__restrict__ x) {
+    const long long cs = L.cs;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)gridDim.x * blockDim.x) {
+        const unsigned m = mask[n];
+        if (!m) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if ((m >> c) & 1u) x[n + c * cs] = 0.0;
+    }
 }
 // ---- outer flexible CG (FP64), preconditioned by an inner solve z = M(r) ------
 // Flexible CG with one stored direction and the Polak-Ribiere beta
@@ -548,9 +552,8 @@ cudaError_t fcg_update(const Layout &L, double *x, double *r, const double *p, c
     return counted(cudaGetLastError());
 }
 
-cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
-                          int nblocks, cudaStream_t st) {
-    dc_accumulate_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, x64, x32, S);
+cudaError_t zero_masked(const Layout &L, const uint8_t *mask, double *x, int nblocks, cudaStream_t st) {
+    zero_masked_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, mask, x);
     return counted(cudaGetLastError());
 }
 
@@ -898,7 +901,6 @@ __device__ __forceinline__ float2 df_of(double x) {
     const float h = (float)x;
     return make_float2(h, (float)(x - (double)h));
 }
-__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
 __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
     const float p = a.x * b.x;
     float e = fmaf(a.x, b.x, -p);
@@ -1053,22 +1055,28 @@ cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int var
 }
 
 // Density of the last executed pass, max |change| and the design-mask mean.
+// The density is always formed in FP64 from rho and dc (the same a = rho sqrt(-dc)
+// and bounds as oc_prepare's FP64 terms): the clamped values rho_min, rho -/+ move
+// and 1 must come out exact, because the next stiffness skips elements with
+// rho < rho_min -- a double-float rho_min (48 bits) lands one ulp below it.  Only
+// the multiplier t comes from the (double-float or FP64) bisection passes.
 __global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const double *__restrict__ rho,
+                                                       const double *__restrict__ dc, double move,
                                                        double *__restrict__ rho_new) {
     __shared__ double red[2 * (256 / 32)];
     __shared__ int last_flag;
     Scalars *S = A.S;
     const double t = S->oc_t_last;
-    const float2 tdf = df_of(t), rmin = df_of(A.rho_min);
     double mc = 0.0, vs = 0.0, cnt = 0.0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
          e += (long long)gridDim.x * blockDim.x) {
         const double r0 = rho[e];
         double v = r0;
         if (A.design[e]) {
-            if (S->oc_pass == 0) v = r0;  // no pass ran (cannot happen with the reference bounds)
-            else if (A.fp64) v = oc_clamp<double>(A.B.a64[e] * t, A.B.lo64[e], A.B.hi64[e], A.rho_min, A.variant);
-            else v = df_to(oc_clamp_df(df_mul(A.B.a32[e], tdf), A.B.lo32[e], A.B.hi32[e], rmin, A.variant));
+            if (S->oc_pass > 0) {  // no pass ran: unchanged (cannot happen with the reference bounds)
+                const double a = r0 * sqrt(-dc[e]);
+                v = oc_clamp<double>(a * t, r0 - move, r0 + move, A.rho_min, A.variant);
+            }
             vs += v;
             cnt += 1.0;
         }
@@ -1097,9 +1105,10 @@ __global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const doubl
     }
 }
 cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min,
-                     const double *rho, double *rho_new, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
+                     const double *rho, const double *dc, double move, double *rho_new, double *partial, Scalars *S,
+                     int nblocks, cudaStream_t st) {
     OcPassArgs a{B, design, fp64, variant, rho_min, 0.0, 1.0, partial, S};
-    oc_final_kernel<<<nblocks, 256, 0, st>>>(a, rho, rho_new);
+    oc_final_kernel<<<nblocks, 256, 0, st>>>(a, rho, dc, move, rho_new);
     return counted(cudaGetLastError());
 }
 

@@ -55,9 +55,9 @@ cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, do
 // recomputed FP64 residual)
 cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
                           const Scalars *S, int nblocks, cudaStream_t st);
-// x64 += x32
-cudaError_t dc_accumulate(const Layout &L, double *x64, const float *x32, const Scalars *S,
-                          int nblocks, cudaStream_t st);
+// x = 0 on every component whose bit is set in the per-node mask (a warm start
+// keeps no value on constrained or orphan DOFs: the reference solution is 0 there)
+cudaError_t zero_masked(const Layout &L, const uint8_t *mask, double *x, int nblocks, cudaStream_t st);
 // outer flexible CG (FP64) with an inner preconditioner output z (FP32):
 // z.r, z.q -> beta (first: 0) ; p = z + beta p ; q = mask(K p), p.q -> alpha ;
 // x += alpha p, r -= alpha q, r.r
@@ -141,8 +141,10 @@ cudaError_t oc_prepare(const OcBuffers &B, const double *rho, const double *dc, 
 // one bisection pass: design volume at the current multiplier -> l1 / l2, stop test
 cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min, double vf,
                     double n_design, double *partial, Scalars *S, int nblocks, cudaStream_t st);
-// new density with the last pass's multiplier, max |change|, design-mask mean -> S
+// new density (FP64, from rho and dc) with the last pass's multiplier, max |change|,
+// design-mask mean -> S
 cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min,
-                     const double *rho, double *rho_new, double *partial, Scalars *S, int nblocks, cudaStream_t st);
+                     const double *rho, const double *dc, double move, double *rho_new, double *partial, Scalars *S,
+                     int nblocks, cudaStream_t st);
 
 }  // namespace amk

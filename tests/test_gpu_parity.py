@@ -89,6 +89,31 @@ def test_solve_matches_oracle(golden, precision):
 
 
 @pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
+def test_warm_start_onto_orphaned_nodes(precision):
+    """A warm-started solve after elements fell below rho_min (C++ rule: skipped)
+    returns 0 on the DOFs those elements orphaned, like a solve from zero and the
+    oracle: an orphan DOF has no stiffness, so the residual never sees a stale value
+    left there, but the element energies of the skipped elements read it."""
+    shape = (12, 6, 4)
+    F, fixed = _cantilever(shape)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, E_min=1e-9, rho_min=0.01, precision=precision, cg_tol=1e-10,
+                             warm_start=1)
+    p.solve(cfg, np.full(shape, 0.5))
+    rho = np.full(shape, 0.5)
+    rho[4:8, :, 2:] = 0.005          # skipped: the nodes strictly inside lose all stiffness
+    u, st = p.solve(cfg, rho)
+    s = O.scales(0, rho.ravel(), None, 3.0, 1e-9, 0.01, 1.0)
+    ref, _, _ = O.pcg(shape, O.ke(), s, fixed, F, tol=1e-13)
+    orphan = np.zeros((shape[0] + 1, shape[1] + 1, shape[2] + 1), bool)
+    orphan[5:8, :, 3:] = True
+    assert np.all(u.reshape(-1, 3)[orphan.ravel()] == 0.0)
+    assert st.converged
+    assert np.abs(u - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
 def test_solve_cfg1_simp_density(precision):
     """48x24x12 cantilever at a SIMP-like density field, rel-res 1e-6."""
     shape = (48, 24, 12)
@@ -165,11 +190,16 @@ def test_oc_fp64(variant):
         ref, rpasses = O.oc_py(rho, dc, design, 0.3, 0.2, 0.01)
     assert passes == rpasses
     assert np.abs(out - ref).max() <= 1e-12
-    # mixed precision: double-float per-element update on the FP32 pipes
+    # mixed precision: double-float bisection passes on the FP32 pipes; the density
+    # itself is formed in FP64, so with the same multiplier it is bit-identical and
+    # the clamped values (rho_min, rho -/+ move, 1) are exact
     cfg.precision = nat.PREC_MIXED
     out32, _, p32 = p.oc_update(cfg, rho, dc, design)
     assert p32 == rpasses
     assert np.abs(out32 - ref).max() <= 1e-12
+    assert np.array_equal(out32, out)
+    assert out32[design.ravel()].min() >= 0.01
+    assert np.any(out32 == 0.01)
 
 
 def test_oc_py_golden(golden):
