@@ -123,6 +123,7 @@ SIGNATURES = {
     "am_simp_get_density": (ctypes.c_int, [_vp, _dp]),
     "am_launch_count": (ctypes.c_longlong, []),
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "am_problem_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "am_problem_layout": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                          ctypes.POINTER(ctypes.c_longlong), _ip]),
     # device pointers are passed as c_void_p
@@ -303,6 +304,12 @@ class Problem:
         check(load().am_bench_kernel(self.handle, int(which), int(reps), int(flush_l2), ctypes.byref(avg),
                                      ctypes.byref(mn)), "am_bench_kernel")
         return avg.value, mn.value
+
+    def stream(self) -> int:
+        """The cudaStream_t of this problem's kernels, as an integer."""
+        st = _vp()
+        check(load().am_problem_stream(self.handle, ctypes.byref(st)), "am_problem_stream")
+        return int(st.value or 0)
 
     def layout_info(self):
         n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)

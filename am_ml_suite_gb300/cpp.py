@@ -46,7 +46,7 @@ class SIMPConfig:
     verbose: bool = True
     # solver (TopologyOptimizer uses tolerance 1e-6, topology_optimizer.cpp:35-40)
     cg_tol: float = 1e-6
-    cg_max_iterations: int = 20000
+    cg_max_iterations: int = 100000
     precision: int = nat.PREC_MIXED
     warm_start: bool = True
 

@@ -382,7 +382,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         // z = M(r) that reduces its residual by inner_tol (or stops at its cap).
         CKS(ensure_vectors(P, true));
         const int max_outer = c.max_outer > 0 ? c.max_outer : 200;
-        const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.1;
+        const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
         const int inner_cap = std::max(50, maxit / 4);
         CK(cudaMemsetAsync(&P->S->o_status, 0, sizeof(int), P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
@@ -566,9 +566,9 @@ void am_simp_config_default(am_simp_config *c, int variant) {
     c->precision = AM_PREC_MIXED;
     c->preconditioner = AM_PRECOND_JACOBI;
     c->cg_tol = 1e-6;
-    c->cg_max_iterations = 20000;
+    c->cg_max_iterations = 100000;
     c->warm_start = 1;
-    c->inner_tol = 0.1;
+    c->inner_tol = 0.01;
     c->max_outer = 200;
     c->layout = AM_LAYOUT_ZFASTEST;
     c->verbose = 0;
@@ -1013,9 +1013,16 @@ long long am_launch_count(void) { return launch_count(); }
 
 am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, double *avg_ms, double *min_ms) {
     CKS(check_problem(P));
-    if (!P->simp_begun || P->iter < 1) return fail(AM_ERR_INVALID_ARG, "run am_simp_step at least once first");
+    if (!P->simp_begun) return fail(AM_ERR_INVALID_ARG, "am_simp_begin not called");
     if (reps < 1) return fail(AM_ERR_INVALID_ARG, "reps must be >= 1");
+    if (P->cases.empty()) return fail(AM_ERR_INVALID_ARG, "no load case set");
     CKS(ensure_vectors(P, false));
+    if (P->iter < 1) {
+        // no step ran yet: operator and mask of the current density, zero vectors
+        CKS(setup_operator(P, P->cfg, P->rho.p));
+        CKS(setup_mask(P, 0));
+        CK(P->cases[0].x64.alloc(3 * (size_t)P->L.cs));
+    }
     CKS(sync_scalars(P));
     const Scalars saved = *P->Sh;
     Scalars run = saved;
@@ -1070,6 +1077,13 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
     CK(cudaStreamSynchronize(P->st));
     if (avg_ms) *avg_ms = tot / reps;
     if (min_ms) *min_ms = mn;
+    return AM_OK;
+}
+
+am_status am_problem_stream(am_problem *P, void **stream) {
+    CKS(check_problem(P));
+    if (!stream) return fail(AM_ERR_INVALID_ARG, "null output");
+    *stream = (void *)P->st;
     return AM_OK;
 }
 

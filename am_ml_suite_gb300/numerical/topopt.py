@@ -36,7 +36,7 @@ class SIMPParams:
     # engine knobs (no counterpart in the reference, which solves directly)
     precision: int = nat.PREC_FP64
     cg_tol: float = 1e-8
-    cg_max_iterations: int = 20000
+    cg_max_iterations: int = 100000
     warm_start: bool = True
 
 

@@ -8,10 +8,11 @@ cylinder (radius 16 voxels through y, axis at the x-z centre, rho = 0) and four
 passive solid 6x6 bolt-pad columns (full height, inset 6 voxels from the x-y
 corners, rho = 1), 3 point loads on the top face at seeded random nodes
 (numpy default_rng(2)), magnitude U(0.5, 1.5), direction uniform on the sphere.
-K*u in FP32 inside an FP64 defect-correction loop to rel-res 1e-6, Jacobi PCG.
+FP64 flexible CG to rel-res 1e-6 preconditioned by FP32 Jacobi-PCG inner solves.
 
 One step = one SIMP iteration (solve, sensitivities, filter, OC update).
-``value``: iterations/s over the timed steps with the state resident in HBM.
+``value``: iterations/s over the timed steps with the state resident in HBM,
+timed with CUDA events on the library's stream.
 ``e2e``: the same metric through the public C ABI from host buffers
 (``am_problem_set_loads`` + ``am_simp_run`` for W+K iterations, density
 downloaded).  The working set of a step (solver vectors + element arrays,
@@ -82,7 +83,8 @@ def build_workload(name):
 def simp_config(nat, W, max_iterations=100):
     return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
-                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=0.1)
+                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=0.01,
+                              cg_max_iterations=200000)
 
 
 class ClockSampler:
@@ -172,13 +174,29 @@ def cpu_baseline(W, steps_gpu_its, pcg_iters_sample=20):
             "phases_s": times}
 
 
+def measured_pcg_iterations(workload):
+    """PCG iterations per SIMP iteration measured by this GB300 arm on the same
+    workload and steps (committed with the profiles), or None."""
+    p = os.path.join(ROOT, "profiles", "pcg_iterations.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(workload)
+    return None if e is None else float(e["pcg_iterations_per_solve"])
+
+
 def run_reference(args, W):
     import oracle as O  # noqa: F401
 
-    # bounded sample per step: one timed sample of the CPU restatement per step
+    # bounded sample per step: one timed sample of the CPU restatement per step,
+    # extrapolated with the PCG iteration count the GB300 arm measured (same
+    # method and tolerance), so both arms do the same number of PCG iterations
     vals = []
     sample = None
-    its = float(os.environ.get("AM_BENCH_PCG_ITS", "2000"))
+    its = measured_pcg_iterations(args.workload)
+    if its is None:
+        its = float(os.environ.get("AM_BENCH_PCG_ITS", "2000"))
     for _ in range(max(1, args.warmup)):
         cpu_baseline(W, its, 5)
     t0 = time.time()
@@ -209,6 +227,9 @@ def main():
     ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--probe", choices=["ku", "resid", "update"],
+                    help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
+    ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -243,27 +264,48 @@ def main():
     shape = W["shape"]
     cfg = simp_config(nat, W)
 
+    if args.probe:
+        # set-up only, then `reps` launches of one kernel (L2 flushed before each)
+        p = nat.Problem(shape, 1.0, 1.0, 0.3)
+        p.set_loads([W["F"]], [W["fixed"]])
+        p.simp_begin(cfg, W["rho0"])
+        which = {"ku": 0, "resid": 1, "update": 2}[args.probe]
+        avg, mn = p.bench_kernel(which, reps=args.reps, flush_l2=True)
+        lay = p.layout_info()
+        p.close()
+        print(json.dumps({"probe": args.probe, "workload": args.workload, "reps": args.reps, "avg_ms": avg,
+                          "min_ms": mn, "nodes": lay["nodes"], "elements": lay["elements"]}))
+        return
+
+    import torch
+
+    torch.cuda.init()
+
     # ---- device-resident timed region --------------------------------------
     p = nat.Problem(shape, 1.0, 1.0, 0.3)
     p.set_loads([W["F"]], [W["fixed"]])
     p.simp_begin(cfg, W["rho0"])
     warm = [p.simp_step() for _ in range(args.warmup)]
     lay = p.layout_info()
+    # CUDA events on the stream the library launches on
+    lib_stream = torch.cuda.ExternalStream(p.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.barrier()
+    torch.cuda.synchronize()
     l0 = nat.launch_count()
     with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        res = [p.simp_step() for _ in range(args.steps)]  # each step ends with a device sync
-        t1 = time.perf_counter()
+        ev0.record(lib_stream)
+        res = [p.simp_step() for _ in range(args.steps)]
+        ev1.record(lib_stream)
+        torch.cuda.synchronize()
     l1 = nat.launch_count()
-    elapsed = t1 - t0
     if world > 1:
-        import torch
-        import torch.distributed as dist
-
+        dist.barrier()
+    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    if world > 1:
         t = torch.tensor([elapsed], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
@@ -290,8 +332,6 @@ def main():
         total = args.warmup + args.steps
         ecfg = simp_config(nat, W, max_iterations=total)
         try:
-            import torch
-
             def pinned(a, dtype):
                 t = torch.empty(a.size, dtype=dtype, pin_memory=True)
                 arr = t.numpy()
@@ -327,7 +367,7 @@ def main():
             "metric": "SIMP iters/s @ rel-res 1e-6 (Jacobi PCG); PCG solve ms in pcg_solve_ms",
             "value": value, "unit": "SIMP iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 K*u + f64 defect correction",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
                        "description": W["desc"], "precision": "mixed", "preconditioner": "jacobi",
@@ -336,7 +376,7 @@ def main():
             "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,
             "solver_residual_max": max(r.solver_residual for r in res),
             "compliance_last": res[-1].compliance,
-            "roofline": {"bound": "hbm", "kernel": "ku_tile_kernel<float,32,8,PCG> (fused p-update + K*p + p.q)",
+            "roofline": {"bound": "hbm", "kernel": "ku2_kernel<8,KU_PCG> (fused p-update + FP32 K*p + p.q)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
                          "avg_ms": ku_ms, "min_ms": ku_min},

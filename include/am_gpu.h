@@ -65,9 +65,10 @@ enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
 
 /* AM_PREC_FP64: every kernel in FP64 (the parity mode).
  * AM_PREC_MIXED: FP64 flexible CG (outer K*u, vectors, dots) preconditioned by FP32
- *   Jacobi PCG inner solves (FP32 K*u, double-float dot accumulation); the outer
- *   residual r = f - K u, compliance, filter and the OC volume sums in FP64 (the OC
- *   per-element update in double-float). */
+ *   Jacobi PCG inner solves (FP32 K*u, double-float dot accumulation); a solve is
+ *   accepted on its recomputed FP64 residual r = f - K u.  Compliance, element
+ *   energies, filter and the new densities are FP64; the OC bisection passes run in
+ *   double-float. */
 enum { AM_PREC_FP64 = 0, AM_PREC_MIXED = 1 };
 
 enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1 };
@@ -87,10 +88,10 @@ typedef struct am_simp_config {
     int precision;            /* AM_PREC_* */
     int preconditioner;       /* AM_PRECOND_* */
     double cg_tol;            /* relative residual ||f - K u|| / ||f|| of every solve */
-    int cg_max_iterations;    /* cap on (inner) PCG iterations per solve */
+    int cg_max_iterations;    /* cap on (inner) PCG iterations per solve (100000 by default) */
     int warm_start;           /* 1: each solve starts from the previous displacement */
     double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve that
-                                 preconditions the FP64 flexible CG (0.1 by default) */
+                                 preconditions the FP64 flexible CG (0.01 by default) */
     int max_outer;            /* MIXED: cap on outer FP64 flexible-CG iterations per solve */
     int layout;               /* AM_LAYOUT_* of density arrays */
     int verbose;
@@ -99,13 +100,13 @@ typedef struct am_simp_config {
 /* Per-solve statistics (SolveStats, linear_solver.hpp:48-56). */
 typedef struct am_solve_stats {
     int iterations;           /* PCG iterations (sum of inner iterations in MIXED) */
-    int outer_iterations;     /* defect-correction steps (MIXED), 1 in FP64 */
+    int outer_iterations;     /* outer FP64 flexible-CG iterations (MIXED), 1 in FP64 */
     double residual;          /* final ||f - K u|| / ||f||, computed in FP64 */
     int converged;
     double solve_time_s;
     double max_displacement;
     double min_displacement;
-    int fp64_iterations;      /* MIXED: FP64 PCG iterations after the FP32 sequence stagnated */
+    int fp64_iterations;      /* reserved: 0 (FP64 iterations are counted in outer_iterations) */
 } am_solve_stats;
 
 /* IterationResult (topology_optimizer.hpp:65-74) plus the extra fields of this engine. */
@@ -123,7 +124,7 @@ typedef struct am_iteration_result {
     double solve_time_s;
     double sensitivity_time_s;
     double update_time_s;      /* filter + OC */
-    int solver_fp64_iterations; /* MIXED: FP64 continuation iterations (FP32 stagnation) */
+    int solver_fp64_iterations; /* reserved: 0 */
 } am_iteration_result;
 
 typedef struct am_problem am_problem;
@@ -218,11 +219,17 @@ am_status am_simp_get_density(am_problem *p, double *rho_out);
 long long am_launch_count(void);
 
 /* Times `reps` single launches of one kernel on the problem's stream with CUDA
- * events (after at least one am_simp_step, on the state it left): which = 0 the
+ * events, after am_simp_begin (on the state the last am_simp_step left, or, before
+ * the first step, on the initial density with zero vectors): which = 0 the
  * fused FP32 PCG K*u, 1 the FP64 residual K*u, 2 the FP32 PCG vector update,
  * 3 the plain FP32 K*u.  flush_l2 != 0 overwrites a 512 MB buffer before each
  * launch so the kernel reads from HBM.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
+
+/* The CUDA stream (cudaStream_t) on which every kernel of the problem runs, for
+ * callers that order their own work after it or time it with CUDA events.  The
+ * reference has no counterpart (its solves are synchronous CPU calls). */
+am_status am_problem_stream(am_problem *p, void **stream);
 
 /* Sizes of the device layout: reference node count, element count, the padded
  * component stride of a device vector, and the K*u tile count. */
