@@ -124,6 +124,14 @@ SIGNATURES = {
     "am_launch_count": (ctypes.c_longlong, []),
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "am_problem_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "am_batch_create": (ctypes.c_int, [ctypes.c_int, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.POINTER(_vp)]),
+    "am_batch_destroy": (ctypes.c_int, [_vp]),
+    "am_batch_set_loads": (ctypes.c_int, [_vp, _dp, _i64p, _i64p]),
+    "am_batch_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip, _dp]),
+    "am_batch_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "am_batch_simp_run": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, _dp, _ip, _ip,
+                                         ctypes.POINTER(ctypes.c_longlong)]),
     "am_problem_layout": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                          ctypes.POINTER(ctypes.c_longlong), _ip]),
     # device pointers are passed as c_void_p
@@ -317,6 +325,85 @@ class Problem:
         check(load().am_problem_layout(self.handle, ctypes.byref(n), ctypes.byref(e), ctypes.byref(cs),
                                        ctypes.byref(t)), "am_problem_layout")
         return dict(nodes=n.value, elements=e.value, vector_stride=cs.value, ku_tiles=t.value)
+
+
+class Batch:
+    """Owns an ``am_batch`` handle: independent C++-variant problems of uneven
+    sizes solved together (one kernel launch per family for the whole batch)."""
+
+    def __init__(self, shapes, h=1.0, E0=1.0, nu=0.3):
+        L = load()
+        self.shapes = [tuple(int(v) for v in s) for s in shapes]
+        self.n = len(self.shapes)
+        sh = np.ascontiguousarray(np.array(self.shapes, dtype=np.int32).ravel())
+        h_ = _vp()
+        check(L.am_batch_create(self.n, ptr(sh, _ip), float(h), float(E0), float(nu), ctypes.byref(h_)),
+              "am_batch_create")
+        self.handle = h_
+        self.nel = [nx * ny * nz for nx, ny, nz in self.shapes]
+        self.N = [3 * (nx + 1) * (ny + 1) * (nz + 1) for nx, ny, nz in self.shapes]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().am_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_loads(self, F_list, fixed_list):
+        if len(F_list) != self.n or len(fixed_list) != self.n:
+            raise ValueError("one force vector and one fixed-DOF list per problem")
+        for f, N in zip(F_list, self.N):
+            if np.asarray(f).size != N:
+                raise ValueError("force vector size mismatch")
+        F = np.ascontiguousarray(np.concatenate([f64(f).ravel() for f in F_list]))
+        fx = [np.asarray(f, dtype=np.int64).ravel() for f in fixed_list]
+        fixed = np.ascontiguousarray(np.concatenate(fx) if fx else np.zeros(0, np.int64))
+        nf = np.array([f.size for f in fx], dtype=np.int64)
+        check(load().am_batch_set_loads(self.handle, ptr(F), ptr(fixed, _i64p), ptr(nf, _i64p)),
+              "am_batch_set_loads")
+
+    def autotune(self, reps=3):
+        w, z, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        ms = ctypes.c_double(0.0)
+        check(load().am_batch_autotune(self.handle, int(reps), ctypes.byref(w), ctypes.byref(z), ctypes.byref(c),
+                                       ctypes.byref(ms)), "am_batch_autotune")
+        return dict(warps=w.value, z_chunk=z.value, ctas_per_sm=c.value, ms=ms.value)
+
+    def stream(self) -> int:
+        st = _vp()
+        check(load().am_batch_stream(self.handle, ctypes.byref(st)), "am_batch_stream")
+        return int(st.value or 0)
+
+    def simp_run(self, cfgs, rho0_list=None):
+        if len(cfgs) != self.n:
+            raise ValueError("one config per problem")
+        arr = (SimpConfig * self.n)(*cfgs)
+        H = max(max(int(c.max_iterations) for c in cfgs), 1)
+        r0 = None
+        if rho0_list is not None:
+            r0 = np.ascontiguousarray(np.concatenate([f64(r).ravel() for r in rho0_list]))
+            if r0.size != sum(self.nel):
+                raise ValueError("density size mismatch")
+        rho = np.zeros(sum(self.nel))
+        ch, vh = np.zeros(self.n * H), np.zeros(self.n * H)
+        it, conv = np.zeros(self.n, np.int32), np.zeros(self.n, np.int32)
+        pcg = np.zeros(self.n, np.int64)
+        check(load().am_batch_simp_run(self.handle, arr, ptr(r0), ptr(rho), ptr(ch), ptr(vh), ptr(it, _ip),
+                                       ptr(conv, _ip), pcg.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))),
+              "am_batch_simp_run")
+        out, o = [], 0
+        for p, (nx, ny, nz) in enumerate(self.shapes):
+            k = int(it[p])
+            out.append(dict(density=rho[o:o + self.nel[p]].copy(), compliance=ch[p * H:p * H + k].copy(),
+                            volume=vh[p * H:p * H + k].copy(), iterations=k, converged=bool(conv[p]),
+                            pcg_iterations=int(pcg[p])))
+            o += self.nel[p]
+        return out
 
 
 def launch_count() -> int:

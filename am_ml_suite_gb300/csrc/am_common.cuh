@@ -60,6 +60,9 @@ struct Scalars {
     int o_status, pad1;
     // last-block counters (one per kernel family so overlapping uses never clash)
     unsigned int cnt_ku, cnt_upd, cnt_oc, cnt_misc, cnt_fcg, pad2;
+    // batched runs: |F|^2 on the free DOFs, and 1 once the problem's SIMP loop ended
+    double b2;
+    int frozen, pad3;
 };
 
 enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4, ST_UPDATE = 5 };
@@ -148,19 +151,30 @@ __device__ __forceinline__ double block_max(double x, double *red) {
     return x;
 }
 
-// Last-block-done protocol: every block publishes its partials, then the block
-// that arrives last (ticket == gridDim.x - 1) reduces them in index order and
-// resets the counter.  Returns true in every thread of the last block.
-__device__ __forceinline__ bool arrive_last(unsigned int *counter, int *flag_smem) {
+// Block coordinates of a kernel body: the body runs either as a stand-alone grid
+// (b = blockIdx.x, n = gridDim.x) or as one work item of a batched persistent
+// grid (b = the item's block within its problem, n = that problem's block count).
+struct Blk {
+    int b, n;
+};
+__device__ __forceinline__ Blk grid_blk() { return Blk{(int)blockIdx.x, (int)gridDim.x}; }
+
+// Last-block-done protocol: every block of a body publishes its partials, then
+// the block that arrives last (ticket == nblocks - 1) reduces them in index order
+// and resets the counter.  Returns true in every thread of the last block.
+__device__ __forceinline__ bool arrive_last_n(unsigned int *counter, int *flag_smem, int nblocks) {
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int t = atomicAdd(counter, 1u);
-        *flag_smem = (t == gridDim.x - 1) ? 1 : 0;
+        *flag_smem = (t == (unsigned int)nblocks - 1u) ? 1 : 0;
     }
     __syncthreads();
     if (*flag_smem) __threadfence();
     return *flag_smem != 0;
+}
+__device__ __forceinline__ bool arrive_last(unsigned int *counter, int *flag_smem) {
+    return arrive_last_n(counter, flag_smem, (int)gridDim.x);
 }
 
 // Sum partial[b*stride + k] over b in [0, nb) in a fixed order, for k < NV.

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/am_gpu.h"
+#include "host_util.h"
 #include "kernels.cuh"
 #include "ku.cuh"
 
@@ -203,39 +204,9 @@ am_status download_elem(am_problem *P, const double *src, double *host, int layo
 am_status build_taps(am_problem *P, double r, int variant) {
     if (P->taps_r == r && P->taps_variant == variant) return AM_OK;
     if (!(r > 0.0) || r > 6.0) return fail(AM_ERR_INVALID_ARG, "filter_radius must be in (0, 6]");
-    const int R = (int)std::ceil(r);
     std::vector<int4> d;
     std::vector<double> w;
-    double tot = 0.0;
-    // CPP: neighbour search order dz, dy, dx (topology_optimizer.cpp:76-101),
-    // weight max(0, r - dist) for dist <= r.  PY: full (2R+1)^3 box of r - dist
-    // for dist <= r, normalised by the sum (topopt.py:135-151).
-    for (int dz = -R; dz <= R; ++dz)
-        for (int dy = -R; dy <= R; ++dy)
-            for (int dx = -R; dx <= R; ++dx) {
-                const double dist = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
-                if (dist <= r) {
-                    const double wt = variant == 0 ? std::max(0.0, r - dist) : r - dist;
-                    if (variant == 1 && wt == 0.0) continue;
-                    d.push_back(make_int4(dx, dy, dz, 0));
-                    w.push_back(wt);
-                    tot += wt;
-                }
-            }
-    if (variant == 1) {
-        // the reference sums the kernel over the box in C order (x, y, z) before
-        // normalising; the zero entries do not change the sum
-        double t2 = 0.0;
-        for (int a = 0; a < 2 * R + 1; ++a)
-            for (int b = 0; b < 2 * R + 1; ++b)
-                for (int c = 0; c < 2 * R + 1; ++c) {
-                    const double dist =
-                        std::sqrt((double)((a - R) * (a - R) + (b - R) * (b - R) + (c - R) * (c - R)));
-                    if (dist <= r) t2 += r - dist;
-                }
-        for (auto &x : w) x /= t2;
-    }
-    (void)tot;
+    filter_taps(r, variant, d, w);
     CK(P->tap_d.alloc(d.size()));
     CK(P->tap_w.alloc(w.size()));
     CK(cudaMemcpyAsync(P->tap_d.p, d.data(), d.size() * sizeof(int4), cudaMemcpyHostToDevice, P->st));
@@ -490,22 +461,6 @@ am_status check_cfg(am_problem *P, const am_simp_config *c) {
     return AM_OK;
 }
 
-// Walsh-basis constants of the unit-modulus hex8 cube of edge h (ku.cuh).
-Modal<double> modal_constants(double E, double nu, double h) {
-    const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
-    const double mu = E / (2.0 * (1.0 + nu));
-    const double a = h / 2.0;
-    return Modal<double>{lam, mu, a / 8.0, a / 24.0, a / 72.0, a / 72.0 * (lam + 4.0 * mu)};
-}
-
-// Entry (row, col) of KE, evaluated with the same operator the kernels apply.
-double element_stiffness_host(const Modal<double> &M, int row, int col) {
-    double u[3][8] = {}, y[3][8];
-    u[col % 3][col / 3] = 1.0;
-    hex8_apply<double>(u, y, M, 1.0, nullptr);
-    return y[row % 3][row / 3];
-}
-
 }  // namespace
 
 // ============================================================================
@@ -603,20 +558,16 @@ am_status am_problem_create(int nx, int ny, int nz, double h, double E0, double 
     P->h = h; P->E0 = E0; P->nu = nu;
     cudaGetDevice(&P->device);
     Layout &L = P->L;
-    L.nx = nx; L.ny = ny; L.nz = nz;
-    L.sx = ((nx + 1) + 3) / 4 * 4;
-    L.sxy = (long long)L.sx * (ny + 1);
-    L.cs = (L.sxy * (nz + 1) + 63) / 64 * 64;
-    L.nel = (long long)nx * ny * nz;
+    L = make_layout(nx, ny, nz);
     P->nn_ref = (long long)(nx + 1) * (ny + 1) * (nz + 1);
     P->N = 3 * P->nn_ref;
     // Lame parameters of the unit-modulus material; K scales linearly with E0
     // and the element scales carry E/E0, so the operator uses E = E0.
     P->M64 = modal_constants(E0, nu, h);
     const Modal<double> &M = P->M64;
-    P->M32 = Modal<float>{(float)M.lam, (float)M.mu, (float)M.c1, (float)M.c2, (float)M.c3, (float)M.c7};
+    P->M32 = modal_float(M);
     // every diagonal entry of the cube KE equals KE[0][0]
-    P->ke00 = element_stiffness_host(M, 0, 0);
+    P->ke00 = element_stiffness_entry(M, 0, 0);
     P->plan32 = ku_plan(L, false, 0);
     P->plan64 = ku_plan(L, true, 0);
     P->nblocks_vec = (int)std::max<long long>(1, std::min<long long>((3 * L.cs + 255) / 256, 152LL * 8));

@@ -1,0 +1,639 @@
+// batch.cu -- am_batch: many independent C++-variant SIMP problems of uneven
+// sizes advanced together by batched persistent kernels (batch.cuh).
+//
+// One SIMP step of the batch is: scales + Jacobi diagonal, warm-start clean-up,
+// FP64 defect correction (FP64 residual, FP32 Jacobi PCG on it, x += x32) until
+// every problem's |F - K u| <= tol |F|, the FP64 residual with element energies,
+// then sensitivities, u.F, filter and the FP64 OC bisection.  Each of these is one
+// launch for the whole batch; the FP32 PCG iterations run as CUDA-graph chunks of
+// 32 iterations, and a problem that has converged (or whose SIMP loop has ended)
+// is skipped by its kernels.  The reference runs one TopologyOptimizer per
+// problem (topology_optimizer.cpp:391-520); the per-problem results follow those
+// semantics.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/am_gpu.h"
+#include "batch.cuh"
+#include "host_util.h"
+#include "kernels.cuh"
+
+using namespace amk;
+
+namespace {
+
+am_status bfail(am_status s, const std::string &msg) {
+    set_last_error(msg.c_str());
+    return s;
+}
+
+#define BCK(call)                                                                          \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return bfail(e_ == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,       \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+#define BCKS(expr)                   \
+    do {                             \
+        am_status s_ = (expr);       \
+        if (s_ != AM_OK) return s_;  \
+    } while (0)
+
+template <typename T>
+struct Pool {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        release();
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) {
+            n = count;
+            e = cudaMemset(p, 0, std::max<size_t>(count, 1) * sizeof(T));
+        }
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+constexpr int kChunk = 32;     // FP32 PCG iterations per CUDA-graph chunk
+constexpr int kMaxRounds = 30; // defect-correction rounds per solve
+constexpr int kSms = 152;
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct am_batch {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int n = 0;
+    std::vector<Layout> L;
+    double h = 1, E0 = 1, nu = 0.3;
+    BatchConst C{};
+    // offsets (in elements of the pool type) per problem
+    std::vector<size_t> eoff, noff, foff, toff, poff;
+    size_t nel_tot = 0, nn_tot = 0;
+    // pools
+    Pool<double> rho, rho_new, s64, ce, dc, dcf, oc_a, oc_lo, oc_hi;
+    Pool<float> s32;
+    Pool<uint8_t> design;
+    Pool<double> F, x64, r64, dinv64;
+    Pool<float> x32, r32, pa, pb, q32, dinv32;
+    Pool<uint8_t> mask, fixed_bits;
+    Pool<long long> f_idx;
+    Pool<double> f_val;
+    Pool<int4> tap_d;
+    Pool<double> tap_w;
+    Pool<double> partial;
+    Pool<Scalars> S;
+    Scalars *Sh = nullptr;  // pinned mirror
+    Pool<BatchItem> items_d;
+    std::vector<BatchItem> items;
+    // work lists
+    Pool<int2> w_elem, w_vec, w_k2, w_k64, w_prob;
+    WorkList elem{}, vec{}, k2{}, k64{}, prob{};
+    // FP32 K*u plan (autotuner): warps per CTA, z chunk (0 = all planes), CTAs per SM
+    int warps = 8, zchunk = 0, ctas = 2;
+    bool loads_set = false;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<long long> pcg_its;
+};
+
+namespace {
+
+int div_up_i(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+am_status upload_worklist(am_batch *B, Pool<int2> &pool, WorkList &wl, const std::vector<int2> &w) {
+    BCK(pool.alloc(w.size()));
+    BCK(cudaMemcpy(pool.p, w.data(), w.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    wl.w = pool.p;
+    wl.n = (int)w.size();
+    (void)B;
+    return AM_OK;
+}
+
+// FP32 K*u tiles of every problem for the plan (warps, zchunk); work items in
+// descending tile height so the persistent grid ends with the short ones.
+am_status plan_k2(am_batch *B, int warps, int zchunk) {
+    struct T {
+        int p, b, h;
+    };
+    std::vector<T> t;
+    for (int p = 0; p < B->n; ++p) {
+        const Layout &L = B->L[p];
+        BatchItem &it = B->items[p];
+        it.k2_tiles_x = div_up_i(L.nx + 1, 30);
+        it.k2_tiles_y = div_up_i(L.ny + 1, 2 * warps - 1);
+        const int planes = L.nz + 1;
+        it.k2_tz = zchunk > 0 ? std::min(zchunk, planes) : planes;
+        it.k2_tiles_z = div_up_i(planes, it.k2_tz);
+        it.n_k2 = it.k2_tiles_x * it.k2_tiles_y * it.k2_tiles_z;
+        for (int b = 0; b < it.n_k2; ++b) {
+            const int tzi = b / (it.k2_tiles_x * it.k2_tiles_y);
+            const int h = std::min(it.k2_tz, planes - tzi * it.k2_tz);
+            t.push_back(T{p, b, h});
+        }
+    }
+    std::stable_sort(t.begin(), t.end(), [](const T &a, const T &b) { return a.h > b.h; });
+    std::vector<int2> w(t.size());
+    for (size_t i = 0; i < t.size(); ++i) w[i] = make_int2(t[i].p, t[i].b);
+    BCKS(upload_worklist(B, B->w_k2, B->k2, w));
+    BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    B->warps = warps;
+    B->zchunk = zchunk;
+    if (B->graph) {
+        cudaGraphExecDestroy(B->graph);
+        B->graph = nullptr;
+    }
+    return AM_OK;
+}
+
+am_status sync_scalars(am_batch *B) {
+    BCK(cudaMemcpyAsync(B->Sh, B->S.p, sizeof(Scalars) * B->n, cudaMemcpyDeviceToHost, B->st));
+    BCK(cudaStreamSynchronize(B->st));
+    return AM_OK;
+}
+
+am_status build_graph(am_batch *B) {
+    if (B->graph) return AM_OK;
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
+        e = batch_pcg_iteration(B->items_d.p, B->k2, B->vec, B->C, B->warps, kSms * B->ctas, kSms * 8, B->st);
+    cudaError_t e2 = cudaStreamEndCapture(B->st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bfail(AM_ERR_CUDA, std::string("batch graph capture: ") +
+                                      cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&B->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(AM_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    return AM_OK;
+}
+
+bool all_done(const am_batch *B) {
+    for (int p = 0; p < B->n; ++p)
+        if (!B->Sh[p].frozen && !B->Sh[p].done) return false;
+    return true;
+}
+
+// FP64 defect correction around FP32 Jacobi PCG for every active problem.
+am_status batch_solve(am_batch *B, int max_chunks) {
+    for (int round = 0; round < kMaxRounds; ++round) {
+        BCK(batch_resid(B->items_d.p, B->k64, B->C, 0, kSms * 4, B->st));
+        BCK(batch_inner_start(B->items_d.p, B->vec, kSms * 8, B->st));
+        BCKS(sync_scalars(B));
+        for (int p = 0; p < B->n; ++p)
+            if (!B->Sh[p].frozen && !std::isfinite(B->Sh[p].res_rr))
+                return bfail(AM_ERR_NAN_DETECTED, "NaN in the residual of batch problem " + std::to_string(p));
+        if (all_done(B)) return AM_OK;
+        int chunks = 0;
+        while (true) {
+            BCK(cudaGraphLaunch(B->graph, B->st));
+            count_launches(2LL * kChunk);
+            BCKS(sync_scalars(B));
+            ++chunks;
+            if (all_done(B)) break;
+            if (chunks > max_chunks) return bfail(AM_ERR_TIMEOUT, "batched PCG did not stop within its cap");
+        }
+        for (int p = 0; p < B->n; ++p) {
+            if (B->Sh[p].frozen) continue;
+            if (B->Sh[p].status == ST_NAN)
+                return bfail(AM_ERR_NAN_DETECTED, "NaN in the PCG of batch problem " + std::to_string(p));
+            B->pcg_its[p] += B->Sh[p].it;
+        }
+        BCK(batch_accumulate(B->items_d.p, B->vec, kSms * 8, B->st));
+    }
+    return AM_OK;  // not converged within the rounds: reported through the residuals
+}
+
+am_status check_batch(am_batch *B) {
+    if (!B) return bfail(AM_ERR_INVALID_ARG, "null batch");
+    BCK(cudaSetDevice(B->device));
+    return AM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+am_status am_batch_destroy(am_batch *B) {
+    if (!B) return AM_OK;
+    cudaSetDevice(B->device);
+    if (B->st) cudaStreamSynchronize(B->st);
+    if (B->graph) cudaGraphExecDestroy(B->graph);
+    for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi,
+                    &B->F, &B->x64, &B->r64, &B->dinv64, &B->f_val, &B->tap_w, &B->partial})
+        q->release();
+    for (auto *q : {&B->s32, &B->x32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32}) q->release();
+    for (auto *q : {&B->design, &B->mask, &B->fixed_bits}) q->release();
+    for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k64, &B->w_prob}) q->release();
+    B->f_idx.release();
+    B->tap_d.release();
+    B->S.release();
+    B->items_d.release();
+    if (B->Sh) cudaFreeHost(B->Sh);
+    if (B->st) cudaStreamDestroy(B->st);
+    delete B;
+    return AM_OK;
+}
+
+am_status am_batch_create(int n, const int *shapes, double h, double E0, double nu, am_batch **out) {
+    if (!out) return bfail(AM_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    if (n < 1 || !shapes) return bfail(AM_ERR_INVALID_ARG, "need n >= 1 problems and their shapes");
+    if (!(h > 0.0) || !(E0 > 0.0) || !(nu > -1.0 && nu < 0.5))
+        return bfail(AM_ERR_INVALID_ARG, "need h > 0, E0 > 0, -1 < nu < 0.5");
+    for (int p = 0; p < n; ++p)
+        if (shapes[3 * p] < 1 || shapes[3 * p + 1] < 1 || shapes[3 * p + 2] < 1)
+            return bfail(AM_ERR_INVALID_ARG, "problem " + std::to_string(p) + ": dimensions must be >= 1");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return bfail(AM_ERR_NO_DEVICE, "no CUDA device");
+    am_batch *B = new am_batch();
+    cudaGetDevice(&B->device);
+    B->n = n;
+    B->h = h;
+    B->E0 = E0;
+    B->nu = nu;
+    B->C.M64 = modal_constants(E0, nu, h);
+    B->C.M32 = modal_float(B->C.M64);
+    B->C.d0 = element_stiffness_entry(B->C.M64, 0, 0);
+    B->L.resize(n);
+    B->eoff.resize(n + 1);
+    B->noff.resize(n + 1);
+    B->poff.resize(n + 1);
+    B->items.assign(n, BatchItem{});
+    B->pcg_its.assign(n, 0);
+    size_t e = 0, nn = 0, pp = 0;
+    for (int p = 0; p < n; ++p) {
+        const Layout L = make_layout(shapes[3 * p], shapes[3 * p + 1], shapes[3 * p + 2]);
+        B->L[p] = L;
+        BatchItem &it = B->items[p];
+        it.L = L;
+        it.n_vec = std::max(1, div_up_i(L.cs, 4LL * BATCH_VEC_THREADS));
+        it.n_elem = std::max(1, div_up_i(L.nel, 4LL * 256));
+        it.k64_tiles_x = div_up_i(L.nx + 1, 32);
+        it.k64_tiles_y = div_up_i(L.ny + 1, 4);
+        it.k64_tz = L.nz + 1;
+        it.k64_tiles_z = 1;
+        it.n_k64 = it.k64_tiles_x * it.k64_tiles_y;
+        B->eoff[p] = e;
+        B->noff[p] = nn;
+        B->poff[p] = pp;
+        e += align_up((size_t)L.nel, 64);
+        nn += (size_t)L.cs;  // multiple of 64
+        // partials: 2 per K*u tile (either plan: at most 15x more tiles than 4-warp
+        // ku2 tiles of 1 plane), 3 per element block, 2 per vector block
+        const size_t k2max = (size_t)div_up_i(L.nx + 1, 30) * div_up_i(L.ny + 1, 7) * (L.nz + 1);
+        pp += align_up(std::max({2 * k2max, 2 * (size_t)it.n_k64, 3 * (size_t)it.n_elem, 2 * (size_t)it.n_vec,
+                                 (size_t)16}),
+                       32);
+    }
+    B->eoff[n] = e;
+    B->noff[n] = nn;
+    B->poff[n] = pp;
+    B->nel_tot = e;
+    B->nn_tot = nn;
+    cudaError_t ce = cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking);
+    auto A = [&](auto &pool, size_t cnt) {
+        if (ce == cudaSuccess) ce = pool.alloc(cnt);
+    };
+    for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi}) A(*q, e);
+    A(B->s32, e);
+    A(B->design, e);
+    for (auto *q : {&B->F, &B->x64, &B->r64}) A(*q, 3 * nn);
+    A(B->dinv64, nn);
+    for (auto *q : {&B->x32, &B->r32, &B->pa, &B->pb, &B->q32}) A(*q, 3 * nn);
+    A(B->dinv32, nn);
+    A(B->mask, nn);
+    A(B->fixed_bits, nn);
+    A(B->partial, pp);
+    A(B->S, (size_t)n);
+    A(B->items_d, (size_t)n);
+    if (ce == cudaSuccess) ce = cudaMallocHost(&B->Sh, sizeof(Scalars) * n);
+    if (ce != cudaSuccess) {
+        am_batch_destroy(B);
+        return bfail(ce == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,
+                     std::string("batch create: ") + cudaGetErrorString(ce));
+    }
+    std::vector<int2> we, wv, w64, wp;
+    for (int p = 0; p < n; ++p) {
+        BatchItem &it = B->items[p];
+        const size_t eo = B->eoff[p], no = B->noff[p];
+        it.rho = B->rho.p + eo;
+        it.rho_new = B->rho_new.p + eo;
+        it.s64 = B->s64.p + eo;
+        it.ce = B->ce.p + eo;
+        it.dc = B->dc.p + eo;
+        it.dcf = B->dcf.p + eo;
+        it.oc_a = B->oc_a.p + eo;
+        it.oc_lo = B->oc_lo.p + eo;
+        it.oc_hi = B->oc_hi.p + eo;
+        it.s32 = B->s32.p + eo;
+        it.design = B->design.p + eo;
+        it.F = B->F.p + 3 * no;
+        it.x64 = B->x64.p + 3 * no;
+        it.r64 = B->r64.p + 3 * no;
+        it.dinv64 = B->dinv64.p + no;
+        it.x32 = B->x32.p + 3 * no;
+        it.r32 = B->r32.p + 3 * no;
+        it.pa = B->pa.p + 3 * no;
+        it.pb = B->pb.p + 3 * no;
+        it.q32 = B->q32.p + 3 * no;
+        it.dinv32 = B->dinv32.p + no;
+        it.mask = B->mask.p + no;
+        it.fixed_bits = B->fixed_bits.p + no;
+        it.partial = B->partial.p + B->poff[p];
+        it.S = B->S.p + p;
+        for (int b = 0; b < it.n_elem; ++b) we.push_back(make_int2(p, b));
+        for (int b = 0; b < it.n_vec; ++b) wv.push_back(make_int2(p, b));
+        for (int b = 0; b < it.n_k64; ++b) w64.push_back(make_int2(p, b));
+        wp.push_back(make_int2(p, 0));
+    }
+    am_status s = upload_worklist(B, B->w_elem, B->elem, we);
+    if (s == AM_OK) s = upload_worklist(B, B->w_vec, B->vec, wv);
+    if (s == AM_OK) s = upload_worklist(B, B->w_k64, B->k64, w64);
+    if (s == AM_OK) s = upload_worklist(B, B->w_prob, B->prob, wp);
+    if (s == AM_OK) s = plan_k2(B, 8, 0);
+    if (s == AM_OK && ku_init_attributes() != cudaSuccess) s = bfail(AM_ERR_CUDA, "kernel attributes");
+    if (s != AM_OK) {
+        am_batch_destroy(B);
+        return s;
+    }
+    *out = B;
+    return AM_OK;
+}
+
+am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed, const int64_t *n_fixed) {
+    BCKS(check_batch(B));
+    if (!F || !n_fixed) return bfail(AM_ERR_INVALID_ARG, "null loads");
+    std::vector<double> Fd(3 * B->nn_tot, 0.0);
+    std::vector<uint8_t> fb(B->nn_tot, 0);
+    std::vector<long long> idx;
+    std::vector<double> val;
+    std::vector<size_t> foff(B->n + 1);
+    size_t fo = 0, xo = 0;
+    for (int p = 0; p < B->n; ++p) {
+        const Layout &L = B->L[p];
+        const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+        const size_t no = B->noff[p];
+        foff[p] = idx.size();
+        for (long long r = 0; r < nn; ++r) {
+            // reference node r = (i*(ny+1) + j)*(nz+1) + k
+            const int k = (int)(r % (L.nz + 1));
+            const long long t = r / (L.nz + 1);
+            const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
+            const long long d = node_index(L, i, j, k);
+            for (int c = 0; c < 3; ++c) {
+                const double v = F[fo + 3 * r + c];
+                if (!std::isfinite(v)) return bfail(AM_ERR_NAN_DETECTED, "non-finite force, problem " + std::to_string(p));
+                Fd[3 * no + (size_t)c * L.cs + d] = v;
+                if (v != 0.0) {
+                    idx.push_back((long long)c * L.cs + d);
+                    val.push_back(v);
+                }
+            }
+        }
+        const int64_t nf = n_fixed[p];
+        if (nf < 0) return bfail(AM_ERR_INVALID_ARG, "negative fixed-DOF count");
+        if (nf > 0 && !fixed) return bfail(AM_ERR_INVALID_ARG, "null fixed DOFs");
+        for (int64_t q = 0; q < nf; ++q) {
+            const int64_t dof = fixed[xo + q];
+            if (dof < 0 || dof >= 3 * nn)
+                return bfail(AM_ERR_DOF_OUT_OF_RANGE, "fixed DOF out of range, problem " + std::to_string(p));
+            const long long r = dof / 3;
+            const int c = (int)(dof % 3);
+            const int k = (int)(r % (L.nz + 1));
+            const long long t = r / (L.nz + 1);
+            const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
+            fb[no + node_index(L, i, j, k)] |= (uint8_t)(1u << c);
+        }
+        fo += 3 * (size_t)nn;
+        xo += (size_t)nf;
+    }
+    foff[B->n] = idx.size();
+    BCK(B->f_idx.alloc(std::max<size_t>(idx.size(), 1)));
+    BCK(B->f_val.alloc(std::max<size_t>(val.size(), 1)));
+    if (!idx.empty()) {
+        BCK(cudaMemcpy(B->f_idx.p, idx.data(), idx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(B->f_val.p, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    BCK(cudaMemcpy(B->F.p, Fd.data(), Fd.size() * sizeof(double), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(B->fixed_bits.p, fb.data(), fb.size(), cudaMemcpyHostToDevice));
+    for (int p = 0; p < B->n; ++p) {
+        BatchItem &it = B->items[p];
+        it.f_idx = B->f_idx.p + foff[p];
+        it.f_val = B->f_val.p + foff[p];
+        it.f_nnz = (int)(foff[p + 1] - foff[p]);
+    }
+    BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    B->loads_set = true;
+    return AM_OK;
+}
+
+am_status am_batch_autotune(am_batch *B, int reps, int *warps, int *z_chunk, int *ctas_per_sm, double *best_ms) {
+    BCKS(check_batch(B));
+    if (reps < 1) return bfail(AM_ERR_INVALID_ARG, "reps must be >= 1");
+    struct Cand {
+        int w, z, c;
+    };
+    const Cand cands[] = {{8, 0, 2}, {8, 16, 2}, {8, 8, 2}, {8, 0, 1}, {4, 0, 4}, {4, 16, 4}, {4, 8, 4}, {4, 0, 2}};
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    double best = 1e300;
+    Cand bc = cands[0];
+    for (const Cand &c : cands) {
+        BCKS(plan_k2(B, c.w, c.z));
+        BCK(batch_ku_plain(B->items_d.p, B->k2, B->C, c.w, kSms * c.c, B->st));  // warm-up
+        BCK(cudaEventRecord(e0, B->st));
+        for (int r = 0; r < reps; ++r) BCK(batch_ku_plain(B->items_d.p, B->k2, B->C, c.w, kSms * c.c, B->st));
+        BCK(cudaEventRecord(e1, B->st));
+        BCK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        const double avg = ms / reps;
+        if (avg < best) {
+            best = avg;
+            bc = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    BCKS(plan_k2(B, bc.w, bc.z));
+    B->ctas = bc.c;
+    if (warps) *warps = bc.w;
+    if (z_chunk) *z_chunk = bc.z;
+    if (ctas_per_sm) *ctas_per_sm = bc.c;
+    if (best_ms) *best_ms = best;
+    return AM_OK;
+}
+
+am_status am_batch_stream(am_batch *B, void **stream) {
+    BCKS(check_batch(B));
+    if (!stream) return bfail(AM_ERR_INVALID_ARG, "null output");
+    *stream = (void *)B->st;
+    return AM_OK;
+}
+
+am_status am_batch_simp_run(am_batch *B, const am_simp_config *cfgs, const double *rho0, double *rho_out,
+                            double *compliance_hist, double *volume_hist, int *iterations, int *converged,
+                            long long *pcg_iterations) {
+    BCKS(check_batch(B));
+    if (!cfgs) return bfail(AM_ERR_INVALID_ARG, "null configs");
+    if (!B->loads_set) return bfail(AM_ERR_INVALID_ARG, "loads not set");
+    const int n = B->n;
+    int hist = 0;
+    for (int p = 0; p < n; ++p) {
+        const am_simp_config &c = cfgs[p];
+        const std::string w = "problem " + std::to_string(p) + ": ";
+        if (c.variant != AM_VARIANT_CPP) return bfail(AM_ERR_INVALID_ARG, w + "batches run the C++ variant");
+        if (c.layout != AM_LAYOUT_ZFASTEST && c.layout != AM_LAYOUT_XFASTEST)
+            return bfail(AM_ERR_INVALID_ARG, w + "unknown layout");
+        if (!(c.volume_fraction > 0.0 && c.volume_fraction <= 1.0))
+            return bfail(AM_ERR_INVALID_ARG, w + "volume_fraction must be in (0, 1]");
+        if (!(c.penalty >= 1.0) || !(c.move_limit > 0.0) || !(c.rho_min >= 0.0) || !(c.E_min >= 0.0))
+            return bfail(AM_ERR_INVALID_ARG, w + "need penalty >= 1, move_limit > 0, rho_min >= 0, E_min >= 0");
+        if (!(c.cg_tol > 0.0)) return bfail(AM_ERR_INVALID_ARG, w + "cg_tol must be > 0");
+        if (!(c.filter_radius > 0.0) || c.filter_radius > 6.0)
+            return bfail(AM_ERR_INVALID_ARG, w + "filter_radius must be in (0, 6]");
+        if (c.max_iterations < 0) return bfail(AM_ERR_INVALID_ARG, w + "max_iterations < 0");
+        hist = std::max(hist, c.max_iterations);
+    }
+    // densities, design masks, taps, parameters
+    std::vector<double> r0(B->nel_tot, 0.0);
+    std::vector<uint8_t> dm(B->nel_tot, 0);
+    std::vector<int4> td;
+    std::vector<double> tw;
+    std::vector<size_t> toff(n + 1);
+    size_t ho = 0;
+    int max_maxit = 1;
+    for (int p = 0; p < n; ++p) {
+        const am_simp_config &c = cfgs[p];
+        const Layout &L = B->L[p];
+        const size_t eo = B->eoff[p];
+        long long nd = 0;
+        for (long long ez = 0; ez < L.nz; ++ez)
+            for (long long ey = 0; ey < L.ny; ++ey)
+                for (long long ex = 0; ex < L.nx; ++ex) {
+                    const long long e = (ez * L.ny + ey) * L.nx + ex;
+                    const long long hidx =
+                        c.layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
+                    const double v = rho0 ? rho0[ho + hidx] : c.volume_fraction;
+                    r0[eo + e] = v;
+                    // design mask from the initial density (topology_optimizer.cpp:419-428)
+                    const bool d = v > c.rho_min + 1e-6 && v < 0.99;
+                    dm[eo + e] = d;
+                    nd += d;
+                }
+        ho += (size_t)L.nel;
+        std::vector<int4> d;
+        std::vector<double> w;
+        filter_taps(c.filter_radius, 0, d, w);
+        toff[p] = td.size();
+        td.insert(td.end(), d.begin(), d.end());
+        tw.insert(tw.end(), w.begin(), w.end());
+        BatchItem &it = B->items[p];
+        it.penalty = c.penalty;
+        it.emin = c.E_min;
+        it.rho_min = c.rho_min;
+        it.move = c.move_limit;
+        it.vf = c.volume_fraction;
+        it.n_design = nd == 0 ? (double)L.nel : (double)nd;
+        it.tol = c.cg_tol;
+        it.maxit = c.cg_max_iterations > 0 ? c.cg_max_iterations : 100000;
+        max_maxit = std::max(max_maxit, it.maxit);
+    }
+    toff[n] = td.size();
+    BCK(B->tap_d.alloc(td.size()));
+    BCK(B->tap_w.alloc(tw.size()));
+    BCK(cudaMemcpy(B->tap_d.p, td.data(), td.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(B->tap_w.p, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice));
+    for (int p = 0; p < n; ++p) {
+        BatchItem &it = B->items[p];
+        it.tap_d = B->tap_d.p + toff[p];
+        it.tap_w = B->tap_w.p + toff[p];
+        it.ntaps = (int)(toff[p + 1] - toff[p]);
+    }
+    BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(B->rho.p, r0.data(), r0.size() * sizeof(double), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(B->design.p, dm.data(), dm.size(), cudaMemcpyHostToDevice));
+    BCK(cudaMemset(B->x64.p, 0, sizeof(double) * B->x64.n));  // cold start; warm starts between steps
+    BCK(cudaMemset(B->S.p, 0, sizeof(Scalars) * n));
+    std::vector<int> frozen(n, 0), its(n, 0), conv(n, 0);
+    for (int p = 0; p < n; ++p) {
+        if (cfgs[p].max_iterations == 0) {
+            frozen[p] = 1;
+            BCK(cudaMemcpy(&B->S.p[p].frozen, &frozen[p], sizeof(int), cudaMemcpyHostToDevice));
+        }
+    }
+    std::fill(B->pcg_its.begin(), B->pcg_its.end(), 0);
+    BCKS(build_graph(B));
+    const int max_chunks = max_maxit / kChunk + 2;
+    for (int step = 0; step < hist; ++step) {
+        if (std::all_of(frozen.begin(), frozen.end(), [](int f) { return f != 0; })) break;
+        BCK(batch_operator(B->items_d.p, B->elem, B->vec, B->C, kSms * 8, B->st));
+        BCK(batch_prepare_solve(B->items_d.p, B->vec, B->prob, kSms * 8, B->st));
+        BCKS(batch_solve(B, max_chunks));
+        BCK(batch_resid(B->items_d.p, B->k64, B->C, 1, kSms * 4, B->st));
+        BCK(batch_update(B->items_d.p, B->elem, B->prob, kSms * 8, B->st));
+        BCKS(sync_scalars(B));
+        for (int p = 0; p < n; ++p) {
+            if (frozen[p]) continue;
+            const Scalars &S = B->Sh[p];
+            const size_t hp = (size_t)p * hist + step;
+            if (compliance_hist) compliance_hist[hp] = S.comp_fu;
+            if (volume_hist) volume_hist[hp] = S.oc_volume;
+            its[p] = step + 1;
+            bool stop = false;
+            if (S.oc_change < cfgs[p].convergence_tol) {
+                conv[p] = 1;
+                stop = true;
+            }
+            if (its[p] >= cfgs[p].max_iterations) stop = true;
+            if (stop) {
+                frozen[p] = 1;
+                BCK(cudaMemcpyAsync(&B->S.p[p].frozen, &frozen[p], sizeof(int), cudaMemcpyHostToDevice, B->st));
+            }
+        }
+        BCK(cudaStreamSynchronize(B->st));
+    }
+    if (rho_out) {
+        std::vector<double> r(B->nel_tot);
+        BCK(cudaMemcpy(r.data(), B->rho.p, r.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        size_t o = 0;
+        for (int p = 0; p < n; ++p) {
+            const Layout &L = B->L[p];
+            const size_t eo = B->eoff[p];
+            for (long long ez = 0; ez < L.nz; ++ez)
+                for (long long ey = 0; ey < L.ny; ++ey)
+                    for (long long ex = 0; ex < L.nx; ++ex) {
+                        const long long e = (ez * L.ny + ey) * L.nx + ex;
+                        const long long hidx =
+                            cfgs[p].layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
+                        rho_out[o + hidx] = r[eo + e];
+                    }
+            o += (size_t)L.nel;
+        }
+    }
+    for (int p = 0; p < n; ++p) {
+        if (iterations) iterations[p] = its[p];
+        if (converged) converged[p] = conv[p];
+        if (pcg_iterations) pcg_iterations[p] = B->pcg_its[p];
+    }
+    return AM_OK;
+}
+
+}  // extern "C"

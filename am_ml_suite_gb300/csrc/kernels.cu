@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 
+#include "batch.cuh"
 #include "kernels.cuh"
 #include "ku.cuh"
 #include "ku2.cuh"
@@ -236,10 +237,9 @@ constexpr int VEC_THREADS = 256;
 // x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer the K*u
 // kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
 template <typename T>
-__global__ void __launch_bounds__(VEC_THREADS)
-    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
+__device__ __forceinline__ void pcg_update_body(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
                       const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
-                      Scalars *S) {
+                      Scalars *S, const Blk B) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag;
     if (S->done) return;
@@ -251,8 +251,8 @@ __global__ void __launch_bounds__(VEC_THREADS)
         // four nodes per thread and step (cs is a multiple of 64, rows 16-byte
         // aligned): all 13 vector loads are issued before the 6 stores
         const long long n4 = cs / 4;
-        for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4;
-             k += (long long)gridDim.x * blockDim.x) {
+        for (long long k = B.b * (long long)blockDim.x + threadIdx.x; k < n4;
+             k += (long long)B.n * blockDim.x) {
             const float4 d = __ldg(reinterpret_cast<const float4 *>(dinv) + k);
             float4 xv[3], rv[3], pv[3], qv[3];
 #pragma unroll
@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(VEC_THREADS)
         }
     } else {
         // one node per thread and step, its three component planes
-        for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
-             n += (long long)gridDim.x * blockDim.x) {
+        for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < cs;
+             n += (long long)B.n * blockDim.x) {
             const T d = dinv[n];
             T xv[3], rv[3], pv[3], qv[3];
 #pragma unroll
@@ -318,12 +318,12 @@ __global__ void __launch_bounds__(VEC_THREADS)
     double v[2] = {a0.value(), a1.value()};
     block_sum<2>(v, red);
     if (threadIdx.x == 0) {
-        partial[2 * blockIdx.x] = v[0];
-        partial[2 * blockIdx.x + 1] = v[1];
+        partial[2 * B.b] = v[0];
+        partial[2 * B.b + 1] = v[1];
     }
-    if (!arrive_last(&S->cnt_upd, &last_flag)) return;
+    if (!arrive_last_n(&S->cnt_upd, &last_flag, B.n)) return;
     double tot[2];
-    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    reduce_partials<2>(partial, B.n, 2, tot, red);
     if (threadIdx.x == 0) {
         const double rr = tot[0], rz = tot[1];
         S->it += 1;
@@ -347,6 +347,13 @@ __global__ void __launch_bounds__(VEC_THREADS)
         S->cnt_upd = 0;
     }
 }
+template <typename T>
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
+                      const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
+                      Scalars *S) {
+    pcg_update_body<T>(L, x, r, pa, pb, q, dinv, partial, S, grid_blk());
+}
 
 template <typename T>
 cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
@@ -367,15 +374,14 @@ template cudaError_t pcg_update<double>(const Layout &, double *, double *, cons
 // sequence; upd_factor: a reliable update is requested when |r|^2 falls below
 // upd_factor * (this |r|^2) (0 disables).  maxit caps S->it.
 template <typename T>
-__global__ void __launch_bounds__(VEC_THREADS)
-    pcg_start_kernel(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double thr,
-                     double upd_factor, int maxit, int restart, double *partial, Scalars *S) {
+__device__ __forceinline__ void pcg_start_body(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double thr,
+                     double upd_factor, int maxit, int restart, double *partial, Scalars *S, const Blk B) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag;
     const long long cs = L.cs;
     Acc<T> a0, a1;
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
-         n += (long long)gridDim.x * blockDim.x) {
+    for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)B.n * blockDim.x) {
         const T d = dinv[n];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -387,12 +393,12 @@ __global__ void __launch_bounds__(VEC_THREADS)
     double v[2] = {a0.value(), a1.value()};
     block_sum<2>(v, red);
     if (threadIdx.x == 0) {
-        partial[2 * blockIdx.x] = v[0];
-        partial[2 * blockIdx.x + 1] = v[1];
+        partial[2 * B.b] = v[0];
+        partial[2 * B.b + 1] = v[1];
     }
-    if (!arrive_last(&S->cnt_upd, &last_flag)) return;
+    if (!arrive_last_n(&S->cnt_upd, &last_flag, B.n)) return;
     double tot[2];
-    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    reduce_partials<2>(partial, B.n, 2, tot, red);
     if (threadIdx.x == 0) {
         S->rr = tot[0];
         if (restart == 1) {
@@ -424,6 +430,12 @@ __global__ void __launch_bounds__(VEC_THREADS)
         S->cnt_upd = 0;
     }
 }
+template <typename T>
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_start_kernel(Layout L, const T *__restrict__ r, const T *__restrict__ dinv, double thr,
+                     double upd_factor, int maxit, int restart, double *partial, Scalars *S) {
+    pcg_start_body<T>(L, r, dinv, thr, upd_factor, maxit, restart, partial, S, grid_blk());
+}
 
 template <typename T>
 cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,
@@ -436,15 +448,19 @@ template cudaError_t pcg_start<float>(const Layout &, const float *, const float
 template cudaError_t pcg_start<double>(const Layout &, const double *, const double *, double, double, int, int,
                                        double *, Scalars *, int, cudaStream_t);
 
-__global__ void dc_inner_init_kernel(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
-                                     float *__restrict__ x32, const Scalars *S) {
+__device__ __forceinline__ void dc_inner_init_body(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
+                                     float *__restrict__ x32, const Scalars *S, const Blk B) {
     (void)S;
     const long long n = 3 * L.cs;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+    for (long long i = B.b * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)B.n * blockDim.x) {
         r32[i] = (float)r64[i];
         x32[i] = 0.f;
     }
+}
+__global__ void dc_inner_init_kernel(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
+                                     float *__restrict__ x32, const Scalars *S) {
+    dc_inner_init_body(L, r64, r32, x32, S, grid_blk());
 }
 cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
                           const Scalars *S, int nblocks, cudaStream_t st) {
@@ -453,16 +469,19 @@ cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float 
 }
 
 // x = 0 on the constrained / orphan components (bit c of mask[n] set)
-__global__ void zero_masked_kernel(Layout L, const uint8_t *__restrict__ mask, double *__restrict__ x) {
+__device__ __forceinline__ void zero_masked_body(Layout L, const uint8_t *__restrict__ mask, double *__restrict__ x, const Blk B) {
     const long long cs = L.cs;
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < cs;
-         n += (long long)gridDim.x * blockDim.x) {
+    for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)B.n * blockDim.x) {
         const unsigned m = mask[n];
         if (!m) continue;
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             if ((m >> c) & 1u) x[n + c * cs] = 0.0;
     }
+}
+__global__ void zero_masked_kernel(Layout L, const uint8_t *__restrict__ mask, double *__restrict__ x) {
+    zero_masked_body(L, mask, x, grid_blk());
 }
 // ---- outer flexible CG (FP64), preconditioned by an inner solve z = M(r) ------
 // Flexible CG with one stored direction and the Polak-Ribiere beta
@@ -571,11 +590,11 @@ __device__ __forceinline__ double pow_fast(double x, double p) {
     return pow(x, p);
 }
 
-__global__ void scales_kernel(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
+__device__ __forceinline__ void scales_body(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
                               int variant, double p, double emin, double rho_min, double E,
-                              double *__restrict__ s64, float *__restrict__ s32) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
-         e += (long long)gridDim.x * blockDim.x) {
+                              double *__restrict__ s64, float *__restrict__ s32, const Blk B) {
+    for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)B.n * blockDim.x) {
         const int g = grid ? grid[e] : 0;
         const double r = rho[e];
         double v;
@@ -592,6 +611,11 @@ __global__ void scales_kernel(Layout L, const double *__restrict__ rho, const in
         if (s32) s32[e] = (float)v;
     }
 }
+__global__ void scales_kernel(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
+                              int variant, double p, double emin, double rho_min, double E,
+                              double *__restrict__ s64, float *__restrict__ s32) {
+    scales_body(L, rho, grid, variant, p, emin, rho_min, E, s64, s32, grid_blk());
+}
 cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int variant, double p,
                    double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st) {
     const int nb = std::max(1, std::min(div_up(L.nel, 256), 152 * 16));
@@ -599,12 +623,12 @@ cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int v
     return counted(cudaGetLastError());
 }
 
-__global__ void diag_mask_kernel(Layout L, const double *__restrict__ s, double d0,
+__device__ __forceinline__ void diag_mask_body(Layout L, const double *__restrict__ s, double d0,
                                  const uint8_t *__restrict__ fixed_bits, double *__restrict__ dinv64,
-                                 float *__restrict__ dinv32, uint8_t *__restrict__ mask) {
+                                 float *__restrict__ dinv32, uint8_t *__restrict__ mask, const Blk B) {
     const long long nn = L.sxy * (L.nz + 1);
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
-         n += (long long)gridDim.x * blockDim.x) {
+    for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < nn;
+         n += (long long)B.n * blockDim.x) {
         const int iz = (int)(n / L.sxy);
         const long long rem = n - (long long)iz * L.sxy;
         const int iy = (int)(rem / L.sx), ix = (int)(rem - (long long)iy * L.sx);
@@ -632,6 +656,11 @@ __global__ void diag_mask_kernel(Layout L, const double *__restrict__ s, double 
         if (dinv64) dinv64[n] = di;
         if (dinv32) dinv32[n] = (float)di;
     }
+}
+__global__ void diag_mask_kernel(Layout L, const double *__restrict__ s, double d0,
+                                 const uint8_t *__restrict__ fixed_bits, double *__restrict__ dinv64,
+                                 float *__restrict__ dinv32, uint8_t *__restrict__ mask) {
+    diag_mask_body(L, s, d0, fixed_bits, dinv64, dinv32, mask, grid_blk());
 }
 cudaError_t diag_mask(const Layout &L, const double *s64, double d0, const uint8_t *fixed_bits,
                       double *dinv64, float *dinv32, uint8_t *mask, cudaStream_t st) {
@@ -731,11 +760,11 @@ template cudaError_t elem_from_dev<double>(const Layout &, const double *, doubl
 // filters
 // ============================================================================
 template <typename T>
-__global__ void filter_cpp_kernel(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw,
+__device__ __forceinline__ void filter_cpp_body(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw,
                                   int ntaps, const double *__restrict__ x, const double *__restrict__ rho,
-                                  double *__restrict__ out) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
-         e += (long long)gridDim.x * blockDim.x) {
+                                  double *__restrict__ out, const Blk B) {
+    for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)B.n * blockDim.x) {
         const int ex = (int)(e % L.nx);
         const long long t = e / L.nx;
         const int ey = (int)(t % L.ny), ez = (int)(t / L.ny);
@@ -752,6 +781,12 @@ __global__ void filter_cpp_kernel(Layout L, const int4 *__restrict__ td, const d
         }
         out[e] = (den > T(1e-15)) ? (double)(num / den) : x[e];
     }
+}
+template <typename T>
+__global__ void filter_cpp_kernel(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw,
+                                  int ntaps, const double *__restrict__ x, const double *__restrict__ rho,
+                                  double *__restrict__ out) {
+    filter_cpp_body<T>(L, td, tw, ntaps, x, rho, out, grid_blk());
 }
 template <typename T>
 cudaError_t filter_cpp(const Layout &L, const Taps &tp, const double *x, const double *rho,
@@ -811,15 +846,14 @@ template cudaError_t filter_py<double>(const Layout &, const Taps &, const doubl
 // ============================================================================
 // sensitivities
 // ============================================================================
-__global__ void __launch_bounds__(256)
-    sens_kernel(Layout L, const double *__restrict__ rho, const double *__restrict__ ce,
+__device__ __forceinline__ void sens_body(Layout L, const double *__restrict__ rho, const double *__restrict__ ce,
                 const double *__restrict__ s, const uint8_t *__restrict__ design, int variant,
-                double p, double *__restrict__ dc, int accumulate, double *partial, Scalars *S) {
+                double p, double *__restrict__ dc, int accumulate, double *partial, Scalars *S, const Blk B) {
     __shared__ double red[256 / 32];
     __shared__ int last_flag;
     double en = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < L.nel;
-         e += (long long)gridDim.x * blockDim.x) {
+    for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < L.nel;
+         e += (long long)B.n * blockDim.x) {
         const double c = ce[e];
         en = fma(s[e], c, en);  // void elements have s = 0
         if (variant == 0) {
@@ -832,14 +866,20 @@ __global__ void __launch_bounds__(256)
     }
     double v[1] = {en};
     block_sum<1>(v, red);
-    if (threadIdx.x == 0) partial[blockIdx.x] = v[0];
-    if (!arrive_last(&S->cnt_misc, &last_flag)) return;
+    if (threadIdx.x == 0) partial[B.b] = v[0];
+    if (!arrive_last_n(&S->cnt_misc, &last_flag, B.n)) return;
     double tot[1];
-    reduce_partials<1>(partial, gridDim.x, 1, tot, red);
+    reduce_partials<1>(partial, B.n, 1, tot, red);
     if (threadIdx.x == 0) {
         S->comp_energy = accumulate ? S->comp_energy + tot[0] : tot[0];
         S->cnt_misc = 0;
     }
+}
+__global__ void __launch_bounds__(256)
+    sens_kernel(Layout L, const double *__restrict__ rho, const double *__restrict__ ce,
+                const double *__restrict__ s, const uint8_t *__restrict__ design, int variant,
+                double p, double *__restrict__ dc, int accumulate, double *partial, Scalars *S) {
+    sens_body(L, rho, ce, s, design, variant, p, dc, accumulate, partial, S, grid_blk());
 }
 cudaError_t sensitivities(const Layout &L, const double *rho, const double *ce, const double *s,
                           const uint8_t *design, int variant, double p, double *dc, int accumulate,
@@ -849,8 +889,8 @@ cudaError_t sensitivities(const Layout &L, const double *rho, const double *ce, 
     return counted(cudaGetLastError());
 }
 
-__global__ void sparse_dot_kernel(const long long *idx, const double *val, int n, const double *u,
-                                  double *out) {
+__device__ __forceinline__ void sparse_dot_body(const long long *idx, const double *val, int n, const double *u,
+                                  double *out, const Blk B) {
     __shared__ double red[256 / 32];
     double acc = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(val[i], u[idx[i]], acc);
@@ -858,14 +898,18 @@ __global__ void sparse_dot_kernel(const long long *idx, const double *val, int n
     block_sum<1>(v, red);
     if (threadIdx.x == 0) *out = v[0];
 }
+__global__ void sparse_dot_kernel(const long long *idx, const double *val, int n, const double *u,
+                                  double *out) {
+    sparse_dot_body(idx, val, n, u, out, grid_blk());
+}
 cudaError_t sparse_dot(const long long *idx, const double *val, int n, const double *u,
                        double *out, cudaStream_t st) {
     sparse_dot_kernel<<<1, 256, 0, st>>>(idx, val, n, u, out);
     return counted(cudaGetLastError());
 }
 
-__global__ void masked_sqnorm_kernel(const long long *idx, const double *val, int n, long long cs,
-                                     const uint8_t *mask, double *out) {
+__device__ __forceinline__ void masked_sqnorm_body(const long long *idx, const double *val, int n, long long cs,
+                                     const uint8_t *mask, double *out, const Blk B) {
     __shared__ double red[256 / 32];
     double acc = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -877,6 +921,10 @@ __global__ void masked_sqnorm_kernel(const long long *idx, const double *val, in
     double v[1] = {acc};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) *out = v[0];
+}
+__global__ void masked_sqnorm_kernel(const long long *idx, const double *val, int n, long long cs,
+                                     const uint8_t *mask, double *out) {
+    masked_sqnorm_body(idx, val, n, cs, mask, out, grid_blk());
 }
 cudaError_t masked_sqnorm(const long long *idx, const double *val, int n, long long cs,
                           const uint8_t *mask, double *out, cudaStream_t st) {
@@ -922,9 +970,9 @@ struct OcPrepArgs {
     Scalars *S;
 };
 
-__global__ void oc_prepare_kernel(OcPrepArgs A) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.nel;
-         e += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void oc_prepare_body(OcPrepArgs A, const Blk B) {
+    for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < A.nel;
+         e += (long long)B.n * blockDim.x) {
         const double r = A.rho[e];
         const double a = r * sqrt(-A.dc[e]);
         const double lo = r - A.move, hi = r + A.move;
@@ -938,7 +986,7 @@ __global__ void oc_prepare_kernel(OcPrepArgs A) {
             A.hi32[e] = df_of(hi);
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (B.b == 0 && threadIdx.x == 0) {
         Scalars *S = A.S;
         const double l1 = A.variant == 0 ? 1e-20 : 1e-9;
         const double l2 = A.variant == 0 ? 1e20 : 1e9;
@@ -951,6 +999,9 @@ __global__ void oc_prepare_kernel(OcPrepArgs A) {
         S->oc_done = 0;
         S->oc_variant = A.variant;
     }
+}
+__global__ void oc_prepare_kernel(OcPrepArgs A) {
+    oc_prepare_body(A, grid_blk());
 }
 cudaError_t oc_prepare(const OcBuffers &B, const double *rho, const double *dc, double move, int fp64,
                        int variant, Scalars *S, cudaStream_t st) {
@@ -1011,7 +1062,7 @@ struct OcPassArgs {
 };
 
 // One bisection pass: volume of the design elements at the current t.
-__global__ void __launch_bounds__(256) oc_pass_kernel(OcPassArgs A) {
+__device__ __forceinline__ void oc_pass_body(OcPassArgs A, const Blk B) {
     __shared__ double red[256 / 32];
     __shared__ int last_flag;
     Scalars *S = A.S;
@@ -1020,15 +1071,15 @@ __global__ void __launch_bounds__(256) oc_pass_kernel(OcPassArgs A) {
     double vol64 = 0.0;
     DF vol{0.f, 0.f};
     if (A.fp64) {
-        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
-             e += (long long)gridDim.x * blockDim.x) {
+        for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+             e += (long long)B.n * blockDim.x) {
             if (!A.design[e]) continue;
             vol64 += oc_clamp<double>(A.B.a64[e] * t, A.B.lo64[e], A.B.hi64[e], A.rho_min, A.variant);
         }
     } else {
         const float2 tdf = df_of(t), rmin = df_of(A.rho_min);
-        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
-             e += (long long)gridDim.x * blockDim.x) {
+        for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+             e += (long long)B.n * blockDim.x) {
             if (!A.design[e]) continue;
             const float2 v = oc_clamp_df(df_mul(A.B.a32[e], tdf), A.B.lo32[e], A.B.hi32[e], rmin, A.variant);
             df_add(vol, v.x);
@@ -1038,14 +1089,17 @@ __global__ void __launch_bounds__(256) oc_pass_kernel(OcPassArgs A) {
     }
     double v[1] = {vol64};
     block_sum<1>(v, red);
-    if (threadIdx.x == 0) A.partial[blockIdx.x] = v[0];
-    if (!arrive_last(&S->cnt_oc, &last_flag)) return;
+    if (threadIdx.x == 0) A.partial[B.b] = v[0];
+    if (!arrive_last_n(&S->cnt_oc, &last_flag, B.n)) return;
     double tot[1];
-    reduce_partials<1>(A.partial, gridDim.x, 1, tot, red);
+    reduce_partials<1>(A.partial, B.n, 1, tot, red);
     if (threadIdx.x == 0) {
         oc_stop_check(S, tot[0] / A.n_design, A.vf, A.variant);
         S->cnt_oc = 0;
     }
+}
+__global__ void __launch_bounds__(256) oc_pass_kernel(OcPassArgs A) {
+    oc_pass_body(A, grid_blk());
 }
 cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min, double vf,
                     double n_design, double *partial, Scalars *S, int nblocks, cudaStream_t st) {
@@ -1060,16 +1114,16 @@ cudaError_t oc_pass(const OcBuffers &B, const uint8_t *design, int fp64, int var
 // and 1 must come out exact, because the next stiffness skips elements with
 // rho < rho_min -- a double-float rho_min (48 bits) lands one ulp below it.  Only
 // the multiplier t comes from the (double-float or FP64) bisection passes.
-__global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const double *__restrict__ rho,
+__device__ __forceinline__ void oc_final_body(OcPassArgs A, const double *__restrict__ rho,
                                                        const double *__restrict__ dc, double move,
-                                                       double *__restrict__ rho_new) {
+                                                       double *__restrict__ rho_new, const Blk B) {
     __shared__ double red[2 * (256 / 32)];
     __shared__ int last_flag;
     Scalars *S = A.S;
     const double t = S->oc_t_last;
     double mc = 0.0, vs = 0.0, cnt = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
-         e += (long long)gridDim.x * blockDim.x) {
+    for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < A.B.nel;
+         e += (long long)B.n * blockDim.x) {
         const double r0 = rho[e];
         double v = r0;
         if (A.design[e]) {
@@ -1087,14 +1141,14 @@ __global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const doubl
     double s2[2] = {vs, cnt};
     block_sum<2>(s2, red);
     if (threadIdx.x == 0) {
-        A.partial[3 * blockIdx.x] = m;
-        A.partial[3 * blockIdx.x + 1] = s2[0];
-        A.partial[3 * blockIdx.x + 2] = s2[1];
+        A.partial[3 * B.b] = m;
+        A.partial[3 * B.b + 1] = s2[0];
+        A.partial[3 * B.b + 2] = s2[1];
     }
-    if (!arrive_last(&S->cnt_oc, &last_flag)) return;
+    if (!arrive_last_n(&S->cnt_oc, &last_flag, B.n)) return;
     if (threadIdx.x == 0) {
         double mm = 0.0, ss = 0.0, cc = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) {
+        for (unsigned b = 0; b < B.n; ++b) {
             mm = fmax(mm, __ldcg(A.partial + 3 * b));
             ss += __ldcg(A.partial + 3 * b + 1);
             cc += __ldcg(A.partial + 3 * b + 2);
@@ -1104,6 +1158,11 @@ __global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const doubl
         S->cnt_oc = 0;
     }
 }
+__global__ void __launch_bounds__(256) oc_final_kernel(OcPassArgs A, const double *__restrict__ rho,
+                                                       const double *__restrict__ dc, double move,
+                                                       double *__restrict__ rho_new) {
+    oc_final_body(A, rho, dc, move, rho_new, grid_blk());
+}
 cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int variant, double rho_min,
                      const double *rho, const double *dc, double move, double *rho_new, double *partial, Scalars *S,
                      int nblocks, cudaStream_t st) {
@@ -1111,5 +1170,286 @@ cudaError_t oc_final(const OcBuffers &B, const uint8_t *design, int fp64, int va
     oc_final_kernel<<<nblocks, 256, 0, st>>>(a, rho, dc, move, rho_new);
     return counted(cudaGetLastError());
 }
+
+
+// ============================================================================
+// Batched persistent kernels (batch.cuh).  Each CTA loops over the work items of
+// its family; an item runs the single-problem body with the item's block index
+// and its problem's block count.  Frozen problems are skipped by every family,
+// problems whose PCG is done by the PCG bodies themselves.
+// ============================================================================
+#define AMK_BATCH_LOOP(WL)                                  \
+    for (int _w = blockIdx.x; _w < (WL).n; _w += gridDim.x) \
+        if (const int2 _k = (WL).w[_w]; true)
+
+__global__ void __launch_bounds__(256) b_scales_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        scales_body(it.L, it.rho, nullptr, 0, it.penalty, it.emin, it.rho_min, 1.0, it.s64, it.s32,
+                    Blk{_k.y, it.n_elem});
+    }
+}
+__global__ void __launch_bounds__(256) b_diag_kernel(const BatchItem *items, WorkList W, double d0) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        diag_mask_body(it.L, it.s64, d0, it.fixed_bits, it.dinv64, it.dinv32, it.mask, Blk{_k.y, it.n_vec});
+    }
+}
+cudaError_t batch_operator(const BatchItem *it, WorkList elem, WorkList vec, const BatchConst &C, int grid,
+                           cudaStream_t st) {
+    b_scales_kernel<<<std::max(1, std::min(grid, elem.n)), 256, 0, st>>>(it, elem);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_diag_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec, C.d0);
+    return counted(cudaGetLastError());
+}
+
+__global__ void __launch_bounds__(256) b_zero_masked_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        zero_masked_body(it.L, it.mask, it.x64, Blk{_k.y, it.n_vec});
+    }
+}
+__global__ void __launch_bounds__(256) b_sqnorm_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        masked_sqnorm_body(it.f_idx, it.f_val, it.f_nnz, it.L.cs, it.mask, &it.S->b2, Blk{0, 1});
+        __syncthreads();
+    }
+}
+cudaError_t batch_prepare_solve(const BatchItem *it, WorkList vec, WorkList prob, int grid, cudaStream_t st) {
+    b_zero_masked_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_sqnorm_kernel<<<std::max(1, std::min(grid, prob.n)), 256, 0, st>>>(it, prob);
+    return counted(cudaGetLastError());
+}
+
+__global__ void __launch_bounds__(KuShape<32, 4>::NT) b_resid_kernel(const BatchItem *items, WorkList W,
+                                                                     Modal<double> M, int energy) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        KuArgs<double> a{};
+        a.L = it.L;
+        a.M = M;
+        a.s = it.s64;
+        a.u = it.x64;
+        a.f = it.F;
+        a.dinv = it.dinv64;
+        a.mask = it.mask;
+        a.y = it.r64;
+        a.ce = energy ? it.ce : nullptr;
+        a.energy = energy;
+        a.partial = it.partial;
+        a.S = it.S;
+        a.tiles_x = it.k64_tiles_x;
+        a.tiles_y = it.k64_tiles_y;
+        a.tiles_z = it.k64_tiles_z;
+        a.tz = it.k64_tz;
+        ku_tile_body<double, 32, 4, KU_RESID>(a, Blk{_k.y, it.n_k64});
+        __syncthreads();
+    }
+}
+cudaError_t batch_resid(const BatchItem *it, WorkList k64, const BatchConst &C, int energy, int grid,
+                        cudaStream_t st) {
+    using Sh = KuShape<32, 4>;
+    const size_t smem = Sh::template smem_bytes<double>();
+    b_resid_kernel<<<std::max(1, std::min(grid, k64.n)), Sh::NT, smem, st>>>(it, k64, C.M64, energy);
+    return counted(cudaGetLastError());
+}
+
+__global__ void __launch_bounds__(256) b_inner_init_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        dc_inner_init_body(it.L, it.r64, it.r32, it.x32, it.S, Blk{_k.y, it.n_vec});
+    }
+}
+// FP32 PCG on K x32 = r32 to |r| <= tol/2 |F| (but at most 1e-6 below its start);
+// a problem whose FP64 residual already meets tol starts done.
+__global__ void __launch_bounds__(256) b_inner_start_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        const double b2 = it.S->b2, rr = it.S->res_rr;
+        const double tol2 = it.tol * it.tol;
+        const double thr = (rr <= tol2 * b2) ? 1e300 : fmax(0.25 * tol2 * b2, 1e-12 * rr);
+        pcg_start_body<float>(it.L, it.r32, it.dinv32, thr, 0.0, it.maxit, 0, it.partial, it.S,
+                              Blk{_k.y, it.n_vec});
+        __syncthreads();
+    }
+}
+cudaError_t batch_inner_start(const BatchItem *it, WorkList vec, int grid, cudaStream_t st) {
+    b_inner_init_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_inner_start_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
+    return counted(cudaGetLastError());
+}
+
+template <int W_, int MODE>
+__global__ void __launch_bounds__(32 * W_, 2) b_ku2_kernel(const BatchItem *items, WorkList W, Modal<float> M) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        Ku2Args a{};
+        a.L = it.L;
+        a.M = M;
+        a.s = it.s32;
+        a.u = it.pa;
+        a.pa = it.pa;
+        a.pb = it.pb;
+        a.r = it.r32;
+        a.dinv = it.dinv32;
+        a.mask = it.mask;
+        a.y = it.q32;
+        a.partial = it.partial;
+        a.S = it.S;
+        a.tiles_x = it.k2_tiles_x;
+        a.tiles_y = it.k2_tiles_y;
+        a.tiles_z = it.k2_tiles_z;
+        a.tz = it.k2_tz;
+        ku2_body<W_, MODE>(a, Blk{_k.y, it.n_k2});
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) b_update_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        pcg_update_body<float>(it.L, it.x32, it.r32, it.pa, it.pb, it.q32, it.dinv32, it.partial, it.S,
+                               Blk{_k.y, it.n_vec});
+        __syncthreads();
+    }
+}
+cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, const BatchConst &C, int warps,
+                                int grid_k2, int grid_vec, cudaStream_t st) {
+    const int g2 = std::max(1, std::min(grid_k2, k2.n));
+    if (warps == 8) b_ku2_kernel<8, KU_PCG><<<g2, 256, 0, st>>>(it, k2, C.M32);
+    else if (warps == 4) b_ku2_kernel<4, KU_PCG><<<g2, 128, 0, st>>>(it, k2, C.M32);
+    else return cudaErrorInvalidValue;
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_update_kernel<<<std::max(1, std::min(grid_vec, vec.n)), 256, 0, st>>>(it, vec);
+    return counted(cudaGetLastError());
+}
+cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
+                           cudaStream_t st) {
+    const int g2 = std::max(1, std::min(grid, k2.n));
+    if (warps == 8) b_ku2_kernel<8, KU_PLAIN><<<g2, 256, 0, st>>>(it, k2, C.M32);
+    else if (warps == 4) b_ku2_kernel<4, KU_PLAIN><<<g2, 128, 0, st>>>(it, k2, C.M32);
+    else return cudaErrorInvalidValue;
+    return counted(cudaGetLastError());
+}
+
+__global__ void __launch_bounds__(256) b_accumulate_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        const long long n = 3 * it.L.cs;
+        for (long long i = (long long)_k.y * blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x)
+            it.x64[i] += (double)it.x32[i];
+    }
+}
+cudaError_t batch_accumulate(const BatchItem *it, WorkList vec, int grid, cudaStream_t st) {
+    b_accumulate_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
+    return counted(cudaGetLastError());
+}
+
+__global__ void __launch_bounds__(256) b_sens_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        sens_body(it.L, it.rho, it.ce, it.s64, it.design, 0, it.penalty, it.dc, 0, it.partial, it.S,
+                  Blk{_k.y, it.n_elem});
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) b_fu_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        sparse_dot_body(it.f_idx, it.f_val, it.f_nnz, it.x64, &it.S->comp_fu, Blk{0, 1});
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) b_filter_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        filter_cpp_body<double>(it.L, it.tap_d, it.tap_w, it.ntaps, it.dc, it.rho, it.dcf, Blk{_k.y, it.n_elem});
+    }
+}
+__device__ __forceinline__ OcPassArgs batch_oc_args(const BatchItem &it) {
+    OcPassArgs a{};
+    a.B.nel = it.L.nel;
+    a.B.a64 = it.oc_a;
+    a.B.lo64 = it.oc_lo;
+    a.B.hi64 = it.oc_hi;
+    a.design = it.design;
+    a.fp64 = 1;
+    a.variant = 0;
+    a.rho_min = it.rho_min;
+    a.vf = it.vf;
+    a.n_design = it.n_design;
+    a.partial = it.partial;
+    a.S = it.S;
+    return a;
+}
+__global__ void __launch_bounds__(256) b_oc_prepare_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        OcPrepArgs a{it.L.nel, it.rho, it.dcf, it.oc_a, it.oc_lo, it.oc_hi, nullptr, nullptr, nullptr,
+                     it.move, 1, 0, it.S};
+        oc_prepare_body(a, Blk{_k.y, it.n_elem});
+    }
+}
+__global__ void __launch_bounds__(256) b_oc_pass_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        oc_pass_body(batch_oc_args(it), Blk{_k.y, it.n_elem});
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) b_oc_final_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        oc_final_body(batch_oc_args(it), it.rho, it.dcf, it.move, it.rho_new, Blk{_k.y, it.n_elem});
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) b_copy_density_kernel(const BatchItem *items, WorkList W) {
+    AMK_BATCH_LOOP(W) {
+        const BatchItem &it = items[_k.x];
+        if (it.S->frozen) continue;
+        for (long long e = (long long)_k.y * blockDim.x + threadIdx.x; e < it.L.nel;
+             e += (long long)it.n_elem * blockDim.x)
+            it.rho[e] = it.rho_new[e];
+    }
+}
+cudaError_t batch_update(const BatchItem *it, WorkList elem, WorkList prob, int grid, cudaStream_t st) {
+    const int ge = std::max(1, std::min(grid, elem.n)), gp = std::max(1, std::min(grid, prob.n));
+    b_sens_kernel<<<ge, 256, 0, st>>>(it, elem);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_fu_kernel<<<gp, 256, 0, st>>>(it, prob);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_filter_kernel<<<ge, 256, 0, st>>>(it, elem);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_oc_prepare_kernel<<<ge, 256, 0, st>>>(it, elem);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    for (int k = 0; k < 100; ++k) {
+        b_oc_pass_kernel<<<ge, 256, 0, st>>>(it, elem);
+        if (cudaError_t e = counted(cudaGetLastError())) return e;
+    }
+    b_oc_final_kernel<<<ge, 256, 0, st>>>(it, elem);
+    if (cudaError_t e = counted(cudaGetLastError())) return e;
+    b_copy_density_kernel<<<ge, 256, 0, st>>>(it, elem);
+    return counted(cudaGetLastError());
+}
+#undef AMK_BATCH_LOOP
 
 }  // namespace amk

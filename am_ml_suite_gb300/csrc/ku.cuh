@@ -150,8 +150,10 @@ struct KuShape {
     }
 };
 
+// One tile (block B.b of B.n) of the tiled K*u; the kernel below runs one tile
+// per CTA, the batched persistent kernel one tile per work item.
 template <typename T, int TX, int TY, int MODE>
-__global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> A) {
+__device__ __forceinline__ void ku_tile_body(KuArgs<T> A, const Blk B) {
     using Sh = KuShape<TX, TY>;
     constexpr int EX = Sh::EX, NE = Sh::NE, SX = Sh::SX, NS = Sh::NS, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
     if (MODE == KU_PCG && A.S->done) return;
     const Layout L = A.L;
     const int tid = threadIdx.x;
-    int b = blockIdx.x;
+    int b = B.b;
     const int tx_ = b % A.tiles_x;
     b /= A.tiles_x;
     const int ty_ = b % A.tiles_y;
@@ -326,12 +328,12 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
     double v[2] = {d0.value(), d1.value()};
     block_sum<2>(v, red);
     if (tid == 0) {
-        A.partial[2 * blockIdx.x] = v[0];
-        A.partial[2 * blockIdx.x + 1] = v[1];
+        A.partial[2 * B.b] = v[0];
+        A.partial[2 * B.b + 1] = v[1];
     }
-    if (!arrive_last(&A.S->cnt_ku, &last_flag)) return;
+    if (!arrive_last_n(&A.S->cnt_ku, &last_flag, B.n)) return;
     double tot[2];
-    reduce_partials<2>(A.partial, gridDim.x, 2, tot, red);
+    reduce_partials<2>(A.partial, B.n, 2, tot, red);
     if (tid == 0) {
         Scalars *S = A.S;
         if (MODE == KU_PCG) {
@@ -359,6 +361,11 @@ __global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> 
         }
         S->cnt_ku = 0;
     }
+}
+
+template <typename T, int TX, int TY, int MODE>
+__global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_tile_kernel(KuArgs<T> A) {
+    ku_tile_body<T, TX, TY, MODE>(A, grid_blk());
 }
 
 }  // namespace amk

@@ -68,8 +68,10 @@ __device__ __forceinline__ Face face_modes(float v0, float v1, float v2, float n
 }
 }  // namespace k2
 
+// One tile (block B.b of B.n); ku2_kernel runs one tile per CTA, the batched
+// persistent kernel one tile per work item.
 template <int W, int MODE>
-__global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
+__device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     using namespace k2;
     constexpr int TY = 2 * W - 1;
     __shared__ float xch[2][W][3][32];  // row-2 partials of each warp, double-buffered by layer
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
     if (MODE == KU_PCG && A.S->done) return;
     const Layout L = A.L;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int b = blockIdx.x;
+    int b = B.b;
     const int tx_ = b % A.tiles_x;
     b /= A.tiles_x;
     const int ty_ = b % A.tiles_y;
@@ -310,10 +312,10 @@ __global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
 
     double dv[1] = {dot.value()};
     block_sum<1>(dv, red);
-    if (threadIdx.x == 0) A.partial[2 * blockIdx.x] = dv[0];
-    if (!arrive_last(&A.S->cnt_ku, &last_flag)) return;
+    if (threadIdx.x == 0) A.partial[2 * B.b] = dv[0];
+    if (!arrive_last_n(&A.S->cnt_ku, &last_flag, B.n)) return;
     double tot[1];
-    reduce_partials<1>(A.partial, gridDim.x, 2, tot, red);
+    reduce_partials<1>(A.partial, B.n, 2, tot, red);
     if (threadIdx.x == 0) {
         Scalars *S = A.S;
         const double pq = tot[0];
@@ -327,6 +329,11 @@ __global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
         }
         S->cnt_ku = 0;
     }
+}
+
+template <int W, int MODE>
+__global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
+    ku2_body<W, MODE>(A, grid_blk());
 }
 
 }  // namespace amk

@@ -236,6 +236,45 @@ am_status am_problem_stream(am_problem *p, void **stream);
 am_status am_problem_layout(am_problem *p, long long *nodes, long long *elements, long long *vector_stride,
                             int *ku_tiles);
 
+/* ---- batched SIMP ---------------------------------------------------------------
+ * Many independent C++-variant problems of uneven sizes run together: one launch
+ * of each kernel family per step for the whole batch (persistent CTAs over a
+ * (problem, block) work list), FP32 Jacobi-PCG iterations in CUDA-graph chunks,
+ * FP64 defect correction to each problem's cg_tol, FP64 OC.  The reference runs
+ * one TopologyOptimizer per problem (topology_optimizer.hpp:132-169); per problem
+ * the results follow TopologyOptimizer::run (topology_optimizer.cpp:391-520). */
+typedef struct am_batch am_batch;
+
+/* n problems on the current device; problem i has shapes[3i] x shapes[3i+1] x
+ * shapes[3i+2] cubic elements of edge h; material (E0, nu) is shared. */
+am_status am_batch_create(int n, const int *shapes, double h, double E0, double nu, am_batch **out);
+am_status am_batch_destroy(am_batch *b);
+
+/* One load case per problem: F concatenates the problems' force vectors
+ * (3 (nx+1)(ny+1)(nz+1) entries each, reference DOF order), fixed their
+ * constrained-DOF lists, n_fixed[i] entries for problem i. */
+am_status am_batch_set_loads(am_batch *b, const double *F, const int64_t *fixed, const int64_t *n_fixed);
+
+/* Autotuner of the batched FP32 K*u: times `reps` launches of each candidate plan
+ * (4 or 8 warps per CTA, z chunks of 8, 16 or all node planes, 1-4 CTAs per SM in
+ * the persistent grid) and keeps the fastest for the following runs.  Outputs
+ * (nullable) the chosen plan and its time per launch. */
+am_status am_batch_autotune(am_batch *b, int reps, int *warps, int *z_chunk, int *ctas_per_sm, double *best_ms);
+
+/* The CUDA stream the batch's kernels run on (cudaStream_t). */
+am_status am_batch_stream(am_batch *b, void **stream);
+
+/* Runs every problem's SIMP loop with its own config cfgs[i] (variant must be
+ * AM_VARIANT_CPP; the solve is FP32 Jacobi PCG inside FP64 defect correction to
+ * cfgs[i].cg_tol).  rho0 concatenates the initial densities in each config's
+ * layout (NULL: volume_fraction everywhere); rho_out receives the final ones.
+ * Histories (nullable) are [n][H], H = max_i cfgs[i].max_iterations, entries past
+ * a problem's last iteration untouched; iterations[i], converged[i] and
+ * pcg_iterations[i] (total FP32 PCG iterations) are per problem (nullable). */
+am_status am_batch_simp_run(am_batch *b, const am_simp_config *cfgs, const double *rho0, double *rho_out,
+                            double *compliance_hist, double *volume_hist, int *iterations, int *converged,
+                            long long *pcg_iterations);
+
 /* ---- allocation-free residual (no counterpart in the reference) ----------------
  * For callers that cannot allocate device memory once they are running -- code
  * inside another framework's fixed memory pool, allocation-free real-time or
