@@ -130,6 +130,9 @@ SIGNATURES = {
     "am_batch_set_loads": (ctypes.c_int, [_vp, _dp, _i64p, _i64p]),
     "am_batch_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip, _dp]),
     "am_batch_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "am_batch_simp_begin": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp]),
+    "am_batch_simp_step": (ctypes.c_int, [_vp, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_longlong), _ip]),
+    "am_batch_get_density": (ctypes.c_int, [_vp, _dp]),
     "am_batch_simp_run": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, _dp, _ip, _ip,
                                          ctypes.POINTER(ctypes.c_longlong)]),
     "am_problem_layout": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
@@ -378,6 +381,39 @@ class Batch:
         st = _vp()
         check(load().am_batch_stream(self.handle, ctypes.byref(st)), "am_batch_stream")
         return int(st.value or 0)
+
+    def simp_begin(self, cfgs, rho0_list=None):
+        if len(cfgs) != self.n:
+            raise ValueError("one config per problem")
+        self._cfgs = (SimpConfig * self.n)(*cfgs)
+        r0 = None
+        if rho0_list is not None:
+            r0 = np.ascontiguousarray(np.concatenate([f64(r).ravel() for r in rho0_list]))
+            if r0.size != sum(self.nel):
+                raise ValueError("density size mismatch")
+        check(load().am_batch_simp_begin(self.handle, self._cfgs, ptr(r0)), "am_batch_simp_begin")
+
+    def simp_step(self):
+        """One SIMP iteration of every running problem: (compliance, volume,
+        change) arrays (NaN for problems that did not step) and the number still
+        running; ``self.pcg_iterations`` holds each problem's PCG iterations so far."""
+        c, v, d = (np.full(self.n, np.nan) for _ in range(3))
+        pcg = np.zeros(self.n, np.int64)
+        act = ctypes.c_int(0)
+        check(load().am_batch_simp_step(self.handle, ptr(c), ptr(v), ptr(d),
+                                        pcg.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), ctypes.byref(act)),
+              "am_batch_simp_step")
+        self.pcg_iterations = pcg
+        return c, v, d, act.value
+
+    def densities(self):
+        rho = np.zeros(sum(self.nel))
+        check(load().am_batch_get_density(self.handle, ptr(rho)), "am_batch_get_density")
+        out, o = [], 0
+        for ne in self.nel:
+            out.append(rho[o:o + ne].copy())
+            o += ne
+        return out
 
     def simp_run(self, cfgs, rho0_list=None):
         if len(cfgs) != self.n:

@@ -107,6 +107,11 @@ struct am_batch {
     bool loads_set = false;
     cudaGraphExec_t graph = nullptr;
     std::vector<long long> pcg_its;
+    // SIMP state between am_batch_simp_begin and the steps
+    bool begun = false;
+    std::vector<am_simp_config> cfg;
+    std::vector<int> frozen, iters, conv;
+    int max_chunks = 0;
 };
 
 namespace {
@@ -488,14 +493,11 @@ am_status am_batch_stream(am_batch *B, void **stream) {
     return AM_OK;
 }
 
-am_status am_batch_simp_run(am_batch *B, const am_simp_config *cfgs, const double *rho0, double *rho_out,
-                            double *compliance_hist, double *volume_hist, int *iterations, int *converged,
-                            long long *pcg_iterations) {
+am_status am_batch_simp_begin(am_batch *B, const am_simp_config *cfgs, const double *rho0) {
     BCKS(check_batch(B));
     if (!cfgs) return bfail(AM_ERR_INVALID_ARG, "null configs");
     if (!B->loads_set) return bfail(AM_ERR_INVALID_ARG, "loads not set");
     const int n = B->n;
-    int hist = 0;
     for (int p = 0; p < n; ++p) {
         const am_simp_config &c = cfgs[p];
         const std::string w = "problem " + std::to_string(p) + ": ";
@@ -510,8 +512,8 @@ am_status am_batch_simp_run(am_batch *B, const am_simp_config *cfgs, const doubl
         if (!(c.filter_radius > 0.0) || c.filter_radius > 6.0)
             return bfail(AM_ERR_INVALID_ARG, w + "filter_radius must be in (0, 6]");
         if (c.max_iterations < 0) return bfail(AM_ERR_INVALID_ARG, w + "max_iterations < 0");
-        hist = std::max(hist, c.max_iterations);
     }
+    B->begun = false;
     // densities, design masks, taps, parameters
     std::vector<double> r0(B->nel_tot, 0.0);
     std::vector<uint8_t> dm(B->nel_tot, 0);
@@ -572,65 +574,113 @@ am_status am_batch_simp_run(am_batch *B, const am_simp_config *cfgs, const doubl
     BCK(cudaMemcpy(B->design.p, dm.data(), dm.size(), cudaMemcpyHostToDevice));
     BCK(cudaMemset(B->x64.p, 0, sizeof(double) * B->x64.n));  // cold start; warm starts between steps
     BCK(cudaMemset(B->S.p, 0, sizeof(Scalars) * n));
-    std::vector<int> frozen(n, 0), its(n, 0), conv(n, 0);
+    B->cfg.assign(cfgs, cfgs + n);
+    B->frozen.assign(n, 0);
+    B->iters.assign(n, 0);
+    B->conv.assign(n, 0);
     for (int p = 0; p < n; ++p) {
         if (cfgs[p].max_iterations == 0) {
-            frozen[p] = 1;
-            BCK(cudaMemcpy(&B->S.p[p].frozen, &frozen[p], sizeof(int), cudaMemcpyHostToDevice));
+            B->frozen[p] = 1;
+            BCK(cudaMemcpy(&B->S.p[p].frozen, &B->frozen[p], sizeof(int), cudaMemcpyHostToDevice));
         }
     }
     std::fill(B->pcg_its.begin(), B->pcg_its.end(), 0);
     BCKS(build_graph(B));
-    const int max_chunks = max_maxit / kChunk + 2;
-    for (int step = 0; step < hist; ++step) {
-        if (std::all_of(frozen.begin(), frozen.end(), [](int f) { return f != 0; })) break;
-        BCK(batch_operator(B->items_d.p, B->elem, B->vec, B->C, kSms * 8, B->st));
-        BCK(batch_prepare_solve(B->items_d.p, B->vec, B->prob, kSms * 8, B->st));
-        BCKS(batch_solve(B, max_chunks));
-        BCK(batch_resid(B->items_d.p, B->k64, B->C, 1, kSms * 4, B->st));
-        BCK(batch_update(B->items_d.p, B->elem, B->prob, kSms * 8, B->st));
-        BCKS(sync_scalars(B));
-        for (int p = 0; p < n; ++p) {
-            if (frozen[p]) continue;
-            const Scalars &S = B->Sh[p];
-            const size_t hp = (size_t)p * hist + step;
-            if (compliance_hist) compliance_hist[hp] = S.comp_fu;
-            if (volume_hist) volume_hist[hp] = S.oc_volume;
-            its[p] = step + 1;
-            bool stop = false;
-            if (S.oc_change < cfgs[p].convergence_tol) {
-                conv[p] = 1;
-                stop = true;
-            }
-            if (its[p] >= cfgs[p].max_iterations) stop = true;
-            if (stop) {
-                frozen[p] = 1;
-                BCK(cudaMemcpyAsync(&B->S.p[p].frozen, &frozen[p], sizeof(int), cudaMemcpyHostToDevice, B->st));
-            }
-        }
-        BCK(cudaStreamSynchronize(B->st));
+    B->max_chunks = max_maxit / kChunk + 2;
+    B->begun = true;
+    return AM_OK;
+}
+
+am_status am_batch_simp_step(am_batch *B, double *compliance, double *volume, double *change,
+                             long long *pcg_iterations, int *n_active) {
+    BCKS(check_batch(B));
+    if (!B->begun) return bfail(AM_ERR_INVALID_ARG, "am_batch_simp_begin not called");
+    BCKS(build_graph(B));  // after a re-plan by the autotuner
+    const int n = B->n;
+    if (std::all_of(B->frozen.begin(), B->frozen.end(), [](int f) { return f != 0; })) {
+        if (n_active) *n_active = 0;
+        return AM_OK;
     }
-    if (rho_out) {
-        std::vector<double> r(B->nel_tot);
-        BCK(cudaMemcpy(r.data(), B->rho.p, r.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        size_t o = 0;
-        for (int p = 0; p < n; ++p) {
-            const Layout &L = B->L[p];
-            const size_t eo = B->eoff[p];
-            for (long long ez = 0; ez < L.nz; ++ez)
-                for (long long ey = 0; ey < L.ny; ++ey)
-                    for (long long ex = 0; ex < L.nx; ++ex) {
-                        const long long e = (ez * L.ny + ey) * L.nx + ex;
-                        const long long hidx =
-                            cfgs[p].layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
-                        rho_out[o + hidx] = r[eo + e];
-                    }
-            o += (size_t)L.nel;
-        }
-    }
+    BCK(batch_operator(B->items_d.p, B->elem, B->vec, B->C, kSms * 8, B->st));
+    BCK(batch_prepare_solve(B->items_d.p, B->vec, B->prob, kSms * 8, B->st));
+    BCKS(batch_solve(B, B->max_chunks));
+    BCK(batch_resid(B->items_d.p, B->k64, B->C, 1, kSms * 4, B->st));
+    BCK(batch_update(B->items_d.p, B->elem, B->prob, kSms * 8, B->st));
+    BCKS(sync_scalars(B));
+    int active = 0;
     for (int p = 0; p < n; ++p) {
-        if (iterations) iterations[p] = its[p];
-        if (converged) converged[p] = conv[p];
+        if (B->frozen[p]) continue;
+        const Scalars &S = B->Sh[p];
+        if (compliance) compliance[p] = S.comp_fu;
+        if (volume) volume[p] = S.oc_volume;
+        if (change) change[p] = S.oc_change;
+        B->iters[p] += 1;
+        bool stop = false;
+        if (S.oc_change < B->cfg[p].convergence_tol) {
+            B->conv[p] = 1;
+            stop = true;
+        }
+        if (B->iters[p] >= B->cfg[p].max_iterations) stop = true;
+        if (stop) {
+            B->frozen[p] = 1;
+            BCK(cudaMemcpyAsync(&B->S.p[p].frozen, &B->frozen[p], sizeof(int), cudaMemcpyHostToDevice, B->st));
+        } else {
+            ++active;
+        }
+    }
+    BCK(cudaStreamSynchronize(B->st));
+    if (pcg_iterations)
+        for (int p = 0; p < n; ++p) pcg_iterations[p] = B->pcg_its[p];
+    if (n_active) *n_active = active;
+    return AM_OK;
+}
+
+am_status am_batch_get_density(am_batch *B, double *rho_out) {
+    BCKS(check_batch(B));
+    if (!B->begun) return bfail(AM_ERR_INVALID_ARG, "am_batch_simp_begin not called");
+    if (!rho_out) return bfail(AM_ERR_INVALID_ARG, "null output");
+    std::vector<double> r(B->nel_tot);
+    BCK(cudaMemcpy(r.data(), B->rho.p, r.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    size_t o = 0;
+    for (int p = 0; p < B->n; ++p) {
+        const Layout &L = B->L[p];
+        const size_t eo = B->eoff[p];
+        for (long long ez = 0; ez < L.nz; ++ez)
+            for (long long ey = 0; ey < L.ny; ++ey)
+                for (long long ex = 0; ex < L.nx; ++ex) {
+                    const long long e = (ez * L.ny + ey) * L.nx + ex;
+                    const long long hidx =
+                        B->cfg[p].layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
+                    rho_out[o + hidx] = r[eo + e];
+                }
+        o += (size_t)L.nel;
+    }
+    return AM_OK;
+}
+
+am_status am_batch_simp_run(am_batch *B, const am_simp_config *cfgs, const double *rho0, double *rho_out,
+                            double *compliance_hist, double *volume_hist, int *iterations, int *converged,
+                            long long *pcg_iterations) {
+    BCKS(am_batch_simp_begin(B, cfgs, rho0));
+    const int n = B->n;
+    int hist = 0;
+    for (int p = 0; p < n; ++p) hist = std::max(hist, cfgs[p].max_iterations);
+    std::vector<double> c(n), v(n);
+    for (int step = 0; step < hist; ++step) {
+        int active = 0;
+        std::vector<int> was(B->frozen);
+        BCKS(am_batch_simp_step(B, c.data(), v.data(), nullptr, nullptr, &active));
+        for (int p = 0; p < n; ++p) {
+            if (was[p]) continue;
+            if (compliance_hist) compliance_hist[(size_t)p * hist + step] = c[p];
+            if (volume_hist) volume_hist[(size_t)p * hist + step] = v[p];
+        }
+        if (active == 0) break;
+    }
+    if (rho_out) BCKS(am_batch_get_density(B, rho_out));
+    for (int p = 0; p < n; ++p) {
+        if (iterations) iterations[p] = B->iters[p];
+        if (converged) converged[p] = B->conv[p];
         if (pcg_iterations) pcg_iterations[p] = B->pcg_its[p];
     }
     return AM_OK;

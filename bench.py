@@ -80,6 +80,136 @@ def build_workload(name):
     return dict(shape=shape, rmin=rmin, vf=vf, F=F, fixed=fixed, rho0=rho0, desc=desc)
 
 
+def build_batch256(n=256, seed=3):
+    """256 independent cantilevers: nelx in U{32..96}, nely in U{16..48}, nelz in
+    U{8..48}, vf ~ U(0.2, 0.5), rmin ~ U(1.2, 2.5), clamped x = 0 face, one unit load
+    at a random node of the x = nelx face in a random unit direction."""
+    rng = np.random.default_rng(seed)
+    probs = []
+    for _ in range(n):
+        nx, ny, nz = int(rng.integers(32, 97)), int(rng.integers(16, 49)), int(rng.integers(8, 49))
+        vf, rmin = float(rng.uniform(0.2, 0.5)), float(rng.uniform(1.2, 2.5))
+        N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+        base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+        fixed = (3 * base[:, None] + np.arange(3)).ravel()
+        j, k = int(rng.integers(0, ny + 1)), int(rng.integers(0, nz + 1))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        F = np.zeros(N)
+        node = nx * (ny + 1) * (nz + 1) + j * (nz + 1) + k
+        F[3 * node:3 * node + 3] = d
+        probs.append(dict(shape=(nx, ny, nz), vf=vf, rmin=rmin, F=F, fixed=fixed))
+    return probs
+
+
+def batch_config(nat, pr, max_iterations=50):
+    return nat.default_config(nat.VARIANT_CPP, volume_fraction=pr["vf"], filter_radius=pr["rmin"], move_limit=0.2,
+                              rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
+                              cg_tol=1e-6, cg_max_iterations=200000)
+
+
+def run_batch(args, nat, world, rank):
+    """Batched workload: one step = one SIMP iteration of every problem."""
+    import torch
+
+    probs = build_batch256()
+    shapes = [pr["shape"] for pr in probs]
+    nel = sum(a * b * c for a, b, c in shapes)
+    nodes = sum((a + 1) * (b + 1) * (c + 1) for a, b, c in shapes)
+    b = nat.Batch(shapes)
+    b.set_loads([pr["F"] for pr in probs], [pr["fixed"] for pr in probs])
+    cfgs = [batch_config(nat, pr) for pr in probs]
+    b.simp_begin(cfgs)
+    plan = b.autotune(reps=5)
+    for _ in range(args.warmup):
+        b.simp_step()
+    its0 = b.pcg_iterations.copy()
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stepped = 0
+    torch.cuda.synchronize()
+    l0 = nat.launch_count()
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            c, _, _, _ = b.simp_step()
+            stepped += int(np.isfinite(c).sum())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    l1 = nat.launch_count()
+    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    its_per_step = (b.pcg_iterations - its0) / max(args.steps, 1)
+    value = world * stepped / elapsed
+    # roofline: plain batched FP32 K*u of the chosen plan (u, y: 12 B per node
+    # each, scale 4 B per element)
+    alg = 24 * nodes + 4 * nel
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (plan["ms"] * 1e-3) / 1e9
+    b.close()
+    e2e = None
+    if not args.no_e2e:
+        total = args.warmup + args.steps
+        q = nat.Batch(shapes)
+        te0 = time.perf_counter()
+        q.set_loads([pr["F"] for pr in probs], [pr["fixed"] for pr in probs])
+        out = q.simp_run([batch_config(nat, pr, total) for pr in probs])
+        te1 = time.perf_counter()
+        q.close()
+        h2d = sum(pr["F"].nbytes + pr["fixed"].nbytes for pr in probs)
+        d2h = sum(o["density"].nbytes for o in out)
+        e2e = {"value": world * len(probs) * total / (te1 - te0), "unit": "problem-iterations/s",
+               "h2d_bytes_per_step": int(h2d / total), "d2h_bytes_per_step": int(d2h / total),
+               "iterations": total, "wall_s": te1 - te0,
+               "note": "am_batch_set_loads + am_batch_simp_run from host buffers (plan of the default autotuner "
+                       "state, cold start included)"}
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        import oracle as O
+
+        # the CPU restatement on a bounded sample: 4 problems, CSR assembly + 10
+        # Jacobi-PCG iterations each, extrapolated per problem with the GPU's PCG
+        # iteration count, scaled by element count to all problems
+        t_tot, nel_s = 0.0, 0
+        t_iter_per_el, t_fixed_per_el = 0.0, 0.0
+        for pr in probs[:4]:
+            prm = O.make_params(volume_fraction=pr["vf"], filter_radius=pr["rmin"], move_limit=0.2, rho_min=0.01,
+                                E_min=1e-9)
+            nx, ny, nz = pr["shape"]
+            times, threads = O.baseline_sample(pr["shape"], prm, np.full(nx * ny * nz, pr["vf"]), pr["F"],
+                                               pr["fixed"], 10)
+            ne = nx * ny * nz
+            t_iter_per_el += times["pcg_iteration"]
+            t_fixed_per_el += (times["assembly"] + times["pcg_setup"] + times["sensitivities"] + times["filter"] +
+                               times["oc"])
+            nel_s += ne
+        t_iter_per_el /= nel_s
+        t_fixed_per_el /= nel_s
+        for p, (nx, ny, nz) in enumerate(shapes):
+            ne = nx * ny * nz
+            t_tot += ne * (t_fixed_per_el + its_per_step[p] * t_iter_per_el)
+        cpu = {"value": len(probs) / t_tot, "unit": "problem-iterations/s", "cores": threads, "kind": "port",
+               "sample": ("CPU restatement (CSR + Jacobi PCG, OpenMP) timed on 4 of the 256 problems: assembly, "
+                          "10 PCG iterations, sensitivities, filter, OC; per-element rates extrapolated to every "
+                          "problem with its GPU PCG iteration count per step")}
+    if rank == 0:
+        line = {
+            "metric": "batched SIMP problem-iterations/s @ rel-res 1e-6 (Jacobi PCG)",
+            "value": value, "unit": "problem-iterations/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "batch256", "problems": len(probs), "elements": nel, "nodes": nodes,
+                       "description": build_batch256.__doc__.strip().replace("\n", " "), "cg_tol": 1e-6,
+                       "autotuned_plan": plan, "l2": "working set per step > 129 MB L2",
+                       "parallelism": f"replicas x{world}"},
+            "pcg_iterations_per_problem_step": float(np.mean(its_per_step)),
+            "roofline": {"bound": "hbm", "kernel": f"b_ku2_kernel<{plan['warps']},KU_PLAIN> (batched FP32 K*u)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": alg, "avg_ms": plan["ms"]},
+            "gpu_launches": int(l1 - l0), "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+
+
 def simp_config(nat, W, max_iterations=100):
     return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
@@ -224,7 +354,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS) + ["batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--probe", choices=["ku", "resid", "update"],
@@ -243,9 +373,14 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("gloo")
-    W = build_workload(args.workload)
+    W = build_workload(args.workload) if args.workload != "batch256" else None
 
     if args.impl == "reference":
+        if args.workload == "batch256":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no reference arm; "
+                                  "its CPU baseline is reported in the GB300 line"}))
+            return
         if rank == 0:
             run_reference(args, W)
         if world > 1:
@@ -261,6 +396,9 @@ def main():
     nat.load()
     if not nat.is_available():
         raise SystemExit("no CUDA device: the GB300 arm needs a GPU")
+    if args.workload == "batch256":
+        run_batch(args, nat, world, rank)
+        return
     shape = W["shape"]
     cfg = simp_config(nat, W)
 

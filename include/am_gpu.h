@@ -264,6 +264,21 @@ am_status am_batch_autotune(am_batch *b, int reps, int *warps, int *z_chunk, int
 /* The CUDA stream the batch's kernels run on (cudaStream_t). */
 am_status am_batch_stream(am_batch *b, void **stream);
 
+/* Starts every problem's SIMP loop with its own config cfgs[i] (variant must be
+ * AM_VARIANT_CPP); rho0 as for am_batch_simp_run.  Resets the solver state. */
+am_status am_batch_simp_begin(am_batch *b, const am_simp_config *cfgs, const double *rho0);
+
+/* One SIMP iteration of every problem whose loop has not ended (runIteration,
+ * topology_optimizer.cpp:294-384).  compliance / volume / change (nullable, [n])
+ * receive the stepped problems' results, pcg_iterations (nullable, [n]) each
+ * problem's FP32 PCG iterations since am_batch_simp_begin, *n_active the problems
+ * still running. */
+am_status am_batch_simp_step(am_batch *b, double *compliance, double *volume, double *change,
+                             long long *pcg_iterations, int *n_active);
+
+/* Current densities of all problems, concatenated, each in its config's layout. */
+am_status am_batch_get_density(am_batch *b, double *rho_out);
+
 /* Runs every problem's SIMP loop with its own config cfgs[i] (variant must be
  * AM_VARIANT_CPP; the solve is FP32 Jacobi PCG inside FP64 defect correction to
  * cfgs[i].cg_tol).  rho0 concatenates the initial densities in each config's

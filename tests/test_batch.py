@@ -122,3 +122,23 @@ def test_batch_errors():
     with pytest.raises(nat.AmError) as e:
         b.simp_run([_cfg(1), py])
     assert e.value.name == "AM_ERR_INVALID_ARG"
+
+
+def test_batch_step_api_matches_run():
+    iters = 3
+    b, _ = _batch(SHAPES[:3], seed=5)
+    cfgs = [_cfg(iters), _cfg(2), _cfg(iters)]
+    run = b.simp_run(cfgs)
+    b.simp_begin(cfgs)
+    hist = []
+    for k, expect_active in zip(range(iters), (3, 2, 0)):
+        c, v, d, active = b.simp_step()
+        hist.append(c)
+        assert active == expect_active
+    assert np.isnan(hist[2][1])  # problem 1 stopped after 2 iterations
+    dens = b.densities()
+    for p, r in enumerate(run):
+        got = np.array([h[p] for h in hist[:r["iterations"]]])
+        assert np.allclose(got, r["compliance"], rtol=1e-12, atol=0)
+        assert np.array_equal(dens[p], r["density"])
+        assert b.pcg_iterations[p] == r["pcg_iterations"]
