@@ -68,7 +68,7 @@ class SolveStats(ctypes.Structure):
         ("solve_time_s", ctypes.c_double),
         ("max_displacement", ctypes.c_double),
         ("min_displacement", ctypes.c_double),
-        ("fp64_iterations", ctypes.c_int),
+        ("learned_applications", ctypes.c_int),
     ]
 
 
@@ -87,7 +87,23 @@ class IterationResult(ctypes.Structure):
         ("solve_time_s", ctypes.c_double),
         ("sensitivity_time_s", ctypes.c_double),
         ("update_time_s", ctypes.c_double),
-        ("solver_fp64_iterations", ctypes.c_int),
+        ("solver_learned_applications", ctypes.c_int),
+    ]
+
+
+class TrainConfig(ctypes.Structure):
+    """Mirror of ``am_train_config``."""
+
+    _fields_ = [
+        ("epochs", ctypes.c_int),
+        ("batch", ctypes.c_int),
+        ("lr", ctypes.c_float),
+        ("beta1", ctypes.c_float),
+        ("beta2", ctypes.c_float),
+        ("eps", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+        ("verbose", ctypes.c_int),
+        ("loss", ctypes.c_int),
     ]
 
 
@@ -124,6 +140,22 @@ SIGNATURES = {
     "am_launch_count": (ctypes.c_longlong, []),
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "am_problem_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "am_precond_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_longlong, ctypes.POINTER(_vp)]),
+    "am_precond_destroy": (ctypes.c_int, [_vp]),
+    "am_precond_num_params": (ctypes.c_longlong, [_vp]),
+    "am_precond_num_samples": (ctypes.c_longlong, [_vp]),
+    "am_precond_get_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_param_grad": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                             ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_harvest": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _ip,
+                                          ctypes.c_int]),
+    "am_precond_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
+    "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
     "am_batch_create": (ctypes.c_int, [ctypes.c_int, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                        ctypes.POINTER(_vp)]),
     "am_batch_destroy": (ctypes.c_int, [_vp]),
@@ -322,12 +354,99 @@ class Problem:
         check(load().am_problem_stream(self.handle, ctypes.byref(st)), "am_problem_stream")
         return int(st.value or 0)
 
+    def set_preconditioner(self, pre):
+        check(load().am_problem_set_preconditioner(self.handle, None if pre is None else pre.handle),
+              "am_problem_set_preconditioner")
+        self._pre = pre
+
     def layout_info(self):
         n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
         t = ctypes.c_int(0)
         check(load().am_problem_layout(self.handle, ctypes.byref(n), ctypes.byref(e), ctypes.byref(cs),
                                        ctypes.byref(t)), "am_problem_layout")
         return dict(nodes=n.value, elements=e.value, vector_stride=cs.value, ku_tiles=t.value)
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class Preconditioner:
+    """Owns an ``am_precond`` handle: the learned conv3d preconditioner."""
+
+    def __init__(self, seed=0, capacity=4096):
+        h = _vp()
+        check(load().am_precond_create(int(seed), int(capacity), ctypes.byref(h)), "am_precond_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().am_precond_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return int(load().am_precond_num_params(self.handle))
+
+    @property
+    def num_samples(self) -> int:
+        return int(load().am_precond_num_samples(self.handle))
+
+    def get_params(self) -> np.ndarray:
+        w = np.zeros(self.num_params, np.float32)
+        check(load().am_precond_get_params(self.handle, w.ctypes.data_as(_fp)), "am_precond_get_params")
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.size != self.num_params:
+            raise ValueError("parameter count mismatch")
+        check(load().am_precond_set_params(self.handle, w.ctypes.data_as(_fp)), "am_precond_set_params")
+
+    def forward(self, x):
+        """x: (n, gz, gy, gx, 4) float32 -> (n, gz, gy, gx, 3)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n, gz, gy, gx, c = x.shape
+        if c != 4:
+            raise ValueError("input has 4 channels")
+        out = np.zeros((n, gz, gy, gx, 3), np.float32)
+        check(load().am_precond_forward(self.handle, n, gz, gy, gx, x.ctypes.data_as(_fp),
+                                        out.ctypes.data_as(_fp)), "am_precond_forward")
+        return out
+
+    def param_grad(self, x, dout):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        dout = np.ascontiguousarray(dout, dtype=np.float32)
+        n, gz, gy, gx, _ = x.shape
+        g = np.zeros(self.num_params, np.float32)
+        check(load().am_precond_param_grad(self.handle, n, gz, gy, gx, x.ctypes.data_as(_fp),
+                                           dout.ctypes.data_as(_fp), g.ctypes.data_as(_fp)), "am_precond_param_grad")
+        return g
+
+    def harvest(self, problem, cfg, rho, iters, load_case=0):
+        it = np.ascontiguousarray(iters, dtype=np.int32)
+        check(load().am_precond_harvest(self.handle, problem.handle, ctypes.byref(cfg), ptr(problem._rho(rho)),
+                                        int(load_case), ptr(it, _ip), it.size), "am_precond_harvest")
+
+    LOSS_RESIDUAL, LOSS_ENERGY = 0, 1
+
+    def train(self, epochs=20, batch=8, lr=1e-3, seed=0, verbose=0, loss=0):
+        c = TrainConfig(int(epochs), int(batch), float(lr), 0.9, 0.999, 1e-8, int(seed), int(verbose), int(loss))
+        losses = np.zeros(max(int(epochs), 1), np.float32)
+        check(load().am_precond_train(self.handle, ctypes.byref(c), losses.ctypes.data_as(_fp)), "am_precond_train")
+        return losses[:int(epochs)]
+
+    def eval(self, first=0, count=None, loss=0):
+        count = self.num_samples - first if count is None else count
+        v = ctypes.c_double(0.0)
+        check(load().am_precond_eval(self.handle, int(first), int(count), int(loss), ctypes.byref(v)),
+              "am_precond_eval")
+        return v.value
 
 
 class Batch:

@@ -15,6 +15,7 @@
 #include "host_util.h"
 #include "kernels.cuh"
 #include "ku.cuh"
+#include "precond.h"
 
 using namespace amk;
 
@@ -135,6 +136,8 @@ struct am_problem {
 
     // SIMP state
     bool simp_begun = false;
+    am_precond *pre = nullptr;       // learned preconditioner (AM_PRECOND_LEARNED)
+    const double *rho_op = nullptr;  // element densities of the current operator
     am_simp_config cfg{};
     double n_design = 0.0;
     int iter = 0;
@@ -222,6 +225,7 @@ Taps taps_of(am_problem *P) { return Taps{P->tap_d.p, P->tap_w.p, P->ntaps}; }
 
 // Element scales + Jacobi diagonal for the density currently in `rho_dev`.
 am_status setup_operator(am_problem *P, const am_simp_config &c, const double *rho_dev) {
+    P->rho_op = rho_dev;
     const int variant = c.variant;
     const int8_t *g = (variant == AM_VARIANT_PY && !P->grid_host.empty()) ? P->grid.p : nullptr;
     CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st));
@@ -300,7 +304,7 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
 }
 
 struct SolveOut {
-    int iterations = 0, outer = 0, converged = 0, fp64_iterations = 0;
+    int iterations = 0, outer = 0, converged = 0, learned = 0;
     double residual = 0.0, time_s = 0.0;
 };
 
@@ -328,7 +332,8 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
     }
     const double tol = c.cg_tol;
     const int maxit = c.cg_max_iterations > 0 ? c.cg_max_iterations : 100000;
-    if (fp64) {
+    const bool learned0 = c.preconditioner == AM_PRECOND_LEARNED && P->pre;
+    if (fp64 && !learned0) {
         CK(cudaMemcpyAsync(P->xw64.p, C.x64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p,
                     P->r64.p, nullptr, P->partial.p, P->S, P->st));
@@ -351,7 +356,13 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         // products, so the accepted iterate has the energy-norm quality of FP64 CG
         // at the same residual) preconditioned by an FP32 Jacobi-PCG inner solve
         // z = M(r) that reduces its residual by inner_tol (or stops at its cap).
+        CKS(ensure_vectors(P, false));
         CKS(ensure_vectors(P, true));
+        // learned preconditioner: the network's z starts each inner Jacobi-PCG
+        // solve; if the outer residual stops falling (< 10 % over 5 outer
+        // iterations) the solve continues with Jacobi PCG alone
+        bool learned = learned0;
+        std::vector<double> hist;
         const int max_outer = c.max_outer > 0 ? c.max_outer : 200;
         const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
         const int inner_cap = std::max(50, maxit / 4);
@@ -363,17 +374,40 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         int total = 0, outer = 0;
         bool nan = !std::isfinite(rel);
         while (!nan && rel > tol && outer < max_outer && total < maxit) {
-            // z = M(r): FP32 PCG on K z = r from zero
-            CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
-            CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, -(inner_red * inner_red), 0.0,
-                                std::min(inner_cap, maxit - total), 0, P->partial.p, P->S, P->nblocks_vec, P->st));
-            int its = 0, stt = 0;
-            CKS(run_pcg<float>(P, &its, &stt));
-            if (stt == ST_NAN) {
-                nan = true;
-                break;
+            int its = 0;
+            if (learned) {
+                // z = M(r) from the network, refined by FP32 Jacobi PCG on the
+                // residual it leaves (r - K z) to the same inner tolerance
+                const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_op, P->st};
+                CKS(precond_apply(P->pre, view, P->r64.p, P->x32.p));
+                if (!(c.inner_tol >= 1.0)) {  // inner_tol >= 1: the network alone
+                    CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->x32.p, P->q32v.p, P->st));
+                    CK(inner_resid(P->L, P->r64.p, P->q32v.p, P->mask.p, P->r32.p, P->nblocks_vec, P->st));
+                    const double thr = inner_red * inner_red * rel * rel * bnorm2;
+                    CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, thr, 0.0, std::min(inner_cap, maxit - total),
+                                        0, P->partial.p, P->S, P->nblocks_vec, P->st));
+                    int stt = 0;
+                    CKS(run_pcg<float>(P, &its, &stt));
+                    if (stt == ST_NAN) {
+                        nan = true;
+                        break;
+                    }
+                    total += its;
+                }
+            } else {
+                // z = M(r): FP32 PCG on K z = r from zero
+                CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
+                CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, -(inner_red * inner_red), 0.0,
+                                    std::min(inner_cap, maxit - total), 0, P->partial.p, P->S, P->nblocks_vec,
+                                    P->st));
+                int stt = 0;
+                CKS(run_pcg<float>(P, &its, &stt));
+                if (stt == ST_NAN) {
+                    nan = true;
+                    break;
+                }
+                total += its;
             }
-            total += its;
             // outer step
             CK(fcg_dots(P->L, P->x32.p, P->r64.p, P->q64v.p, outer == 0 ? 1 : 0, P->partial.p, P->S,
                         P->nblocks_vec, P->st));
@@ -390,7 +424,13 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             }
             rel = std::sqrt(P->Sh->o_rr / bnorm2);
             if (c.verbose >= 2)
-                std::printf("  outer %d: inner %d (total %d) rel-res %.3e\n", outer, its, total, rel);
+                std::printf("  outer %d: %s %d (total %d) rel-res %.3e\n", outer, learned ? "learned" : "inner", its,
+                            total, rel);
+            if (learned) {
+                ++o.learned;
+                hist.push_back(rel);
+                if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) learned = false;  // Jacobi from here
+            }
             if (rel <= tol) {
                 // accept on the recomputed FP64 residual (and element energies)
                 CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p,
@@ -450,8 +490,10 @@ am_status check_cfg(am_problem *P, const am_simp_config *c) {
         return fail(AM_ERR_INVALID_ARG, "unknown precision");
     if (c->layout != AM_LAYOUT_ZFASTEST && c->layout != AM_LAYOUT_XFASTEST)
         return fail(AM_ERR_INVALID_ARG, "unknown layout");
-    if (c->preconditioner != AM_PRECOND_JACOBI)
-        return fail(AM_ERR_INVALID_ARG, "preconditioner not available in this build");
+    if (c->preconditioner != AM_PRECOND_JACOBI && c->preconditioner != AM_PRECOND_LEARNED)
+        return fail(AM_ERR_INVALID_ARG, "unknown preconditioner");
+    if (c->preconditioner == AM_PRECOND_LEARNED && !P->pre)
+        return fail(AM_ERR_INVALID_ARG, "AM_PRECOND_LEARNED needs am_problem_set_preconditioner");
     if (!(c->volume_fraction > 0.0 && c->volume_fraction <= 1.0))
         return fail(AM_ERR_INVALID_ARG, "volume_fraction must be in (0, 1]");
     if (!(c->penalty >= 1.0) || !(c->move_limit > 0.0) || !(c->rho_min >= 0.0) || !(c->E_min >= 0.0))
@@ -745,7 +787,7 @@ am_status am_solve(am_problem *P, const am_simp_config *cfg, const double *rho, 
         stats->residual = o.residual;
         stats->converged = o.converged;
         stats->solve_time_s = o.time_s;
-        stats->fp64_iterations = o.fp64_iterations;
+        stats->learned_applications = o.learned;
         stats->max_displacement = 0.0;
         stats->min_displacement = 0.0;
         if (u_out) {
@@ -902,7 +944,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     double t1 = now_s();
     R.assembly_time_s = t1 - t0;
     double comp = 0.0;
-    int total_its = 0, total_outer = 0, total_fp64 = 0, conv = 1;
+    int total_its = 0, total_outer = 0, total_learned = 0, conv = 1;
     double worst_res = 0.0;
     double t_solve = 0.0, t_sens = 0.0;
     for (int lc = 0; lc < (int)P->cases.size(); ++lc) {
@@ -913,7 +955,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
         CKS(solve_case(P, c, lc, true, o));
         total_its += o.iterations;
         total_outer += o.outer;
-        total_fp64 += o.fp64_iterations;
+        total_learned += o.learned;
         conv = conv && o.converged;
         worst_res = std::max(worst_res, o.residual);
         double te = now_s();
@@ -935,7 +977,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     R.solver_outer_iterations = total_outer;
     R.solver_residual = worst_res;
     R.solver_converged = conv;
-    R.solver_fp64_iterations = total_fp64;
+    R.solver_learned_applications = total_learned;
     double tu = now_s();
     // filter (topology_optimizer.cpp:351 / topopt.py:363), FP64 in every mode: the
     // OC bisection is discrete, so an FP32 filter's rounding can flip one of its
@@ -1028,6 +1070,74 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
     CK(cudaStreamSynchronize(P->st));
     if (avg_ms) *avg_ms = tot / reps;
     if (min_ms) *min_ms = mn;
+    return AM_OK;
+}
+
+am_status am_problem_set_preconditioner(am_problem *P, am_precond *m) {
+    CKS(check_problem(P));
+    P->pre = m;
+    return AM_OK;
+}
+
+am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config *cfg, const double *rho,
+                             int load_case, const int *iters, int n_iters) {
+    CKS(check_problem(P));
+    if (!m) return fail(AM_ERR_INVALID_ARG, "null preconditioner");
+    if (!cfg || !rho || !iters || n_iters < 1) return fail(AM_ERR_INVALID_ARG, "need cfg, rho and iteration counts");
+    am_simp_config c = *cfg;
+    c.preconditioner = AM_PRECOND_JACOBI;
+    CKS(check_cfg(P, &c));
+    if (load_case < 0 || load_case >= (int)P->cases.size()) return fail(AM_ERR_INVALID_ARG, "load case out of range");
+    for (int i = 0; i < n_iters; ++i)
+        if (iters[i] < 0 || (i > 0 && iters[i] < iters[i - 1]))
+            return fail(AM_ERR_INVALID_ARG, "iteration counts must be >= 0 and ascending");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, false));
+    CKS(upload_elem(P, rho, P->rho_f.p, c.layout));
+    CKS(setup_operator(P, c, P->rho_f.p));
+    CKS(setup_mask(P, load_case));
+    LoadCaseDev &C = P->cases[load_case];
+    // r = mask(F) (the residual of u = 0), then FP32 Jacobi PCG from u = 0
+    CK(cudaMemsetAsync(P->xw64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
+    CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p, nullptr,
+                P->partial.p, P->S, P->st));
+    CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
+    const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_f.p, P->st};
+    int did = -1;
+    CKS(precond_add_density(m, view, P->M32, P->s32.p, &did));
+    CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, 0.0, 0.0, std::max(iters[0], 0), 0, P->partial.p, P->S,
+                        P->nblocks_vec, P->st));
+    CKS(sync_scalars(P));
+    // snapshots of (r_k, u_k); the errors need u*, solved after the sequence
+    const size_t nv = 3 * (size_t)P->L.cs;
+    DevBuf<float> snap;
+    CK(snap.alloc(2 * nv * (size_t)n_iters));
+    for (int i = 0; i < n_iters; ++i) {
+        if (iters[i] > P->Sh->it && P->Sh->status != ST_BREAKDOWN && P->Sh->status != ST_NAN) {
+            // continue the same sequence up to iters[i]
+            const int maxit = iters[i], zero = 0, running = ST_RUNNING;
+            CK(cudaMemcpyAsync(&P->S->maxit, &maxit, sizeof(int), cudaMemcpyHostToDevice, P->st));
+            CK(cudaMemcpyAsync(&P->S->done, &zero, sizeof(int), cudaMemcpyHostToDevice, P->st));
+            CK(cudaMemcpyAsync(&P->S->status, &running, sizeof(int), cudaMemcpyHostToDevice, P->st));
+            int its = 0, stt = 0;
+            CKS(run_pcg<float>(P, &its, &stt));
+            if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the harvesting PCG");
+        }
+        CK(cudaMemcpyAsync(snap.p + 2 * nv * i, P->r32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice, P->st));
+        CK(cudaMemcpyAsync(snap.p + 2 * nv * i + nv, P->x32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice,
+                           P->st));
+    }
+    // u*: FP64-accepted solve to 1e-10 from zero
+    am_simp_config cs = c;
+    cs.precision = AM_PREC_MIXED;
+    cs.cg_tol = 1e-10;
+    cs.warm_start = 0;
+    cs.verbose = 0;
+    SolveOut o;
+    CKS(solve_case(P, cs, load_case, false, o));
+    for (int i = 0; i < n_iters; ++i)
+        CKS(precond_add_sample(m, did, snap.p + 2 * nv * i, snap.p + 2 * nv * i + nv, C.x64.p, P->st));
+    CK(cudaStreamSynchronize(P->st));
     return AM_OK;
 }
 

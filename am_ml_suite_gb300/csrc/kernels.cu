@@ -468,6 +468,25 @@ cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float 
     return counted(cudaGetLastError());
 }
 
+// r32 = mask(r64 - q32): the residual left by an initial guess with K x = q
+__global__ void inner_resid_kernel(Layout L, const double *__restrict__ r64, const float *__restrict__ q32,
+                                   const uint8_t *__restrict__ mask, float *__restrict__ r32) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < L.cs;
+         n += (long long)gridDim.x * blockDim.x) {
+        const unsigned m = mask[n];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long i = n + c * L.cs;
+            r32[i] = ((m >> c) & 1u) ? 0.f : (float)(r64[i] - (double)q32[i]);
+        }
+    }
+}
+cudaError_t inner_resid(const Layout &L, const double *r64, const float *q32, const uint8_t *mask, float *r32,
+                        int nblocks, cudaStream_t st) {
+    inner_resid_kernel<<<nblocks, 256, 0, st>>>(L, r64, q32, mask, r32);
+    return counted(cudaGetLastError());
+}
+
 // x = 0 on the constrained / orphan components (bit c of mask[n] set)
 __device__ __forceinline__ void zero_masked_body(Layout L, const uint8_t *__restrict__ mask, double *__restrict__ x, const Blk B) {
     const long long cs = L.cs;

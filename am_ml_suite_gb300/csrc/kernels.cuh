@@ -55,6 +55,9 @@ cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, do
 // recomputed FP64 residual)
 cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
                           const Scalars *S, int nblocks, cudaStream_t st);
+// r32 = mask(r64 - q32) (inner residual of an initial guess x with K x = q32)
+cudaError_t inner_resid(const Layout &L, const double *r64, const float *q32, const uint8_t *mask, float *r32,
+                        int nblocks, cudaStream_t st);
 // x = 0 on every component whose bit is set in the per-node mask (a warm start
 // keeps no value on constrained or orphan DOFs: the reference solution is 0 there)
 cudaError_t zero_masked(const Layout &L, const uint8_t *mask, double *x, int nblocks, cudaStream_t st);

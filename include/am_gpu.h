@@ -106,7 +106,7 @@ typedef struct am_solve_stats {
     double solve_time_s;
     double max_displacement;
     double min_displacement;
-    int fp64_iterations;      /* reserved: 0 (FP64 iterations are counted in outer_iterations) */
+    int learned_applications; /* outer iterations preconditioned by the learned network */
 } am_solve_stats;
 
 /* IterationResult (topology_optimizer.hpp:65-74) plus the extra fields of this engine. */
@@ -124,7 +124,7 @@ typedef struct am_iteration_result {
     double solve_time_s;
     double sensitivity_time_s;
     double update_time_s;      /* filter + OC */
-    int solver_fp64_iterations; /* reserved: 0 */
+    int solver_learned_applications; /* outer iterations preconditioned by the learned network */
 } am_iteration_result;
 
 typedef struct am_problem am_problem;
@@ -235,6 +235,62 @@ am_status am_problem_stream(am_problem *p, void **stream);
  * component stride of a device vector, and the K*u tile count. */
 am_status am_problem_layout(am_problem *p, long long *nodes, long long *elements, long long *vector_stride,
                             int *ku_tiles);
+
+/* ---- learned preconditioner -------------------------------------------------------
+ * No counterpart in the reference (its am.ai package is an unrelated placeholder,
+ * src/am/ai/model.py:18-67).  A 3-D convolutional encoder-decoder on the node grid
+ * (4 levels, 16/32/64/128 channels, 3x3x3 kernels, skip connections, 1,461,456
+ * BF16 weights, FP32 accumulate) maps a residual r (and the node densities) to
+ * z ~ K^-1 r.  It works on the Jacobi-scaled system D^-1/2 K D^-1/2 and adds its
+ * output to the Jacobi step, so the untrained network is Jacobi.  Training
+ * minimises |K z - r|^2 / |r|^2 in that scaling, on residuals harvested from the
+ * engine's own Jacobi PCG solves, with Adam on FP32 master weights; forward and
+ * backward run on the GPU's tensor cores (conv3d.cu). */
+typedef struct am_precond am_precond;
+
+typedef struct am_train_config {
+    int epochs;
+    int batch;        /* samples per Adam step */
+    float lr;         /* 1e-3 */
+    float beta1, beta2, eps;
+    uint64_t seed;    /* sample order */
+    int verbose;
+    int loss;         /* 0: |K z - r|^2 / |r|^2 (residual norm); 1: 1 - (z.r)^2 / ((z.Kz)(e.r)),
+                         e = K^-1 r the harvested error: the share of the error energy
+                         that the best multiple of z misses */
+} am_train_config;
+
+/* seed: weight initialisation; capacity: training samples the set can hold. */
+am_status am_precond_create(uint64_t seed, long long capacity, am_precond **out);
+am_status am_precond_destroy(am_precond *m);
+long long am_precond_num_params(am_precond *m);
+long long am_precond_num_samples(am_precond *m);
+/* FP32 master weights, layer by layer, each [27 taps][cout][cin]. */
+am_status am_precond_get_params(am_precond *m, float *w);
+am_status am_precond_set_params(am_precond *m, const float *w);
+/* Network on host tensors [n][gz][gy][gx][4] -> [n][gz][gy][gx][3] (grid dims
+ * multiples of 8), and the weight gradient of sum(out * dout); for inspection and
+ * gradient checks. */
+am_status am_precond_forward(am_precond *m, int n, int gz, int gy, int gx, const float *in, float *out);
+am_status am_precond_param_grad(am_precond *m, int n, int gz, int gy, int gx, const float *in, const float *dout,
+                                float *grad);
+/* Adds training samples: at density rho (host, cfg->layout) the problem's FP32
+ * Jacobi PCG runs from u = 0 on load case `load_case`; the residual r_k and the
+ * error e_k = u* - u_k after each iteration count k in iters[0..n_iters)
+ * (ascending; 0 = the load itself) form a sample, u* from an FP64-accepted solve
+ * to 1e-10.  All samples of one preconditioner come from one grid size. */
+am_status am_precond_harvest(am_precond *m, am_problem *p, const am_simp_config *cfg, const double *rho,
+                             int load_case, const int *iters, int n_iters);
+/* Adam over the samples for cfg->epochs; epoch_loss[e] (nullable) the mean loss. */
+am_status am_precond_train(am_precond *m, const am_train_config *cfg, float *epoch_loss);
+/* Mean loss (loss: as in am_train_config) over samples [first, first + count). */
+am_status am_precond_eval(am_precond *m, long long first, long long count, int loss, double *mean_loss);
+/* Solves of `p` with preconditioner AM_PRECOND_LEARNED use `m` (NULL detaches):
+ * FP64 flexible CG whose preconditioner is the network's z = M(r) refined by FP32
+ * Jacobi PCG on r - K z to inner_tol; if the residual stops falling (less than
+ * 10 % over 5 outer iterations) the solve continues with Jacobi PCG alone.  The
+ * FP64 residual accepts every solve, as with Jacobi. */
+am_status am_problem_set_preconditioner(am_problem *p, am_precond *m);
 
 /* ---- batched SIMP ---------------------------------------------------------------
  * Many independent C++-variant problems of uneven sizes run together: one launch

@@ -1,0 +1,168 @@
+"""The learned preconditioner: the conv3d network's forward pass and weight
+gradients against a float64 PyTorch CPU reference of the same architecture, and
+training / use inside the flexible CG."""
+import numpy as np
+import pytest
+
+from am_ml_suite_gb300 import _native as nat
+
+pytestmark = pytest.mark.gpu
+
+# (cin, cout) of the 15 convolutions, in the library's parameter order
+SPEC = [(16, 16), (16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (64, 128), (128, 128),
+        (192, 64), (64, 64), (96, 32), (32, 32), (48, 16), (16, 16), (16, 16)]
+
+
+def _split(w):
+    out, o = [], 0
+    for cin, cout in SPEC:
+        n = 27 * cout * cin
+        out.append(w[o:o + n].reshape(27, cout, cin))
+        o += n
+    assert o == w.size
+    return out
+
+
+def _unet_reference(x, ws):
+    """float64 CPU reference: x (n, gz, gy, gx, 4); ws per layer [27][cout][cin]."""
+    torch = pytest.importorskip("torch")
+    F = torch.nn.functional
+    W = [torch.tensor(w, dtype=torch.float64, requires_grad=True) for w in ws]
+
+    def conv(l, t, relu=True):
+        cout, cin = W[l].shape[1], t.shape[1]
+        k = W[l][:, :, :cin].reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)
+        y = F.conv3d(t, k, padding=1)
+        return F.relu(y) if relu else y
+
+    def up(t):
+        return F.interpolate(t, scale_factor=2, mode="nearest")
+
+    t = torch.tensor(x, dtype=torch.float64).permute(0, 4, 1, 2, 3)
+    e1 = conv(1, conv(0, t))
+    e2 = conv(3, conv(2, F.avg_pool3d(e1, 2)))
+    e3 = conv(5, conv(4, F.avg_pool3d(e2, 2)))
+    e4 = conv(7, conv(6, F.avg_pool3d(e3, 2)))
+    d3 = conv(9, conv(8, torch.cat([up(e4), e3], 1)))
+    d2 = conv(11, conv(10, torch.cat([up(d3), e2], 1)))
+    d1 = conv(13, conv(12, torch.cat([up(d2), e1], 1)))
+    out = conv(14, d1, relu=False)[:, :3].permute(0, 2, 3, 4, 1)
+    return out, W
+
+
+def _random_params(pre, seed):
+    rng = np.random.default_rng(seed)
+    ws = []
+    for l, (cin, cout) in enumerate(SPEC):
+        used = 4 if l == 0 else cin
+        w = np.zeros((27, cout, cin), np.float32)
+        w[:, :, :used] = rng.uniform(-1, 1, size=(27, cout, used)) * np.sqrt(6.0 / (27 * used))
+        ws.append(w)
+    flat = np.concatenate([w.ravel() for w in ws])
+    pre.set_params(flat)
+    return [w.astype(np.float64) for w in _split(pre.get_params())]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_network_forward_and_weight_gradients_match_reference():
+    torch = pytest.importorskip("torch")
+    pre = nat.Preconditioner(seed=1, capacity=0)
+    assert pre.num_params == 1472256  # 1,461,456 trainable + channel padding
+    ws = _random_params(pre, 2)
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(2, 16, 8, 8, 4)).astype(np.float32)
+    dout = rng.normal(size=(2, 16, 8, 8, 3)).astype(np.float32)
+    ref, W = _unet_reference(x.astype(np.float64), ws)
+    got = pre.forward(x)
+    # BF16 weights and activations through 15 layers: ~1 % relative
+    assert _rel(got, ref.detach().numpy()) <= 3e-2
+    (ref * torch.tensor(dout, dtype=torch.float64)).sum().backward()
+    g = _split(pre.param_grad(x, dout))
+    errs, coss = [], []
+    for l, (cin, _) in enumerate(SPEC):
+        used = 4 if l == 0 else cin
+        gr = W[l].grad.numpy()[:, :, :used]
+        gg = g[l][:, :, :used].astype(np.float64)
+        errs.append(_rel(gg, gr))
+        coss.append(float((gr * gg).sum() / (np.linalg.norm(gr) * np.linalg.norm(gg))))
+    print("relative gradient error per layer", np.round(errs, 4), "cosine", np.round(coss, 5))
+    # The gradients are stored in BF16 after every backward stage and pass through
+    # ReLU masks taken from BF16 activations, so their error grows with depth from
+    # the output: <= 2 % at the output layer, <= 20 % at the bottleneck, with the
+    # direction (cosine) within 2 % everywhere.
+    assert errs[14] <= 2e-2 and errs[13] <= 6e-2, errs
+    assert max(errs) <= 0.2, errs
+    assert min(coss) >= 0.98, coss
+    assert np.all(g[0][:, :, 4:] == 0.0)  # padding input channels get no gradient
+
+
+def test_untrained_network_is_the_jacobi_step():
+    """The last layer starts at zero: the network's correction is zero."""
+    pre = nat.Preconditioner(seed=4, capacity=0)
+    x = np.random.default_rng(5).normal(size=(1, 8, 8, 8, 4)).astype(np.float32)
+    assert np.all(pre.forward(x) == 0.0)
+
+
+def _cantilever(shape):
+    nx, ny, nz = shape
+    N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(N)
+    line = [nx * (ny + 1) * (nz + 1) + j * (nz + 1) + nz // 2 for j in range(ny + 1)]
+    F[3 * np.array(line) + 2] = -1.0 / len(line)
+    return F, fixed
+
+
+def test_harvest_train_and_learned_solves_keep_the_answer():
+    """Residual/error pairs harvested from the engine's own Jacobi PCG at SIMP
+    densities; Adam on the GPU lowers the training loss well below the Jacobi
+    step's; a flexible-CG solve with the trained network is accepted on the same
+    FP64 residual and returns the Jacobi solve's displacement."""
+    shape = (31, 15, 15)
+    F, fixed = _cantilever(shape)
+    p = nat.Problem(shape)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, volume_fraction=0.3, filter_radius=1.5, rho_min=0.01, E_min=1e-9,
+                             convergence_tol=0.0, max_iterations=10, cg_tol=1e-6)
+    pre = nat.Preconditioner(seed=0, capacity=256)
+    p.simp_begin(cfg, np.full(shape, 0.3))
+    for _ in range(6):
+        p.simp_step()
+        pre.harvest(p, cfg, p.simp_density(), [0, 2, 8, 32, 128])
+    assert pre.num_samples == 30
+    before = pre.eval(loss=pre.LOSS_RESIDUAL)
+    energy_before = pre.eval(loss=pre.LOSS_ENERGY)
+    assert 0.0 < energy_before <= 1.0
+    losses = pre.train(epochs=12, batch=6, lr=1e-3, loss=pre.LOSS_RESIDUAL)
+    after = pre.eval(loss=pre.LOSS_RESIDUAL)
+    assert losses[-1] < losses[0]
+    assert after < 0.5 * before, (before, after)
+    rho = p.simp_density()
+    tol = 1e-9
+    cj = nat.default_config(nat.VARIANT_CPP, rho_min=0.01, E_min=1e-9, cg_tol=tol, warm_start=0)
+    uj, sj = p.solve(cj, rho)
+    p.set_preconditioner(pre)
+    cl = nat.default_config(nat.VARIANT_CPP, rho_min=0.01, E_min=1e-9, cg_tol=tol, warm_start=0,
+                            preconditioner=nat.PRECOND_LEARNED)
+    ul, sl = p.solve(cl, rho)
+    assert sl.converged and sl.residual <= tol and sl.learned_applications >= 1
+    assert np.linalg.norm(ul - uj) / np.linalg.norm(uj) <= 1e-6
+    # the network alone (no Jacobi refinement) is still judged by the FP64 residual
+    cl.inner_tol = 2.0
+    un, sn = p.solve(cl, rho)
+    assert sn.converged and sn.residual <= tol
+    assert np.linalg.norm(un - uj) / np.linalg.norm(uj) <= 1e-6
+
+
+def test_learned_needs_an_attached_network():
+    p = nat.Problem((8, 4, 4))
+    F, fixed = _cantilever((8, 4, 4))
+    p.set_loads([F], [fixed])
+    c = nat.default_config(nat.VARIANT_CPP, preconditioner=nat.PRECOND_LEARNED)
+    with pytest.raises(nat.AmError) as e:
+        p.solve(c, np.full((8, 4, 4), 0.5))
+    assert e.value.name == "AM_ERR_INVALID_ARG"
