@@ -121,6 +121,7 @@ struct am_problem {
     // vectors
     DevBuf<double> r64, xw64, p64a, p64b, q64v, vstage;
     DevBuf<float> x32, r32, p32a, p32b, q32v;
+    DevBuf<double> xi64;  // FP64 iterate of the FP32 inner PCG (the flexible CG's z)
     DevBuf<double> partial;
     Scalars *S = nullptr;    // device
     Scalars *Sh = nullptr;   // pinned host mirror
@@ -166,6 +167,7 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
         CK(P->q64v.alloc(nv));
     } else {
         CK(P->x32.alloc(nv));
+        CK(P->xi64.alloc(nv));
         CK(P->r32.alloc(nv));
         CK(P->p32a.alloc(nv));
         CK(P->p32b.alloc(nv));
@@ -251,11 +253,12 @@ template <typename T>
 am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
     cudaGraph_t g = nullptr;
     const KuLaunch &K = std::is_same<T, float>::value ? P->plan32 : P->plan64;
-    T *x, *r, *pa, *pb, *q;
+    double *x;
+    T *r, *pa, *pb, *q;
     const T *dinv, *s;
     Modal<T> M;
     if constexpr (std::is_same<T, float>::value) {
-        x = P->x32.p; r = P->r32.p; pa = P->p32a.p; pb = P->p32b.p; q = P->q32v.p;
+        x = P->xi64.p; r = P->r32.p; pa = P->p32a.p; pb = P->p32b.p; q = P->q32v.p;
         dinv = P->dinv32.p; s = P->s32.p; M = P->M32;
     } else {
         x = P->xw64.p; r = P->r64.p; pa = P->p64a.p; pb = P->p64b.p; q = P->q64v.p;
@@ -379,11 +382,13 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 // z = M(r) from the network, refined by FP32 Jacobi PCG on the
                 // residual it leaves (r - K z) to the same inner tolerance
                 const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_op, P->st};
-                CKS(precond_apply(P->pre, view, P->r64.p, P->x32.p));
+                CKS(precond_apply(P->pre, view, P->r64.p, P->xi64.p));
                 if (!(c.inner_tol >= 1.0)) {  // inner_tol >= 1: the network alone
+                    CK(to_float(P->xi64.p, P->x32.p, 3 * P->L.cs, P->nblocks_vec, P->st));
                     CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->x32.p, P->q32v.p, P->st));
                     CK(inner_resid(P->L, P->r64.p, P->q32v.p, P->mask.p, P->r32.p, P->nblocks_vec, P->st));
-                    const double thr = inner_red * inner_red * rel * rel * bnorm2;
+                    const double tgt = std::max(inner_red * rel, 0.3 * tol);
+                    const double thr = tgt * tgt * bnorm2;
                     CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, thr, 0.0, std::min(inner_cap, maxit - total),
                                         0, P->partial.p, P->S, P->nblocks_vec, P->st));
                     int stt = 0;
@@ -395,9 +400,11 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                     total += its;
                 }
             } else {
-                // z = M(r): FP32 PCG on K z = r from zero
-                CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
-                CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, -(inner_red * inner_red), 0.0,
+                // z = M(r): FP32 PCG (FP64 iterate) on K z = r from zero, to
+                // inner_tol of |r| but not below 0.3 tol |f| (the overall goal)
+                CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->xi64.p, P->S, P->nblocks_vec, P->st));
+                const double tgt = std::max(inner_red * rel, 0.3 * tol);
+                CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, tgt * tgt * bnorm2, 0.0,
                                     std::min(inner_cap, maxit - total), 0, P->partial.p, P->S, P->nblocks_vec,
                                     P->st));
                 int stt = 0;
@@ -409,9 +416,9 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 total += its;
             }
             // outer step
-            CK(fcg_dots(P->L, P->x32.p, P->r64.p, P->q64v.p, outer == 0 ? 1 : 0, P->partial.p, P->S,
+            CK(fcg_dots(P->L, P->xi64.p, P->r64.p, P->q64v.p, outer == 0 ? 1 : 0, P->partial.p, P->S,
                         P->nblocks_vec, P->st));
-            CK(fcg_direction(P->L, P->x32.p, P->p64a.p, P->S, P->nblocks_vec, P->st));
+            CK(fcg_direction(P->L, P->xi64.p, P->p64a.p, P->S, P->nblocks_vec, P->st));
             CK(ku_dot(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p, P->S,
                       P->st));
             CK(fcg_update(P->L, C.x64.p, P->r64.p, P->p64a.p, P->q64v.p, P->partial.p, P->S, P->nblocks_vec,
@@ -664,6 +671,7 @@ am_status am_problem_destroy(am_problem *P) {
     for (auto *b : d64) b->release();
     P->oc_a32.release(); P->oc_lo32.release(); P->oc_hi32.release();
     DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->r32, &P->p32a, &P->p32b, &P->q32v};
+    P->xi64.release();
     for (auto *b : d32) b->release();
     P->design.release(); P->mask.release(); P->nofix.release(); P->grid.release(); P->tap_d.release();
     if (P->S) cudaFree(P->S);
@@ -1047,7 +1055,7 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                             P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
                 break;
             case 2:
-                CK(pcg_update<float>(P->L, P->x32.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p, P->dinv32.p,
+                CK(pcg_update<float>(P->L, P->xi64.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p, P->dinv32.p,
                                      P->partial.p, P->S, P->nblocks_vec, P->st));
                 break;
             case 3:
@@ -1101,7 +1109,7 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
     CK(cudaMemsetAsync(P->xw64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
     CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p, nullptr,
                 P->partial.p, P->S, P->st));
-    CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->x32.p, P->S, P->nblocks_vec, P->st));
+    CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->xi64.p, P->S, P->nblocks_vec, P->st));
     const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_f.p, P->st};
     int did = -1;
     CKS(precond_add_density(m, view, P->M32, P->s32.p, &did));
@@ -1111,7 +1119,9 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
     // snapshots of (r_k, u_k); the errors need u*, solved after the sequence
     const size_t nv = 3 * (size_t)P->L.cs;
     DevBuf<float> snap;
-    CK(snap.alloc(2 * nv * (size_t)n_iters));
+    DevBuf<double> snapx;
+    CK(snap.alloc(nv * (size_t)n_iters));
+    CK(snapx.alloc(nv * (size_t)n_iters));
     for (int i = 0; i < n_iters; ++i) {
         if (iters[i] > P->Sh->it && P->Sh->status != ST_BREAKDOWN && P->Sh->status != ST_NAN) {
             // continue the same sequence up to iters[i]
@@ -1123,9 +1133,8 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
             CKS(run_pcg<float>(P, &its, &stt));
             if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the harvesting PCG");
         }
-        CK(cudaMemcpyAsync(snap.p + 2 * nv * i, P->r32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice, P->st));
-        CK(cudaMemcpyAsync(snap.p + 2 * nv * i + nv, P->x32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice,
-                           P->st));
+        CK(cudaMemcpyAsync(snap.p + nv * i, P->r32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice, P->st));
+        CK(cudaMemcpyAsync(snapx.p + nv * i, P->xi64.p, nv * sizeof(double), cudaMemcpyDeviceToDevice, P->st));
     }
     // u*: FP64-accepted solve to 1e-10 from zero
     am_simp_config cs = c;
@@ -1136,7 +1145,7 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
     SolveOut o;
     CKS(solve_case(P, cs, load_case, false, o));
     for (int i = 0; i < n_iters; ++i)
-        CKS(precond_add_sample(m, did, snap.p + 2 * nv * i, snap.p + 2 * nv * i + nv, C.x64.p, P->st));
+        CKS(precond_add_sample(m, did, snap.p + nv * i, snapx.p + nv * i, C.x64.p, P->st));
     CK(cudaStreamSynchronize(P->st));
     return AM_OK;
 }

@@ -2,7 +2,8 @@
 // sizes advanced together by batched persistent kernels (batch.cuh).
 //
 // One SIMP step of the batch is: scales + Jacobi diagonal, warm-start clean-up,
-// FP64 defect correction (FP64 residual, FP32 Jacobi PCG on it, x += x32) until
+// FP64 defect correction (FP64 residual, FP32 Jacobi PCG on it updating the FP64
+// iterate) until
 // every problem's |F - K u| <= tol |F|, the FP64 residual with element energies,
 // then sensitivities, u.F, filter and the FP64 OC bisection.  Each of these is one
 // launch for the whole batch; the FP32 PCG iterations run as CUDA-graph chunks of
@@ -88,7 +89,7 @@ struct am_batch {
     Pool<float> s32;
     Pool<uint8_t> design;
     Pool<double> F, x64, r64, dinv64;
-    Pool<float> x32, r32, pa, pb, q32, dinv32;
+    Pool<float> r32, pa, pb, q32, dinv32;
     Pool<uint8_t> mask, fixed_bits;
     Pool<long long> f_idx;
     Pool<double> f_val;
@@ -219,7 +220,6 @@ am_status batch_solve(am_batch *B, int max_chunks) {
                 return bfail(AM_ERR_NAN_DETECTED, "NaN in the PCG of batch problem " + std::to_string(p));
             B->pcg_its[p] += B->Sh[p].it;
         }
-        BCK(batch_accumulate(B->items_d.p, B->vec, kSms * 8, B->st));
     }
     return AM_OK;  // not converged within the rounds: reported through the residuals
 }
@@ -242,7 +242,7 @@ am_status am_batch_destroy(am_batch *B) {
     for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi,
                     &B->F, &B->x64, &B->r64, &B->dinv64, &B->f_val, &B->tap_w, &B->partial})
         q->release();
-    for (auto *q : {&B->s32, &B->x32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32}) q->release();
+    for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32}) q->release();
     for (auto *q : {&B->design, &B->mask, &B->fixed_bits}) q->release();
     for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k64, &B->w_prob}) q->release();
     B->f_idx.release();
@@ -320,7 +320,7 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     A(B->design, e);
     for (auto *q : {&B->F, &B->x64, &B->r64}) A(*q, 3 * nn);
     A(B->dinv64, nn);
-    for (auto *q : {&B->x32, &B->r32, &B->pa, &B->pb, &B->q32}) A(*q, 3 * nn);
+    for (auto *q : {&B->r32, &B->pa, &B->pb, &B->q32}) A(*q, 3 * nn);
     A(B->dinv32, nn);
     A(B->mask, nn);
     A(B->fixed_bits, nn);
@@ -352,7 +352,6 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         it.x64 = B->x64.p + 3 * no;
         it.r64 = B->r64.p + 3 * no;
         it.dinv64 = B->dinv64.p + no;
-        it.x32 = B->x32.p + 3 * no;
         it.r32 = B->r32.p + 3 * no;
         it.pa = B->pa.p + 3 * no;
         it.pb = B->pb.p + 3 * no;

@@ -25,7 +25,7 @@ struct BatchItem {
     uint8_t *design;
     // node arrays: [3][cs] vectors, per-node inverse diagonal / mask / constraint bits
     double *F, *x64, *r64, *dinv64;
-    float *x32, *r32, *pa, *pb, *q32, *dinv32;
+    float *r32, *pa, *pb, *q32, *dinv32;
     uint8_t *mask, *fixed_bits;
     // nonzeros of F (node-plane index) for u.F and |F|^2
     const long long *f_idx;
@@ -70,8 +70,8 @@ cudaError_t batch_prepare_solve(const BatchItem *it, WorkList vec, WorkList prob
 // r64 = mask(F - K x64) (FP64), |r|^2 -> S->res_rr; element energies when energy != 0
 cudaError_t batch_resid(const BatchItem *it, WorkList k64, const BatchConst &C, int energy, int grid,
                         cudaStream_t st);
-// r32 = r64, x32 = 0, then the FP32 PCG start (a problem whose FP64 residual already
-// meets tol is marked done)
+// r32 = r64, then the FP32 PCG start; the sequence updates the FP64 iterate x64
+// (a problem whose FP64 residual already meets tol is marked done)
 cudaError_t batch_inner_start(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
 // one FP32 PCG iteration for every active problem: fused K*p (warps = 4 or 8) + update
 cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, const BatchConst &C, int warps,
@@ -79,8 +79,6 @@ cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, 
 // plain FP32 K*u (y = q32, u = pa) over the batch, for the autotuner
 cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
                            cudaStream_t st);
-// x64 += x32
-cudaError_t batch_accumulate(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
 // sensitivities + u.F, filter, OC bisection (FP64), new density copied into rho
 cudaError_t batch_update(const BatchItem *it, WorkList elem, WorkList prob, int grid, cudaStream_t st);
 

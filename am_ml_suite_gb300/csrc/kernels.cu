@@ -237,7 +237,7 @@ constexpr int VEC_THREADS = 256;
 // x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer the K*u
 // kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
 template <typename T>
-__device__ __forceinline__ void pcg_update_body(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
+__device__ __forceinline__ void pcg_update_body(Layout L, double *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
                       const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
                       Scalars *S, const Blk B) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
@@ -248,46 +248,41 @@ __device__ __forceinline__ void pcg_update_body(Layout L, T *__restrict__ x, T *
     const long long cs = L.cs;
     Acc<T> a0, a1;
     if constexpr (std::is_same<T, float>::value) {
-        // four nodes per thread and step (cs is a multiple of 64, rows 16-byte
-        // aligned): all 13 vector loads are issued before the 6 stores
+        // FP32 r, p, q with an FP64 iterate x: the rounding of an FP32 x (eps |K||x|
+        // at this stiffness contrast) would cap the true residual near 1e-2, FP64 x
+        // keeps the FP32 sequence converging like FP64 PCG.  One component of four
+        // nodes per thread and step (cs is a multiple of 64, rows 16-byte aligned).
         const long long n4 = cs / 4;
-        for (long long k = B.b * (long long)blockDim.x + threadIdx.x; k < n4;
-             k += (long long)B.n * blockDim.x) {
+        const long long units = 3 * n4;
+        for (long long u = B.b * (long long)blockDim.x + threadIdx.x; u < units;
+             u += (long long)B.n * blockDim.x) {
+            const long long k = u - ((u >= n4) + (u >= 2 * n4)) * n4;  // node group of this unit
             const float4 d = __ldg(reinterpret_cast<const float4 *>(dinv) + k);
-            float4 xv[3], rv[3], pv[3], qv[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const long long i = k + c * n4;
-                xv[c] = reinterpret_cast<const float4 *>(x)[i];
-                rv[c] = reinterpret_cast<const float4 *>(r)[i];
-                pv[c] = __ldg(reinterpret_cast<const float4 *>(p) + i);
-                qv[c] = __ldg(reinterpret_cast<const float4 *>(q) + i);
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                xv[c].x = fmaf(alpha, pv[c].x, xv[c].x);
-                xv[c].y = fmaf(alpha, pv[c].y, xv[c].y);
-                xv[c].z = fmaf(alpha, pv[c].z, xv[c].z);
-                xv[c].w = fmaf(alpha, pv[c].w, xv[c].w);
-                rv[c].x = fmaf(-alpha, qv[c].x, rv[c].x);
-                rv[c].y = fmaf(-alpha, qv[c].y, rv[c].y);
-                rv[c].z = fmaf(-alpha, qv[c].z, rv[c].z);
-                rv[c].w = fmaf(-alpha, qv[c].w, rv[c].w);
-                a0.add_prod(rv[c].x, rv[c].x);
-                a0.add_prod(rv[c].y, rv[c].y);
-                a0.add_prod(rv[c].z, rv[c].z);
-                a0.add_prod(rv[c].w, rv[c].w);
-                a1.add_prod(rv[c].x, d.x * rv[c].x);
-                a1.add_prod(rv[c].y, d.y * rv[c].y);
-                a1.add_prod(rv[c].z, d.z * rv[c].z);
-                a1.add_prod(rv[c].w, d.w * rv[c].w);
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const long long i = k + c * n4;
-                reinterpret_cast<float4 *>(x)[i] = xv[c];
-                reinterpret_cast<float4 *>(r)[i] = rv[c];
-            }
+            double2 x01 = reinterpret_cast<const double2 *>(x)[2 * u];
+            double2 x23 = reinterpret_cast<const double2 *>(x)[2 * u + 1];
+            float4 rv = reinterpret_cast<const float4 *>(r)[u];
+            const float4 pv = __ldg(reinterpret_cast<const float4 *>(p) + u);
+            const float4 qv = __ldg(reinterpret_cast<const float4 *>(q) + u);
+            const double ad = (double)alpha;
+            x01.x = fma(ad, (double)pv.x, x01.x);
+            x01.y = fma(ad, (double)pv.y, x01.y);
+            x23.x = fma(ad, (double)pv.z, x23.x);
+            x23.y = fma(ad, (double)pv.w, x23.y);
+            rv.x = fmaf(-alpha, qv.x, rv.x);
+            rv.y = fmaf(-alpha, qv.y, rv.y);
+            rv.z = fmaf(-alpha, qv.z, rv.z);
+            rv.w = fmaf(-alpha, qv.w, rv.w);
+            reinterpret_cast<double2 *>(x)[2 * u] = x01;
+            reinterpret_cast<double2 *>(x)[2 * u + 1] = x23;
+            reinterpret_cast<float4 *>(r)[u] = rv;
+            a0.add_prod(rv.x, rv.x);
+            a0.add_prod(rv.y, rv.y);
+            a0.add_prod(rv.z, rv.z);
+            a0.add_prod(rv.w, rv.w);
+            a1.add_prod(rv.x, d.x * rv.x);
+            a1.add_prod(rv.y, d.y * rv.y);
+            a1.add_prod(rv.z, d.z * rv.z);
+            a1.add_prod(rv.w, d.w * rv.w);
         }
     } else {
         // one node per thread and step, its three component planes
@@ -349,19 +344,19 @@ __device__ __forceinline__ void pcg_update_body(Layout L, T *__restrict__ x, T *
 }
 template <typename T>
 __global__ void __launch_bounds__(VEC_THREADS)
-    pcg_update_kernel(Layout L, T *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
+    pcg_update_kernel(Layout L, double *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
                       const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
                       Scalars *S) {
     pcg_update_body<T>(L, x, r, pa, pb, q, dinv, partial, S, grid_blk());
 }
 
 template <typename T>
-cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
+cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st) {
     pcg_update_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, pa, pb, q, dinv, partial, S);
     return counted(cudaGetLastError());
 }
-template cudaError_t pcg_update<float>(const Layout &, float *, float *, const float *, const float *,
+template cudaError_t pcg_update<float>(const Layout &, double *, float *, const float *, const float *,
                                        const float *, const float *, double *, Scalars *, int, cudaStream_t);
 template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *, const double *,
                                         const double *, const double *, double *, Scalars *, int, cudaStream_t);
@@ -448,23 +443,34 @@ template cudaError_t pcg_start<float>(const Layout &, const float *, const float
 template cudaError_t pcg_start<double>(const Layout &, const double *, const double *, double, double, int, int,
                                        double *, Scalars *, int, cudaStream_t);
 
+// r32 = r64 and (x != nullptr) x = 0
 __device__ __forceinline__ void dc_inner_init_body(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
-                                     float *__restrict__ x32, const Scalars *S, const Blk B) {
+                                     double *__restrict__ x, const Scalars *S, const Blk B) {
     (void)S;
     const long long n = 3 * L.cs;
     for (long long i = B.b * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)B.n * blockDim.x) {
         r32[i] = (float)r64[i];
-        x32[i] = 0.f;
+        if (x) x[i] = 0.0;
     }
 }
 __global__ void dc_inner_init_kernel(Layout L, const double *__restrict__ r64, float *__restrict__ r32,
-                                     float *__restrict__ x32, const Scalars *S) {
-    dc_inner_init_body(L, r64, r32, x32, S, grid_blk());
+                                     double *__restrict__ x, const Scalars *S) {
+    dc_inner_init_body(L, r64, r32, x, S, grid_blk());
 }
-cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
+cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, double *x,
                           const Scalars *S, int nblocks, cudaStream_t st) {
-    dc_inner_init_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, r64, r32, x32, S);
+    dc_inner_init_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, r64, r32, x, S);
+    return counted(cudaGetLastError());
+}
+
+__global__ void to_float_kernel(const double *__restrict__ a, float *__restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+cudaError_t to_float(const double *a, float *b, long long n, int nblocks, cudaStream_t st) {
+    to_float_kernel<<<nblocks, 256, 0, st>>>(a, b, n);
     return counted(cudaGetLastError());
 }
 
@@ -507,7 +513,7 @@ __global__ void zero_masked_kernel(Layout L, const uint8_t *__restrict__ mask, d
 // (Notay, SIAM J. Sci. Comput. 22 (2000)): beta = z_new.(r_new - r_old) / z_old.r_old,
 // and r_new - r_old = -alpha q, so beta = -alpha z_new.q / z_old.r_old.
 __global__ void __launch_bounds__(VEC_THREADS)
-    fcg_dots_kernel(Layout L, const float *__restrict__ z, const double *__restrict__ r,
+    fcg_dots_kernel(Layout L, const double *__restrict__ z, const double *__restrict__ r,
                     const double *__restrict__ q, int first, double *partial, Scalars *S) {
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag;
@@ -515,7 +521,7 @@ __global__ void __launch_bounds__(VEC_THREADS)
     double zr = 0.0, zq = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const double zi = (double)z[i];
+        const double zi = z[i];
         zr = fma(zi, r[i], zr);
         if (!first) zq = fma(zi, q[i], zq);
     }
@@ -535,22 +541,22 @@ __global__ void __launch_bounds__(VEC_THREADS)
         S->cnt_fcg = 0;
     }
 }
-cudaError_t fcg_dots(const Layout &L, const float *z, const double *r, const double *q, int first,
+cudaError_t fcg_dots(const Layout &L, const double *z, const double *r, const double *q, int first,
                      double *partial, Scalars *S, int nblocks, cudaStream_t st) {
     fcg_dots_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, z, r, q, first, partial, S);
     return counted(cudaGetLastError());
 }
 
 // p = z + beta p
-__global__ void fcg_direction_kernel(Layout L, const float *__restrict__ z, double *__restrict__ p,
+__global__ void fcg_direction_kernel(Layout L, const double *__restrict__ z, double *__restrict__ p,
                                      const Scalars *S) {
     const double beta = S->o_beta;
     const long long n = 3 * L.cs;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
-        p[i] = beta == 0.0 ? (double)z[i] : fma(beta, p[i], (double)z[i]);
+        p[i] = beta == 0.0 ? z[i] : fma(beta, p[i], z[i]);
 }
-cudaError_t fcg_direction(const Layout &L, const float *z, double *p, const Scalars *S, int nblocks,
+cudaError_t fcg_direction(const Layout &L, const double *z, double *p, const Scalars *S, int nblocks,
                           cudaStream_t st) {
     fcg_direction_kernel<<<nblocks, VEC_THREADS, 0, st>>>(L, z, p, S);
     return counted(cudaGetLastError());
@@ -1284,7 +1290,8 @@ __global__ void __launch_bounds__(256) b_inner_init_kernel(const BatchItem *item
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
-        dc_inner_init_body(it.L, it.r64, it.r32, it.x32, it.S, Blk{_k.y, it.n_vec});
+        // the FP32 sequence continues the FP64 iterate x64 (no zeroing)
+        dc_inner_init_body(it.L, it.r64, it.r32, nullptr, it.S, Blk{_k.y, it.n_vec});
     }
 }
 // FP32 PCG on K x32 = r32 to |r| <= tol/2 |F| (but at most 1e-6 below its start);
@@ -1338,7 +1345,7 @@ __global__ void __launch_bounds__(256) b_update_kernel(const BatchItem *items, W
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
-        pcg_update_body<float>(it.L, it.x32, it.r32, it.pa, it.pb, it.q32, it.dinv32, it.partial, it.S,
+        pcg_update_body<float>(it.L, it.x64, it.r32, it.pa, it.pb, it.q32, it.dinv32, it.partial, it.S,
                                Blk{_k.y, it.n_vec});
         __syncthreads();
     }
@@ -1359,20 +1366,6 @@ cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C
     if (warps == 8) b_ku2_kernel<8, KU_PLAIN><<<g2, 256, 0, st>>>(it, k2, C.M32);
     else if (warps == 4) b_ku2_kernel<4, KU_PLAIN><<<g2, 128, 0, st>>>(it, k2, C.M32);
     else return cudaErrorInvalidValue;
-    return counted(cudaGetLastError());
-}
-
-__global__ void __launch_bounds__(256) b_accumulate_kernel(const BatchItem *items, WorkList W) {
-    AMK_BATCH_LOOP(W) {
-        const BatchItem &it = items[_k.x];
-        if (it.S->frozen) continue;
-        const long long n = 3 * it.L.cs;
-        for (long long i = (long long)_k.y * blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x)
-            it.x64[i] += (double)it.x32[i];
-    }
-}
-cudaError_t batch_accumulate(const BatchItem *it, WorkList vec, int grid, cudaStream_t st) {
-    b_accumulate_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
     return counted(cudaGetLastError());
 }
 

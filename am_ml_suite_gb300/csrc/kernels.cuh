@@ -42,31 +42,34 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
                      double *r, double *ce, double *partial, Scalars *S, cudaStream_t st);
 
 // ---- PCG vector kernels ------------------------------------------------------
-// x += alpha p; r -= alpha q (p = the pair member written this iteration);
+// x += alpha p; r -= alpha q (p = the pair member written this iteration; x is
+// FP64 for both precisions of r, p, q);
 // rr, rz -> S (beta, stop tests: converged / reliable update due / max it)
 template <typename T>
-cudaError_t pcg_update(const Layout &L, T *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
+cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st);
 // (re)start from the residual r (already masked); see pcg_start_kernel
 template <typename T>
 cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,
                       int restart, double *partial, Scalars *S, int nblocks, cudaStream_t st);
-// r32 = r64, x32 = 0 (reliable update: the FP32 sequence continues from the
+// r32 = r64 and, if x != nullptr, x = 0 (the FP32 sequence starts from the
 // recomputed FP64 residual)
-cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, float *x32,
+cudaError_t dc_inner_init(const Layout &L, const double *r64, float *r32, double *x,
                           const Scalars *S, int nblocks, cudaStream_t st);
+// b = (float)a, n entries
+cudaError_t to_float(const double *a, float *b, long long n, int nblocks, cudaStream_t st);
 // r32 = mask(r64 - q32) (inner residual of an initial guess x with K x = q32)
 cudaError_t inner_resid(const Layout &L, const double *r64, const float *q32, const uint8_t *mask, float *r32,
                         int nblocks, cudaStream_t st);
 // x = 0 on every component whose bit is set in the per-node mask (a warm start
 // keeps no value on constrained or orphan DOFs: the reference solution is 0 there)
 cudaError_t zero_masked(const Layout &L, const uint8_t *mask, double *x, int nblocks, cudaStream_t st);
-// outer flexible CG (FP64) with an inner preconditioner output z (FP32):
+// outer flexible CG (FP64) with an inner preconditioner output z (FP64):
 // z.r, z.q -> beta (first: 0) ; p = z + beta p ; q = mask(K p), p.q -> alpha ;
 // x += alpha p, r -= alpha q, r.r
-cudaError_t fcg_dots(const Layout &L, const float *z, const double *r, const double *q, int first,
+cudaError_t fcg_dots(const Layout &L, const double *z, const double *r, const double *q, int first,
                      double *partial, Scalars *S, int nblocks, cudaStream_t st);
-cudaError_t fcg_direction(const Layout &L, const float *z, double *p, const Scalars *S, int nblocks,
+cudaError_t fcg_direction(const Layout &L, const double *z, double *p, const Scalars *S, int nblocks,
                           cudaStream_t st);
 cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
                    const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st);

@@ -245,7 +245,7 @@ __global__ void scaled_norm_kernel(Layout L, const double *r, const float *dsq, 
 
 // z = dsq (r~ + N(r~)) * scale on free DOFs (inference); r~ recomputed from r
 __global__ void apply_out_kernel(Layout L, int gz, int gy, int gx, const double *r, const float *dsq,
-                                 const uint8_t *mask, const float *out, const double *nrm2, double nfree, float *z) {
+                                 const uint8_t *mask, const float *out, const double *nrm2, double nfree, double *z) {
     const double rms = sqrt(fmax(*nrm2, 1e-300) / fmax(nfree, 1.0));
     const long long nn = L.cs;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
@@ -257,10 +257,10 @@ __global__ void apply_out_kernel(Layout L, int gz, int gy, int gx, const double 
         const uint8_t m = real ? mask[n] : 7;
         const long long v = ((long long)iz * gy + iy) * gx + ix;
         for (int k = 0; k < 3; ++k) {
-            float val = 0.f;
+            double val = 0.0;
             if (!((m >> k) & 1u)) {
                 const double rt = (double)dsq[n] * r[n + k * L.cs] / rms;
-                val = (float)((double)dsq[n] * (rt + (double)out[v * 16 + k]) * rms);
+                val = (double)dsq[n] * (rt + (double)out[v * 16 + k]) * rms;
             }
             z[n + k * L.cs] = val;
         }
@@ -346,7 +346,7 @@ __global__ void scale_sample_kernel(Layout L, const float *r, const float *dsq, 
 
 // e~ = (xstar - xk) / (dsq rms) on free DOFs (the ideal network output
 // r~ + N(r~) for this residual)
-__global__ void scale_error_kernel(Layout L, const double *xstar, const float *xk, const float *dsq,
+__global__ void scale_error_kernel(Layout L, const double *xstar, const double *xk, const float *dsq,
                                    const uint8_t *mask, float *out, const double *nrm2, double nfree) {
     const double rms = sqrt(fmax(*nrm2, 1e-300) / fmax(nfree, 1.0));
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < L.cs;
@@ -355,7 +355,7 @@ __global__ void scale_error_kernel(Layout L, const double *xstar, const float *x
         for (int k = 0; k < 3; ++k) {
             const long long i = n + k * L.cs;
             out[i] = (((m >> k) & 1u) || !(dsq[n] > 0.f)) ? 0.f
-                                                          : (float)((xstar[i] - (double)xk[i]) / ((double)dsq[n] * rms));
+                                                          : (float)((xstar[i] - xk[i]) / ((double)dsq[n] * rms));
         }
     }
 }
@@ -608,7 +608,7 @@ void network_grid(const Layout &L, int &gz, int &gy, int &gx) {
 
 namespace amk {
 
-am_status precond_apply(am_precond *M, const PrecondView &v, const double *r, float *z) {
+am_status precond_apply(am_precond *M, const PrecondView &v, const double *r, double *z) {
     const Layout &L = v.L;
     int gz, gy, gx;
     network_grid(L, gz, gy, gx);
@@ -670,7 +670,7 @@ am_status precond_add_density(am_precond *M, const PrecondView &v, const Modal<f
     return AM_OK;
 }
 
-am_status precond_add_sample(am_precond *M, int density_id, const float *r32, const float *xk, const double *xstar,
+am_status precond_add_sample(am_precond *M, int density_id, const float *r32, const double *xk, const double *xstar,
                              cudaStream_t st) {
     if (density_id < 0 || density_id >= (int)M->dens.size()) return pfail(AM_ERR_INVALID_ARG, "bad density id");
     if (M->nsamples >= M->capacity) return pfail(AM_ERR_SIZE_MISMATCH, "training set full (capacity)");

@@ -20,16 +20,16 @@ struct PrecondView {
 };
 
 // z = M(r): the network's approximation of K^{-1} r (r, z device vectors [3][cs])
-am_status precond_apply(am_precond *m, const PrecondView &v, const double *r, float *z);
+am_status precond_apply(am_precond *m, const PrecondView &v, const double *r, double *z);
 
 // Training data: one density (its FP32 element scales and the operator
 // constants) then residual snapshots at that density.  The first density fixes
 // the training grid; later ones must have the same layout.
 am_status precond_add_density(am_precond *m, const PrecondView &v, const Modal<float> &M32, const float *s32,
                               int *density_id);
-// r32: the residual of the iterate xk (FP32, nullable) whose exact solution is
-// xstar (FP64, nullable); with both, the sample also stores the error xstar - xk.
-am_status precond_add_sample(am_precond *m, int density_id, const float *r32, const float *xk, const double *xstar,
+// r32: the residual of the iterate xk (nullable) whose exact solution is xstar
+// (nullable); with both, the sample also stores the error xstar - xk.
+am_status precond_add_sample(am_precond *m, int density_id, const float *r32, const double *xk, const double *xstar,
                              cudaStream_t st);
 
 }  // namespace amk

@@ -65,7 +65,8 @@ enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
 
 /* AM_PREC_FP64: every kernel in FP64 (the parity mode).
  * AM_PREC_MIXED: FP64 flexible CG (outer K*u, vectors, dots) preconditioned by FP32
- *   Jacobi PCG inner solves (FP32 K*u, double-float dot accumulation); a solve is
+ *   Jacobi PCG inner solves (FP32 K*u, r and p, FP64 iterate, double-float dot
+ *   accumulation); a solve is
  *   accepted on its recomputed FP64 residual r = f - K u.  Compliance, element
  *   energies, filter and the new densities are FP64; the OC bisection passes run in
  *   double-float. */
@@ -91,7 +92,8 @@ typedef struct am_simp_config {
     int cg_max_iterations;    /* cap on (inner) PCG iterations per solve (100000 by default) */
     int warm_start;           /* 1: each solve starts from the previous displacement */
     double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve that
-                                 preconditions the FP64 flexible CG (0.01 by default) */
+                                 preconditions the FP64 flexible CG; an inner solve stops at
+                                 max(inner_tol |r|, 0.3 cg_tol |f|) (0.01 by default) */
     int max_outer;            /* MIXED: cap on outer FP64 flexible-CG iterations per solve */
     int layout;               /* AM_LAYOUT_* of density arrays */
     int verbose;
