@@ -107,6 +107,26 @@ class TrainConfig(ctypes.Structure):
     ]
 
 
+class RunMetadata(ctypes.Structure):
+    """Mirror of ``am_run_metadata``."""
+
+    _fields_ = [
+        ("case_name", ctypes.c_char_p), ("mode", ctypes.c_char_p), ("provenance", ctypes.c_char_p),
+        ("resolution_mm", ctypes.c_double),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("n_elements", ctypes.c_longlong), ("n_design", ctypes.c_longlong), ("n_fixed", ctypes.c_longlong),
+        ("n_void", ctypes.c_longlong),
+        ("volume_fraction_target", ctypes.c_double),
+        ("has_history", ctypes.c_int),
+        ("volume_fraction_final", ctypes.c_double), ("compliance_final", ctypes.c_double),
+        ("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+        ("elapsed_time_s", ctypes.c_double),
+        ("threads", ctypes.c_int),
+        ("filter_radius", ctypes.c_double), ("E_min", ctypes.c_double), ("penalty", ctypes.c_double),
+        ("move_limit", ctypes.c_double),
+    ]
+
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _i8p = ctypes.POINTER(ctypes.c_int8)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
@@ -156,6 +176,10 @@ SIGNATURES = {
     "am_precond_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
+    "am_write_density_npy": (ctypes.c_int, [ctypes.c_char_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int]),
+    "am_write_history_csv": (ctypes.c_int, [ctypes.c_char_p, _dp, _dp, ctypes.c_int]),
+    "am_write_metadata_json": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(RunMetadata)]),
     "am_batch_create": (ctypes.c_int, [ctypes.c_int, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                        ctypes.POINTER(_vp)]),
     "am_batch_destroy": (ctypes.c_int, [_vp]),
@@ -559,6 +583,30 @@ class Batch:
                             pcg_iterations=int(pcg[p])))
             o += self.nel[p]
         return out
+
+
+def write_density_npy(path, rho, shape, layout=LAYOUT_ZFASTEST):
+    nx, ny, nz = (int(v) for v in shape)
+    r = f64(rho).ravel()
+    if r.size != nx * ny * nz:
+        raise ValueError("density size mismatch")
+    check(load().am_write_density_npy(os.fsencode(path), ptr(r), nx, ny, nz, int(layout)), "am_write_density_npy")
+
+
+def write_history_csv(path, compliance, volume):
+    c, v = f64(compliance).ravel(), f64(volume).ravel()
+    if c.size != v.size:
+        raise ValueError("history lengths differ")
+    check(load().am_write_history_csv(os.fsencode(path), ptr(c), ptr(v), c.size), "am_write_history_csv")
+
+
+def write_metadata_json(path, **fields):
+    m = RunMetadata()
+    for k, v in fields.items():
+        if not hasattr(m, k):
+            raise AttributeError(f"unknown metadata field {k}")
+        setattr(m, k, v.encode() if isinstance(v, str) else v)
+    check(load().am_write_metadata_json(os.fsencode(path), ctypes.byref(m)), "am_write_metadata_json")
 
 
 def launch_count() -> int:

@@ -348,6 +348,33 @@ am_status am_batch_simp_run(am_batch *b, const am_simp_config *cfgs, const doubl
                             double *compliance_hist, double *volume_hist, int *iterations, int *converged,
                             long long *pcg_iterations);
 
+/* ---- result writers (host only) ----------------------------------------------------
+ * The output files of the reference's C++ driver (cpp_engine/src/am_topopt.cpp), with
+ * its formats: numbers as a default C++ stream prints them (6 significant digits). */
+
+/* density_field.npy: NumPy v1.0, '<f8', C order (nx, ny, nz) (saveNpy, :344-396);
+ * rho in `layout`. */
+am_status am_write_density_npy(const char *path, const double *rho, int nx, int ny, int nz, int layout);
+
+/* history.csv: "iteration,compliance,volume" then one line per iteration (:622-629). */
+am_status am_write_history_csv(const char *path, const double *compliance, const double *volume, int n);
+
+/* metadata.json fields (saveMetadata, :401-447). */
+typedef struct am_run_metadata {
+    const char *case_name, *mode, *provenance;   /* e.g. "BRK-A-01", "cpp_standalone", "cpp_hpc_engine" */
+    double resolution_mm;
+    int nx, ny, nz;
+    long long n_elements, n_design, n_fixed, n_void;
+    double volume_fraction_target;
+    int has_history;                             /* 1: write the two *_final fields */
+    double volume_fraction_final, compliance_final;
+    int iterations, converged;
+    double elapsed_time_s;
+    int threads;                                 /* written as "openmp_threads" */
+    double filter_radius, E_min, penalty, move_limit;
+} am_run_metadata;
+am_status am_write_metadata_json(const char *path, const am_run_metadata *m);
+
 /* ---- allocation-free residual (no counterpart in the reference) ----------------
  * For callers that cannot allocate device memory once they are running -- code
  * inside another framework's fixed memory pool, allocation-free real-time or
