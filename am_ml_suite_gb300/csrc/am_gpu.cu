@@ -223,7 +223,7 @@ am_status build_taps(am_problem *P, double r, int variant) {
     return AM_OK;
 }
 
-Taps taps_of(am_problem *P) { return Taps{P->tap_d.p, P->tap_w.p, P->ntaps}; }
+Taps taps_of(am_problem *P) { return Taps{P->tap_d.p, P->tap_w.p, P->ntaps, (int)std::ceil(P->taps_r)}; }
 
 // Element scales + Jacobi diagonal for the density currently in `rho_dev`.
 am_status setup_operator(am_problem *P, const am_simp_config &c, const double *rho_dev) {

@@ -74,6 +74,8 @@ static cudaError_t set_ku_attr() {
                                 (int)Sh::template smem_bytes<T>());
 }
 
+cudaError_t filter_init_attributes();
+
 cudaError_t ku_init_attributes() {
     cudaError_t e;
 #define AMK_ATTR(T, X, Y, M) \
@@ -91,7 +93,7 @@ cudaError_t ku_init_attributes() {
     AMK_ATTR(double, 32, 4, KU_DOT)
     AMK_ATTR(double, 32, 8, KU_DOT)
 #undef AMK_ATTR
-    return cudaSuccess;
+    return filter_init_attributes();
 }
 
 template <typename T, int TX, int TY, int MODE>
@@ -813,9 +815,134 @@ __global__ void filter_cpp_kernel(Layout L, const int4 *__restrict__ td, const d
                                   double *__restrict__ out) {
     filter_cpp_body<T>(L, td, tw, ntaps, x, rho, out, grid_blk());
 }
+// Shared-memory halo stencil (FP64): a CTA of 32 x 8 threads owns a tile of
+// 32 x 8 x 4 elements (4 per thread along z) and first stages the tile plus a
+// halo of R = ceil(rmin) elements in shared memory -- (rho, x) for the C++ rule,
+// zero outside the grid (a zero term adds +0.0, so the sums equal the skipping
+// loop's bit for bit), or the reflected value for the Python rule -- then every
+// element sums its taps in the tap order from shared memory.
+constexpr int FT_X = 32, FT_Y = 8, FT_Z = 4;
+template <int R>
+constexpr size_t filter_smem_bytes(int arrays) {
+    return sizeof(double) * arrays * (FT_X + 2 * R) * (FT_Y + 2 * R) * (FT_Z + 2 * R);
+}
+
+__device__ __forceinline__ int reflect_idx(int i, int n);
+
+template <int R, int VARIANT>
+__global__ void __launch_bounds__(FT_X *FT_Y)
+    filter_smem_kernel(Layout L, const int4 *__restrict__ td, const double *__restrict__ tw, int ntaps,
+                       const double *__restrict__ x, const double *__restrict__ rho, double *__restrict__ out,
+                       int mode, double lo) {
+    extern __shared__ double fsm[];
+    constexpr int HX = FT_X + 2 * R, HY = FT_Y + 2 * R, HZ = FT_Z + 2 * R, HN = HX * HY * HZ;
+    double *sa = fsm;       // CPP: rho ; PY: the filtered quantity
+    double *sb = fsm + HN;  // CPP: x
+    const int tiles_x = (L.nx + FT_X - 1) / FT_X, tiles_y = (L.ny + FT_Y - 1) / FT_Y;
+    int b = blockIdx.x;
+    const int bx = b % tiles_x;
+    b /= tiles_x;
+    const int by = b % tiles_y, bz = b / tiles_y;
+    const int x0 = bx * FT_X - R, y0 = by * FT_Y - R, z0 = bz * FT_Z - R;
+    const int tid = threadIdx.y * FT_X + threadIdx.x;
+    for (int i = tid; i < HN; i += FT_X * FT_Y) {
+        const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+        int gx = x0 + hx, gy = y0 + hy, gz = z0 + hz;
+        if (VARIANT == 0) {
+            double ra = 0.0, xb = 0.0;
+            if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny && gz >= 0 && gz < L.nz) {
+                const long long n = elem_index(L, gx, gy, gz);
+                ra = rho[n];
+                xb = x[n];
+            }
+            sa[i] = ra;
+            sb[i] = xb;
+        } else {
+            const long long n = elem_index(L, reflect_idx(gx, L.nx), reflect_idx(gy, L.ny), reflect_idx(gz, L.nz));
+            sa[i] = mode == 2 ? x[n] * rho[n] : x[n];
+        }
+    }
+    __syncthreads();
+    const int ex = bx * FT_X + threadIdx.x, ey = by * FT_Y + threadIdx.y;
+    if (ex >= L.nx || ey >= L.ny) return;
+    for (int k = 0; k < FT_Z; ++k) {
+        const int ez = bz * FT_Z + k;
+        if (ez >= L.nz) break;
+        const int c = ((k + R) * HY + threadIdx.y + R) * HX + threadIdx.x + R;
+        double num = 0.0, den = 0.0, acc = 0.0;
+        for (int t = 0; t < ntaps; ++t) {
+            const int4 d = __ldg(td + t);
+            const double w = __ldg(tw + t);
+            const int j = c + (d.z * HY + d.y) * HX + d.x;
+            if (VARIANT == 0) {
+                const double rn = sa[j];
+                num += w * rn * sb[j];
+                den += w * rn;
+            } else {
+                acc += w * sa[j];
+            }
+        }
+        const long long e = elem_index(L, ex, ey, ez);
+        if (VARIANT == 0) {
+            out[e] = (den > 1e-15) ? num / den : x[e];
+        } else {
+            double o = acc;
+            if (mode == 1) o = npmin(npmax(o, lo), 1.0);
+            else if (mode == 2) o = o / npmax(rho[e], 1e-3);
+            out[e] = o;
+        }
+    }
+}
+
+template <int VARIANT>
+static bool launch_filter_smem(const Layout &L, const Taps &tp, const double *x, const double *rho, double *out,
+                               int mode, double lo, cudaStream_t st, cudaError_t *err) {
+    const int R = tp.R;
+    if (R < 1 || R > 3) return false;
+    const int tiles = ((L.nx + FT_X - 1) / FT_X) * ((L.ny + FT_Y - 1) / FT_Y) * ((L.nz + FT_Z - 1) / FT_Z);
+    const dim3 blk(FT_X, FT_Y);
+    const int arrays = VARIANT == 0 ? 2 : 1;
+    switch (R) {
+        case 1:
+            filter_smem_kernel<1, VARIANT><<<tiles, blk, filter_smem_bytes<1>(arrays), st>>>(L, tp.d, tp.w, tp.n, x,
+                                                                                            rho, out, mode, lo);
+            break;
+        case 2:
+            filter_smem_kernel<2, VARIANT><<<tiles, blk, filter_smem_bytes<2>(arrays), st>>>(L, tp.d, tp.w, tp.n, x,
+                                                                                            rho, out, mode, lo);
+            break;
+        default:
+            filter_smem_kernel<3, VARIANT><<<tiles, blk, filter_smem_bytes<3>(arrays), st>>>(L, tp.d, tp.w, tp.n, x,
+                                                                                            rho, out, mode, lo);
+            break;
+    }
+    *err = counted(cudaGetLastError());
+    return true;
+}
+
+cudaError_t filter_init_attributes() {
+    cudaError_t e;
+#define AMK_FATTR(R, V, A)                                                                                  \
+    if ((e = cudaFuncSetAttribute(filter_smem_kernel<R, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                  (int)filter_smem_bytes<R>(A))) != cudaSuccess)                            \
+        return e;
+    AMK_FATTR(1, 0, 2)
+    AMK_FATTR(2, 0, 2)
+    AMK_FATTR(3, 0, 2)
+    AMK_FATTR(1, 1, 1)
+    AMK_FATTR(2, 1, 1)
+    AMK_FATTR(3, 1, 1)
+#undef AMK_FATTR
+    return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t filter_cpp(const Layout &L, const Taps &tp, const double *x, const double *rho,
                        double *out, cudaStream_t st) {
+    if constexpr (std::is_same<T, double>::value) {
+        cudaError_t e;
+        if (launch_filter_smem<0>(L, tp, x, rho, out, 0, 0.0, st, &e)) return e;
+    }
     filter_cpp_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(
         L, tp.d, tp.w, tp.n, x, rho, out);
     return counted(cudaGetLastError());
@@ -859,6 +986,10 @@ __global__ void filter_py_kernel(Layout L, const int4 *__restrict__ td, const do
 template <typename T>
 cudaError_t filter_py(const Layout &L, const Taps &tp, const double *x, const double *rho,
                       double *out, int mode, double lo, cudaStream_t st) {
+    if constexpr (std::is_same<T, double>::value) {
+        cudaError_t e;
+        if (launch_filter_smem<1>(L, tp, x, rho, out, mode, lo, st, &e)) return e;
+    }
     filter_py_kernel<T><<<std::max(1, std::min(div_up(L.nel, 256), 152 * 16)), 256, 0, st>>>(
         L, tp.d, tp.w, tp.n, x, rho, out, mode, lo);
     return counted(cudaGetLastError());

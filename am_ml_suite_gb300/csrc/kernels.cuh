@@ -106,6 +106,7 @@ struct Taps {
     const int4 *d;       // (dx, dy, dz, 0)
     const double *w;     // weight
     int n;
+    int R;               // ceil(rmin): the halo of the shared-memory stencil (FP64, R <= 3)
 };
 // CPP: out = sum w rho_n x_n / sum w rho_n (neighbours in the grid), x if den <= 1e-15
 template <typename T>

@@ -385,6 +385,9 @@ def main():
     ap.add_argument("--probe", choices=["ku", "resid", "update"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--compare-fp64", action="store_true",
+                    help="time --steps SIMP iterations in mixed precision and in FP64 plain Jacobi from the same "
+                         "start and report the ratio and the compliance / density agreement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -426,6 +429,38 @@ def main():
         return
     shape = W["shape"]
     cfg = simp_config(nat, W)
+
+    if args.compare_fp64:
+        import torch
+
+        out = {}
+        for name, prec in (("mixed", nat.PREC_MIXED), ("fp64", nat.PREC_FP64)):
+            p = nat.Problem(shape, 1.0, 1.0, 0.3)
+            p.set_loads([W["F"]], [W["fixed"]])
+            c = simp_config(nat, W)
+            c.precision = prec
+            p.simp_begin(c, W["rho0"])
+            st = torch.cuda.ExternalStream(p.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            res = [p.simp_step() for _ in range(args.steps)]
+            e1.record(st)
+            torch.cuda.synchronize()
+            out[name] = dict(s=e0.elapsed_time(e1) * 1e-3, comp=np.array([r.compliance for r in res]),
+                             its=[r.solver_iterations for r in res], res=max(r.solver_residual for r in res),
+                             rho=p.simp_density())
+            p.close()
+        m, f = out["mixed"], out["fp64"]
+        print(json.dumps({
+            "metric": "SIMP s/iteration: mixed (FP32 inner, FP64 flexible CG) vs FP64 plain Jacobi PCG, same GPU",
+            "workload": args.workload, "steps": args.steps, "mixed_s_per_step": m["s"] / args.steps,
+            "fp64_s_per_step": f["s"] / args.steps, "speedup": f["s"] / m["s"],
+            "compliance_rel_diff_max": float(np.max(np.abs(m["comp"] - f["comp"]) / np.abs(f["comp"]))),
+            "density_max_abs_diff": float(np.max(np.abs(m["rho"] - f["rho"]))),
+            "pcg_iterations_mixed": m["its"], "pcg_iterations_fp64": f["its"],
+            "residual_max": max(m["res"], f["res"])}))
+        return
 
     if args.probe:
         # set-up only, then `reps` launches of one kernel (L2 flushed before each)
