@@ -171,6 +171,8 @@ SIGNATURES = {
     "am_precond_param_grad": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                              ctypes.POINTER(ctypes.c_float)]),
+    "am_precond_bench_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, _dp, _dp]),
     "am_precond_harvest": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _ip,
                                           ctypes.c_int]),
     "am_precond_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
@@ -451,6 +453,13 @@ class Preconditioner:
         check(load().am_precond_param_grad(self.handle, n, gz, gy, gx, x.ctypes.data_as(_fp),
                                            dout.ctypes.data_as(_fp), g.ctypes.data_as(_fp)), "am_precond_param_grad")
         return g
+
+    def bench_forward(self, n, gz, gy, gx, reps=5):
+        """(ms per forward pass, convolution flops per pass) on a device tensor."""
+        ms, fl = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        check(load().am_precond_bench_forward(self.handle, int(n), int(gz), int(gy), int(gx), int(reps),
+                                              ctypes.byref(ms), ctypes.byref(fl)), "am_precond_bench_forward")
+        return ms.value, fl.value
 
     def harvest(self, problem, cfg, rho, iters, load_case=0):
         it = np.ascontiguousarray(iters, dtype=np.int32)

@@ -261,9 +261,13 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     if (n < 1 || !shapes) return bfail(AM_ERR_INVALID_ARG, "need n >= 1 problems and their shapes");
     if (!(h > 0.0) || !(E0 > 0.0) || !(nu > -1.0 && nu < 0.5))
         return bfail(AM_ERR_INVALID_ARG, "need h > 0, E0 > 0, -1 < nu < 0.5");
-    for (int p = 0; p < n; ++p)
+    for (int p = 0; p < n; ++p) {
         if (shapes[3 * p] < 1 || shapes[3 * p + 1] < 1 || shapes[3 * p + 2] < 1)
             return bfail(AM_ERR_INVALID_ARG, "problem " + std::to_string(p) + ": dimensions must be >= 1");
+        // the batched warp-row K*u indexes a problem's nodes with 32-bit integers
+        if (3 * make_layout(shapes[3 * p], shapes[3 * p + 1], shapes[3 * p + 2]).cs >= (1LL << 31))
+            return bfail(AM_ERR_SIZE_MISMATCH, "problem " + std::to_string(p) + ": too large for a batch");
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return bfail(AM_ERR_NO_DEVICE, "no CUDA device");
     am_batch *B = new am_batch();

@@ -3,11 +3,11 @@
 // preconditioner (conv3d.cuh).
 //
 // Forward / backward-data: implicit GEMM, M = voxels (128 per CTA), N = output
-// channels (16, 32 or 64 per CTA), K = 27 taps x input channels in steps of 16.
-// Each K step stages a 128 x 16 slab of the input (the tap-shifted voxel rows,
-// zero-filled outside the grid) and a N x 16 slab of the weights in shared memory
-// with cp.async (double buffered), and the warps read their fragments with
-// ldmatrix.  Backward-weight: GEMM over voxels, M = output channels, N = input
+// channels (16, 32 or 64 per CTA), K = 27 taps x input channels.  A pipeline
+// stage holds 4 (tap, 16-channel) units -- a 128 x 64 slab of tap-shifted voxel
+// rows (zero-filled outside the grid) and the matching N x 64 weights -- staged
+// with cp.async (double buffered) and read with ldmatrix, so each barrier pair
+// covers 4 K steps of 16.  Backward-weight: GEMM over voxels, M = output channels, N = input
 // channels (tiles of 16/32), K = voxels in chunks of 64, split over the warps of a
 // CTA and over CTAs, finished with FP32 atomics.
 #include <algorithm>
@@ -67,6 +67,11 @@ struct FwdArgs {
 };
 
 constexpr int FM = 128;  // voxels per forward CTA
+constexpr int KU = 4;    // (tap, 16-channel) units per pipeline stage: K = 64 per barrier pair
+
+// 16-byte chunk index inside a 128-byte (KU x 16 BF16) shared-memory row, XOR
+// swizzled by the row so the 8 rows an ldmatrix reads fall on distinct banks
+__device__ __forceinline__ int swz8(int row, int chunk) { return chunk ^ (row & 7); }
 
 template <int NT>
 __global__ void __launch_bounds__(256) conv_fwd_kernel(FwdArgs A) {
@@ -74,15 +79,15 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(FwdArgs A) {
     constexpr int WM = 8 / WN;            // warps along M
     constexpr int TM = FM / WM, TN = NT / WN;
     constexpr int MI = TM / 16, NI = TN / 8;
-    __shared__ __align__(128) __nv_bfloat16 sA[2][FM * 16];
-    __shared__ __align__(128) __nv_bfloat16 sB[2][NT * 16];
+    __shared__ __align__(128) __nv_bfloat16 sA[2][FM * KU * 16];
+    __shared__ __align__(128) __nv_bfloat16 sB[2][NT * KU * 16];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = warp % WM, wn = warp / WM;
     const long long v0 = (long long)blockIdx.x * FM;
     const int n0 = blockIdx.y * NT;
     const int Dx = A.dx, Dy = A.dy, Dz = A.dz;
-    // the input row this thread stages: row tid/2, 16-byte half tid%2
-    const int arow = tid >> 1, ahalf = tid & 1;
+    // the input row this thread stages: row tid/2, units (tid%2)*2 and +1
+    const int arow = tid >> 1, apart = tid & 1;
     const long long av = v0 + arow;
     const bool arow_ok = av < A.V;
     int ax = 0, ay = 0, az = 0;
@@ -95,19 +100,30 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(FwdArgs A) {
         az = (int)(t % Dz);
     }
     const int ksteps = A.cin / 16;
-    const int nstages = 27 * ksteps;
+    const int units = 27 * ksteps;  // (tap, 16-channel chunk) pairs, tap-major
+    const int nstages = (units + KU - 1) / KU;
     auto load_stage = [&](int s, int buf) {
-        const int tap = s / ksteps, kc = s - tap * ksteps;
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int sx = ax + dx, sy = ay + dy, sz = az + dz;
-        const bool ok = arow_ok && sx >= 0 && sx < Dx && sy >= 0 && sy < Dy && sz >= 0 && sz < Dz;
-        const long long sv = av + ((long long)dz * Dy + dy) * Dx + dx;
-        const __nv_bfloat16 *src = ok ? A.x + sv * A.xcs + A.xco + kc * 16 + ahalf * 8 : A.x;
-        cp_async16(&sA[buf][arow * 16 + swz(arow, ahalf, 16) * 8], src, ok);
-        if (tid < NT * 2) {
-            const int brow = tid >> 1, bhalf = tid & 1;
-            const __nv_bfloat16 *wsrc = A.w + ((long long)tap * A.cout + n0 + brow) * A.cin + kc * 16 + bhalf * 8;
-            cp_async16(&sB[buf][brow * 16 + swz(brow, bhalf, 16) * 8], wsrc, true);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int j = apart * 2 + q;  // unit of the stage
+            const int u = s * KU + j;
+            const int tap = u / ksteps, kc = u - tap * ksteps;
+            const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+            const int sx = ax + dx, sy = ay + dy, sz = az + dz;
+            const bool ok = u < units && arow_ok && sx >= 0 && sx < Dx && sy >= 0 && sy < Dy && sz >= 0 && sz < Dz;
+            const long long sv = av + ((long long)dz * Dy + dy) * Dx + dx;
+            const __nv_bfloat16 *src = ok ? A.x + sv * A.xcs + A.xco + kc * 16 : A.x;
+            cp_async16(&sA[buf][arow * KU * 16 + swz8(arow, 2 * j) * 8], src, ok);
+            cp_async16(&sA[buf][arow * KU * 16 + swz8(arow, 2 * j + 1) * 8], ok ? src + 8 : A.x, ok);
+        }
+        for (int t = tid; t < NT * KU * 2; t += 256) {
+            const int brow = t / (KU * 2), c = t % (KU * 2);
+            const int u = s * KU + c / 2;
+            const bool ok = u < units;
+            const int tap = ok ? u / ksteps : 0, kc = ok ? u - tap * ksteps : 0;
+            const __nv_bfloat16 *wsrc =
+                ok ? A.w + ((long long)tap * A.cout + n0 + brow) * A.cin + kc * 16 + (c & 1) * 8 : A.w;
+            cp_async16(&sB[buf][brow * KU * 16 + swz8(brow, c) * 8], wsrc, ok);
         }
         cp_async_commit();
     };
@@ -129,24 +145,27 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(FwdArgs A) {
             cp_async_wait<0>();
         }
         __syncthreads();
-        unsigned a[MI][4];
 #pragma unroll
-        for (int mi = 0; mi < MI; ++mi) {
-            const int r = wm * TM + mi * 16 + mrow + ((mtx & 1) ? 8 : 0);
-            const int h = mtx >> 1;
-            ldsm_x4(a[mi][0], a[mi][1], a[mi][2], a[mi][3], &sA[buf][r * 16 + swz(r, h, 16) * 8]);
+        for (int j = 0; j < KU; ++j) {
+            unsigned a[MI][4];
+#pragma unroll
+            for (int mi = 0; mi < MI; ++mi) {
+                const int r = wm * TM + mi * 16 + mrow + ((mtx & 1) ? 8 : 0);
+                const int c = 2 * j + (mtx >> 1);
+                ldsm_x4(a[mi][0], a[mi][1], a[mi][2], a[mi][3], &sA[buf][r * KU * 16 + swz8(r, c) * 8]);
+            }
+            unsigned b[NI][2];
+#pragma unroll
+            for (int nj = 0; nj < NI; nj += 2) {
+                const int r = wn * TN + nj * 8 + mrow + ((mtx >> 1) ? 8 : 0);
+                const int c = 2 * j + (mtx & 1);
+                ldsm_x4(b[nj][0], b[nj][1], b[nj + 1][0], b[nj + 1][1], &sB[buf][r * KU * 16 + swz8(r, c) * 8]);
+            }
+#pragma unroll
+            for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+                for (int ni = 0; ni < NI; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni][0], b[ni][1]);
         }
-        unsigned b[NI][2];
-#pragma unroll
-        for (int nj = 0; nj < NI; nj += 2) {
-            const int r = wn * TN + nj * 8 + mrow + ((mtx >> 1) ? 8 : 0);
-            const int h = mtx & 1;
-            ldsm_x4(b[nj][0], b[nj][1], b[nj + 1][0], b[nj + 1][1], &sB[buf][r * 16 + swz(r, h, 16) * 8]);
-        }
-#pragma unroll
-        for (int mi = 0; mi < MI; ++mi)
-#pragma unroll
-            for (int ni = 0; ni < NI; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni][0], b[ni][1]);
         __syncthreads();
     }
     // epilogue: rows g and g+8 of each m16 tile, columns 2*tig, 2*tig+1 of each n8 tile

@@ -33,10 +33,16 @@ KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms) {
         K.ty = 4;
         K.warps = 0;
         ctas_per_sm = 3;
-    } else {
+    } else if (3 * L.cs < (1LL << 31) && L.nel < (1LL << 31)) {
+        // warp-row kernel (32-bit indices)
         K.warps = 8;
         K.tx = Ku2Shape<8>::TX;
         K.ty = Ku2Shape<8>::TY;
+        ctas_per_sm = 2;
+    } else {
+        K.tx = 32;
+        K.ty = 8;
+        K.warps = 0;
         ctas_per_sm = 2;
     }
     K.tiles_x = div_up(L.nx + 1, K.tx);

@@ -88,7 +88,12 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     const int tz_ = b / A.tiles_y;
     const int x0 = tx_ * 30, y0 = ty_ * TY, z0 = tz_ * A.tz;
     const int z1 = min(z0 + A.tz, L.nz + 1);
-    const long long cs = L.cs;
+    // 32-bit node and element indices (the host guarantees 3 cs < 2^31): the
+    // address arithmetic of the 30-odd loads and stores per lane and layer is the
+    // largest integer cost of the kernel
+    const int cs = (int)L.cs, sx = L.sx, sxy = (int)L.sxy, enx = L.nx, enxy = L.nx * L.ny;
+    auto nidx = [&](int ix, int iy, int iz) { return iz * sxy + iy * sx + ix; };
+    auto eidx = [&](int ex, int ey, int ez) { return ez * enxy + ey * enx + ex; };
     const int gx = x0 - 1 + lane;            // this lane's node column (element column for lanes < 31)
     const int gy0 = y0 - 1 + 2 * w;          // node rows gy0, gy0+1, gy0+2
     const bool col_in = gx >= 0 && gx <= L.nx;
@@ -118,12 +123,12 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     // memory round trips overlap.
     auto load_plane = [&](int iz, float (&v)[3][3]) {
         float d[3], rv[3][3], pv[3][3];
-        long long n[3];
+        int n[3];
         bool ok[3];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
             ok[rr] = col_in && row_in[rr] && iz >= 0 && iz <= L.nz;
-            n[rr] = ok[rr] ? node_index(L, gx, gy0 + rr, iz) : 0;
+            n[rr] = ok[rr] ? nidx(gx, gy0 + rr, iz) : 0;
             d[rr] = 0.f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) rv[rr][c] = pv[rr][c] = 0.f;
@@ -185,13 +190,13 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
         // constraint bits of this layer's output nodes, issued first ----------------
         float sA = 0.f, sB = 0.f;
         if (elem_col && ez >= 0 && ez < L.nz) {
-            if (elemA_row) sA = __ldg(gs + elem_index(L, gx, gy0, ez));
-            if (elemB_row) sB = __ldg(gs + elem_index(L, gx, gy0 + 1, ez));
+            if (elemA_row) sA = __ldg(gs + eidx(gx, gy0, ez));
+            if (elemB_row) sB = __ldg(gs + eidx(gx, gy0 + 1, ez));
         }
         unsigned mrow[2] = {0u, 0u};
         if (MODE == KU_PCG && ez >= z0 && lane_owned) {
-            if (row_in[0]) mrow[0] = __ldg(gm + node_index(L, gx, gy0, ez));
-            if (row_in[1]) mrow[1] = __ldg(gm + node_index(L, gx, gy0 + 1, ez));
+            if (row_in[0]) mrow[0] = __ldg(gm + nidx(gx, gy0, ez));
+            if (row_in[1]) mrow[1] = __ldg(gm + nidx(gx, gy0 + 1, ez));
         }
         // ---- top plane of this layer -----------------------------------------
         float v[3][3];
@@ -285,7 +290,7 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
 #pragma unroll
             for (int rr = 0; rr < 2; ++rr) {
                 if ((rr == 0 && w == 0) || !row_in[rr]) continue;
-                const long long n = node_index(L, gx, gy0 + rr, ez);
+                const int n = nidx(gx, gy0 + rr, ez);
                 if (MODE == KU_PLAIN) {
 #pragma unroll
                     for (int c = 0; c < 3; ++c) A.y[n + c * cs] = V[rr][c];

@@ -940,6 +940,40 @@ am_status am_precond_param_grad(am_precond *M, int n, int gz, int gy, int gx, co
     return AM_OK;
 }
 
+am_status am_precond_bench_forward(am_precond *M, int n, int gz, int gy, int gx, int reps, double *avg_ms,
+                                   double *flops) {
+    PCKS(check_pre(M));
+    if (n < 1 || gz < 8 || gy < 8 || gx < 8 || gz % 8 || gy % 8 || gx % 8 || reps < 1)
+        return pfail(AM_ERR_INVALID_ARG, "need positive multiples of 8 and reps >= 1");
+    Acts &A = M->infer;
+    PCK(ensure_acts(A, n, gz, gy, gx, false));
+    const long long V = (long long)n * gz * gy * gx;
+    PCK(fill_zero_bf16(A.x0, V * 16, M->st));
+    PCK(forward(M, A, M->st));  // warm-up
+    cudaEvent_t e0, e1;
+    PCK(cudaEventCreate(&e0));
+    PCK(cudaEventCreate(&e1));
+    PCK(cudaEventRecord(e0, M->st));
+    for (int r = 0; r < reps; ++r) PCK(forward(M, A, M->st));
+    PCK(cudaEventRecord(e1, M->st));
+    PCK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    PCK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (avg_ms) *avg_ms = ms / reps;
+    if (flops) {
+        // 2 * 27 * cin * cout per voxel of each layer's grid (channels as computed)
+        double f = 0.0;
+        const int level[kLayers] = {0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0};
+        for (int l = 0; l < kLayers; ++l)
+            f += 2.0 * 27.0 * kSpec[l].cin * kSpec[l].cout * (double)(V >> (3 * level[l]));
+        *flops = f;
+    }
+    count_launches(21LL * (reps + 1));
+    return AM_OK;
+}
+
 am_status am_precond_train(am_precond *M, const am_train_config *cfg, float *epoch_loss) {
     PCKS(check_pre(M));
     if (!cfg) return pfail(AM_ERR_INVALID_ARG, "null training config");

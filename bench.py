@@ -382,7 +382,7 @@ def main():
     ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS) + ["batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--probe", choices=["ku", "resid", "update"],
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--compare-fp64", action="store_true",
@@ -460,6 +460,19 @@ def main():
             "density_max_abs_diff": float(np.max(np.abs(m["rho"] - f["rho"]))),
             "pcg_iterations_mixed": m["its"], "pcg_iterations_fp64": f["its"],
             "residual_max": max(m["res"], f["res"])}))
+        return
+
+    if args.probe == "conv":
+        # forward passes of the learned preconditioner on this workload's node grid
+        pre = nat.Preconditioner(seed=0, capacity=0)
+        nx, ny, nz = shape
+        g = [(v + 1 + 7) // 8 * 8 for v in (nz, ny, nx)]
+        ms, flops = pre.bench_forward(1, g[0], g[1], g[2], reps=args.reps)
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f).get("bf16_tflops", 1900.0))
+        tf = flops / (ms * 1e-3) / 1e12
+        print(json.dumps({"probe": "conv", "workload": args.workload, "grid_zyx": g, "reps": args.reps,
+                          "ms_per_forward": ms, "tflops": tf, "bf16_peak_tflops": peak, "frac": tf / peak}))
         return
 
     if args.probe:

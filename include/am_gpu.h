@@ -276,6 +276,11 @@ am_status am_precond_set_params(am_precond *m, const float *w);
 am_status am_precond_forward(am_precond *m, int n, int gz, int gy, int gx, const float *in, float *out);
 am_status am_precond_param_grad(am_precond *m, int n, int gz, int gy, int gx, const float *in, const float *dout,
                                 float *grad);
+/* Times `reps` forward passes of the network on an n x gz x gy x gx device tensor
+ * (multiples of 8) with CUDA events; *flops = the convolutions' 2*27*cin*cout per
+ * voxel summed over the layers (measurement; no reference counterpart). */
+am_status am_precond_bench_forward(am_precond *m, int n, int gz, int gy, int gx, int reps, double *avg_ms,
+                                   double *flops);
 /* Adds training samples: at density rho (host, cfg->layout) the problem's FP32
  * Jacobi PCG runs from u = 0 on load case `load_case`; the residual r_k and the
  * error e_k = u* - u_k after each iteration count k in iters[0..n_iters)
