@@ -92,14 +92,17 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     // address arithmetic of the 30-odd loads and stores per lane and layer is the
     // largest integer cost of the kernel
     const int cs = (int)L.cs, sx = L.sx, sxy = (int)L.sxy, enx = L.nx, enxy = L.nx * L.ny;
-    auto nidx = [&](int ix, int iy, int iz) { return iz * sxy + iy * sx + ix; };
-    auto eidx = [&](int ex, int ey, int ez) { return ez * enxy + ey * enx + ex; };
+
     const int gx = x0 - 1 + lane;            // this lane's node column (element column for lanes < 31)
     const int gy0 = y0 - 1 + 2 * w;          // node rows gy0, gy0+1, gy0+2
     const bool col_in = gx >= 0 && gx <= L.nx;
     const bool row_in[3] = {gy0 >= 0 && gy0 <= L.ny, gy0 + 1 >= 0 && gy0 + 1 <= L.ny,
                             gy0 + 2 >= 0 && gy0 + 2 <= L.ny};
     const bool lane_owned = lane >= 1 && lane <= 30 && gx <= L.nx;
+    // this lane's offsets of rows gy0 .. gy0+2 within a node plane (plane iz adds iz sxy)
+    const int rowoff[3] = {gy0 * sx + gx, (gy0 + 1) * sx + gx, (gy0 + 2) * sx + gx};
+    const bool rowok[3] = {col_in && row_in[0], col_in && row_in[1], col_in && row_in[2]};
+    const int erowA = gy0 * enx + gx, erowB = (gy0 + 1) * enx + gx;  // element rows (layer ez adds ez nx ny)
     const bool elem_col = lane <= 30 && gx >= 0 && gx < L.nx;
     const bool elemA_row = gy0 >= 0 && gy0 < L.ny, elemB_row = gy0 + 1 >= 0 && gy0 + 1 < L.ny;
 
@@ -127,8 +130,8 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
         bool ok[3];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
-            ok[rr] = col_in && row_in[rr] && iz >= 0 && iz <= L.nz;
-            n[rr] = ok[rr] ? nidx(gx, gy0 + rr, iz) : 0;
+            ok[rr] = rowok[rr] && iz >= 0 && iz <= L.nz;
+            n[rr] = ok[rr] ? iz * sxy + rowoff[rr] : 0;
             d[rr] = 0.f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) rv[rr][c] = pv[rr][c] = 0.f;
@@ -190,13 +193,13 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
         // constraint bits of this layer's output nodes, issued first ----------------
         float sA = 0.f, sB = 0.f;
         if (elem_col && ez >= 0 && ez < L.nz) {
-            if (elemA_row) sA = __ldg(gs + eidx(gx, gy0, ez));
-            if (elemB_row) sB = __ldg(gs + eidx(gx, gy0 + 1, ez));
+            if (elemA_row) sA = __ldg(gs + ez * enxy + erowA);
+            if (elemB_row) sB = __ldg(gs + ez * enxy + erowB);
         }
         unsigned mrow[2] = {0u, 0u};
         if (MODE == KU_PCG && ez >= z0 && lane_owned) {
-            if (row_in[0]) mrow[0] = __ldg(gm + nidx(gx, gy0, ez));
-            if (row_in[1]) mrow[1] = __ldg(gm + nidx(gx, gy0 + 1, ez));
+            if (row_in[0]) mrow[0] = __ldg(gm + ez * sxy + rowoff[0]);
+            if (row_in[1]) mrow[1] = __ldg(gm + ez * sxy + rowoff[1]);
         }
         // ---- top plane of this layer -----------------------------------------
         float v[3][3];
@@ -290,7 +293,7 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
 #pragma unroll
             for (int rr = 0; rr < 2; ++rr) {
                 if ((rr == 0 && w == 0) || !row_in[rr]) continue;
-                const int n = nidx(gx, gy0 + rr, ez);
+                const int n = ez * sxy + rowoff[rr];
                 if (MODE == KU_PLAIN) {
 #pragma unroll
                     for (int c = 0; c < 3; ++c) A.y[n + c * cs] = V[rr][c];
