@@ -66,6 +66,82 @@ __device__ __forceinline__ Face face_modes(float v0, float v1, float v2, float n
     f.dd = sub(dhi, dlo);
     return f;
 }
+// The element transform of one layer for the lane's two elements: face modes of
+// the bottom (FB) and top (FT) node planes -> Walsh coefficients -> scaled modal
+// stiffness -> transposed transform.  The bottom half of the result joins the
+// carry CT of the plane below and gives V: rows 0..2 of the bottom plane at this
+// lane's column, with the left neighbour lane's elements added (row 0 still lacks
+// the warp below's elements, row 2 is passed to the warp above).  The top half
+// becomes the new carry.
+__device__ __forceinline__ void layer_math(const Face (&FB)[3], const Face (&FT)[3], Face (&CT)[3], const float2 sc,
+                                           const Modal<float> &M, const float2 lam, const float2 mu,
+                                           const float2 twomu, const float2 thrmu, float (&V)[3][3]) {
+    const float2 c1 = mul(sc, splat(M.c1)), c2 = mul(sc, splat(M.c2)), c7 = mul(sc, splat(M.c7));
+    // ---- z stage: Walsh coefficients A[m][c] of both elements --------------
+    float2 A1[3], A2[3], A3[3], A4[3], A5[3], A6[3], A7[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        A1[c] = add(FT[c].ds, FB[c].ds);
+        A6[c] = sub(FT[c].ds, FB[c].ds);
+        A2[c] = add(FT[c].sd, FB[c].sd);
+        A5[c] = sub(FT[c].sd, FB[c].sd);
+        A3[c] = sub(FT[c].ss, FB[c].ss);
+        A4[c] = add(FT[c].dd, FB[c].dd);
+        A7[c] = sub(FT[c].dd, FB[c].dd);
+    }
+    // ---- modal stiffness (scaled) ---------------------------------------------
+    float2 Y1[3], Y2[3], Y3[3], Y4[3], Y5[3], Y6[3], Y7[3];
+    {
+        const float2 lt = mul(lam, add(add(A1[0], A2[1]), A3[2]));
+        const float2 s00 = fma(twomu, A1[0], lt), s11 = fma(twomu, A2[1], lt), s22 = fma(twomu, A3[2], lt);
+        const float2 s01 = mul(mu, add(A1[1], A2[0]));
+        const float2 s02 = mul(mu, add(A1[2], A3[0]));
+        const float2 s12 = mul(mu, add(A2[2], A3[1]));
+        Y1[0] = mul(c1, s00); Y1[1] = mul(c1, s01); Y1[2] = mul(c1, s02);
+        Y2[0] = Y1[1];        Y2[1] = mul(c1, s11); Y2[2] = mul(c1, s12);
+        Y3[0] = Y1[2];        Y3[1] = Y2[2];        Y3[2] = mul(c1, s22);
+        const float2 ltx = mul(lam, add(A4[1], A6[2]));
+        const float2 lte = mul(lam, add(A4[0], A5[2]));
+        const float2 ltz = mul(lam, add(A6[0], A5[1]));
+        const float2 shx = mul(mu, add(A4[2], A6[1]));
+        const float2 she = mul(mu, add(A4[2], A5[0]));
+        const float2 shz = mul(mu, add(A6[1], A5[0]));
+        Y4[0] = mul(c2, fma(thrmu, A4[0], lte));
+        Y4[1] = mul(c2, fma(thrmu, A4[1], ltx));
+        Y4[2] = mul(c2, add(shx, she));
+        Y6[0] = mul(c2, fma(thrmu, A6[0], ltz));
+        Y6[1] = mul(c2, add(shx, shz));
+        Y6[2] = mul(c2, fma(thrmu, A6[2], ltx));
+        Y5[0] = mul(c2, add(she, shz));
+        Y5[1] = mul(c2, fma(thrmu, A5[1], ltz));
+        Y5[2] = mul(c2, fma(thrmu, A5[2], lte));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Y7[c] = mul(c7, A7[c]);
+    }
+    // ---- transposed z stage; the bottom half joins the carry of the plane ----
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        Face P;  // face modes of plane ez: carried top half of layer ez-1 + bottom half of layer ez
+        P.ss = sub(CT[c].ss, Y3[c]);
+        P.sd = add(CT[c].sd, sub(Y2[c], Y5[c]));
+        P.ds = add(CT[c].ds, sub(Y1[c], Y6[c]));
+        P.dd = add(CT[c].dd, sub(Y4[c], Y7[c]));
+        CT[c].ss = Y3[c];
+        CT[c].sd = add(Y2[c], Y5[c]);
+        CT[c].ds = add(Y1[c], Y6[c]);
+        CT[c].dd = add(Y4[c], Y7[c]);
+        // transposed y and x stages
+        const float2 sHi = add(P.ss, P.sd), sLo = sub(P.ss, P.sd);
+        const float2 dHi = add(P.ds, P.dd), dLo = sub(P.ds, P.dd);
+        const float2 loR = add(sLo, dLo), loL = sub(sLo, dLo);
+        const float2 hiR = add(sHi, dHi), hiL = sub(sHi, dHi);
+        // rows: 0 <- first element lo; 1 <- first hi + second lo; 2 <- second hi
+        const float R0 = loR.x, R1 = hiR.x + loR.y, R2 = hiR.y;
+        V[0][c] = loL.x + __shfl_up_sync(0xffffffffu, R0, 1);
+        V[1][c] = (hiL.x + loL.y) + __shfl_up_sync(0xffffffffu, R1, 1);
+        V[2][c] = hiL.y + __shfl_up_sync(0xffffffffu, R2, 1);
+    }
+}
 }  // namespace k2
 
 // One tile (block B.b of B.n); ku2_kernel runs one tile per CTA, the batched
@@ -212,73 +288,8 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
             const float n2 = __shfl_down_sync(0xffffffffu, v[2][c], 1);
             FT[c] = face_modes(v[0][c], v[1][c], v[2][c], n0, n1, n2);
         }
-        const float2 sc = make_float2(sA, sB);
-        const float2 c1 = mul(sc, splat(A.M.c1)), c2 = mul(sc, splat(A.M.c2)), c7 = mul(sc, splat(A.M.c7));
-        // ---- z stage: Walsh coefficients A[m][c] of both elements --------------
-        float2 A1[3], A2[3], A3[3], A4[3], A5[3], A6[3], A7[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            A1[c] = add(FT[c].ds, FB[c].ds);
-            A6[c] = sub(FT[c].ds, FB[c].ds);
-            A2[c] = add(FT[c].sd, FB[c].sd);
-            A5[c] = sub(FT[c].sd, FB[c].sd);
-            A3[c] = sub(FT[c].ss, FB[c].ss);
-            A4[c] = add(FT[c].dd, FB[c].dd);
-            A7[c] = sub(FT[c].dd, FB[c].dd);
-        }
-        // ---- modal stiffness (scaled) ---------------------------------------------
-        float2 Y1[3], Y2[3], Y3[3], Y4[3], Y5[3], Y6[3], Y7[3];
-        {
-            const float2 lt = mul(lam, add(add(A1[0], A2[1]), A3[2]));
-            const float2 s00 = fma(twomu, A1[0], lt), s11 = fma(twomu, A2[1], lt), s22 = fma(twomu, A3[2], lt);
-            const float2 s01 = mul(mu, add(A1[1], A2[0]));
-            const float2 s02 = mul(mu, add(A1[2], A3[0]));
-            const float2 s12 = mul(mu, add(A2[2], A3[1]));
-            Y1[0] = mul(c1, s00); Y1[1] = mul(c1, s01); Y1[2] = mul(c1, s02);
-            Y2[0] = Y1[1];        Y2[1] = mul(c1, s11); Y2[2] = mul(c1, s12);
-            Y3[0] = Y1[2];        Y3[1] = Y2[2];        Y3[2] = mul(c1, s22);
-            const float2 ltx = mul(lam, add(A4[1], A6[2]));
-            const float2 lte = mul(lam, add(A4[0], A5[2]));
-            const float2 ltz = mul(lam, add(A6[0], A5[1]));
-            const float2 shx = mul(mu, add(A4[2], A6[1]));
-            const float2 she = mul(mu, add(A4[2], A5[0]));
-            const float2 shz = mul(mu, add(A6[1], A5[0]));
-            Y4[0] = mul(c2, fma(thrmu, A4[0], lte));
-            Y4[1] = mul(c2, fma(thrmu, A4[1], ltx));
-            Y4[2] = mul(c2, add(shx, she));
-            Y6[0] = mul(c2, fma(thrmu, A6[0], ltz));
-            Y6[1] = mul(c2, add(shx, shz));
-            Y6[2] = mul(c2, fma(thrmu, A6[2], ltx));
-            Y5[0] = mul(c2, add(she, shz));
-            Y5[1] = mul(c2, fma(thrmu, A5[1], ltz));
-            Y5[2] = mul(c2, fma(thrmu, A5[2], lte));
-#pragma unroll
-            for (int c = 0; c < 3; ++c) Y7[c] = mul(c7, A7[c]);
-        }
-        // ---- transposed z stage; the bottom half joins the carry of the plane ----
         float V[3][3];  // node values of rows 0..2 of plane ez (this warp's part)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            Face P;  // face modes of plane ez: carried top half of layer ez-1 + bottom half of layer ez
-            P.ss = sub(CT[c].ss, Y3[c]);
-            P.sd = add(CT[c].sd, sub(Y2[c], Y5[c]));
-            P.ds = add(CT[c].ds, sub(Y1[c], Y6[c]));
-            P.dd = add(CT[c].dd, sub(Y4[c], Y7[c]));
-            CT[c].ss = Y3[c];
-            CT[c].sd = add(Y2[c], Y5[c]);
-            CT[c].ds = add(Y1[c], Y6[c]);
-            CT[c].dd = add(Y4[c], Y7[c]);
-            // transposed y and x stages
-            const float2 sHi = add(P.ss, P.sd), sLo = sub(P.ss, P.sd);
-            const float2 dHi = add(P.ds, P.dd), dLo = sub(P.ds, P.dd);
-            const float2 loR = add(sLo, dLo), loL = sub(sLo, dLo);
-            const float2 hiR = add(sHi, dHi), hiL = sub(sHi, dHi);
-            // rows: 0 <- first element lo; 1 <- first hi + second lo; 2 <- second hi
-            const float R0 = loR.x, R1 = hiR.x + loR.y, R2 = hiR.y;
-            V[0][c] = loL.x + __shfl_up_sync(0xffffffffu, R0, 1);
-            V[1][c] = (hiL.x + loL.y) + __shfl_up_sync(0xffffffffu, R1, 1);
-            V[2][c] = hiL.y + __shfl_up_sync(0xffffffffu, R2, 1);
-        }
+        layer_math(FB, FT, CT, make_float2(sA, sB), A.M, lam, mu, twomu, thrmu, V);
         // ---- shared row with the warp above -------------------------------------
         const int slot = ez & 1;
 #pragma unroll
