@@ -53,26 +53,33 @@ double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Device array of n elements at p, zero-filled, with `pad` zero elements of
+// slack before and after it (vectors read by the unpredicated K*u kernel).
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
-    cudaError_t alloc(size_t count) {
-        if (p && n >= count) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    T *base = nullptr;
+    size_t pad = 0;
+    cudaError_t alloc(size_t count, size_t slack = 0) {
+        if (p && n >= count && pad >= slack) return cudaSuccess;
+        release();
+        const size_t total = std::max<size_t>(count + 2 * slack, 1);
+        cudaError_t e = cudaMalloc(&base, total * sizeof(T));
         if (e == cudaSuccess) {
+            p = base + slack;
             n = count;
-            e = cudaMemset(p, 0, std::max<size_t>(count, 1) * sizeof(T));
+            pad = slack;
+            e = cudaMemset(base, 0, total * sizeof(T));
+        } else {
+            base = nullptr;
         }
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
+        if (base) cudaFree(base);
+        p = base = nullptr;
+        n = pad = 0;
     }
 };
 
@@ -158,7 +165,8 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
     CK(P->xw64.alloc(nv));
     CK(P->vstage.alloc(std::max<size_t>(nv, (size_t)P->N)));
     CK(P->dinv64.alloc(P->L.cs));
-    CK(P->dinv32.alloc(P->L.cs));
+    const size_t slack = (size_t)ku2_slack(P->L);  // PCG vectors of the unpredicated K*u
+    CK(P->dinv32.alloc(P->L.cs, slack));
     CK(P->mask.alloc(P->L.cs));
     CK(P->nofix.alloc(P->L.cs));
     if (fp64) {
@@ -168,9 +176,9 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
     } else {
         CK(P->x32.alloc(nv));
         CK(P->xi64.alloc(nv));
-        CK(P->r32.alloc(nv));
-        CK(P->p32a.alloc(nv));
-        CK(P->p32b.alloc(nv));
+        CK(P->r32.alloc(nv, slack));
+        CK(P->p32a.alloc(nv, slack));
+        CK(P->p32b.alloc(nv, slack));
         CK(P->q32v.alloc(nv));
     }
     const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), P->nblocks_vec, 152 * 16});
@@ -999,8 +1007,7 @@ am_status am_simp_step(am_problem *P, am_iteration_result *res) {
     // OC update
     CKS(run_oc(P, f64, c.variant, c.move_limit, c.rho_min, c.volume_fraction, P->n_design, P->rho.p, P->dcf.p,
                P->design.p, P->rho_new.p));
-    std::swap(P->rho.p, P->rho_new.p);
-    std::swap(P->rho.n, P->rho_new.n);
+    std::swap(P->rho, P->rho_new);
     R.update_time_s = now_s() - tu;
     R.max_density_change = P->Sh->oc_change;
     R.volume_fraction = P->Sh->oc_volume;

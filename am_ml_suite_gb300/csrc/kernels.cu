@@ -121,6 +121,8 @@ static cudaError_t dispatch_ku(const KuLaunch &K, KuArgs<T> &a, cudaStream_t st)
     return cudaErrorInvalidValue;
 }
 
+// PCG launches come from the single-problem engine, whose PCG vectors carry
+// ku2_slack(): their node loads are unpredicated
 template <int MODE>
 static cudaError_t launch_ku2(const KuLaunch &K, Ku2Args &a, cudaStream_t st) {
     a.tiles_x = K.tiles_x;
@@ -128,7 +130,7 @@ static cudaError_t launch_ku2(const KuLaunch &K, Ku2Args &a, cudaStream_t st) {
     a.tiles_z = K.tiles_z;
     a.tz = K.tz;
     if (K.warps == 8) {
-        ku2_kernel<8, MODE><<<K.ntiles(), 256, 0, st>>>(a);
+        ku2_kernel<8, MODE, MODE == KU_PCG><<<K.ntiles(), 256, 0, st>>>(a);
         return counted(cudaGetLastError());
     }
     return cudaErrorInvalidValue;

@@ -15,6 +15,11 @@ void count_launches(long long n);
 void set_last_error(const char *msg);
 
 // ---- tiled K*u (ku.cuh: FP64 / generic, ku2.cuh: FP32 warp-row form) --------
+// Slack (entries) on both sides of a vector read by the unpredicated warp-row
+// PCG kernel: the tiles' halo reaches one plane below node 0 and up to one plane,
+// 2W+1 rows and 32 columns past the last plane of the last component.
+inline long long ku2_slack(const Layout &L) { return (2 * L.sxy + 64LL * L.sx + 256 + 63) / 64 * 64; }
+
 struct KuLaunch {
     int tx, ty;  // owned node columns per tile (one of the compiled shapes)
     int tz;      // node planes per tile
@@ -31,7 +36,9 @@ template <typename T>
 cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
                      T *y, cudaStream_t st);
 // p = dinv r + beta p_prev, q = mask(K p), partial p.q -> S->alpha.  p_prev / p are
-// the ping-pong pair (pa, pb) chosen by the parity of S->it.
+// the ping-pong pair (pa, pb) chosen by the parity of S->it.  FP32 on the warp-row
+// plan: pa, pb, r and dinv are read without bounds predicates and need
+// ku2_slack(L) finite (zeroed) entries before and after their allocation.
 template <typename T>
 cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, T *pa, T *pb,
                    const T *r, const T *dinv, const uint8_t *mask, T *q, double *partial, Scalars *S,

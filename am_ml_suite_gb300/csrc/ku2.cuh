@@ -145,8 +145,14 @@ __device__ __forceinline__ void layer_math(const Face (&FB)[3], const Face (&FT)
 }  // namespace k2
 
 // One tile (block B.b of B.n); ku2_kernel runs one tile per CTA, the batched
-// persistent kernel one tile per work item.
-template <int W, int MODE>
+// persistent kernel one tile per work item.  UNPRED: node loads are not
+// predicated on the grid bounds.  A lane then reads, for nodes outside the grid,
+// whatever finite values lie there (padding, a neighbouring row or plane, or the
+// ku2_slack() zero slack around the vectors); those values only enter elements
+// outside the grid, whose scale is 0, so the result is bitwise the same as with
+// zeros.  The vectors must be finite and allocated with ku2_slack() entries
+// (kernels.cuh) on both sides.
+template <int W, int MODE, bool UNPRED = false>
 __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     using namespace k2;
     constexpr int TY = 2 * W - 1;
@@ -206,12 +212,17 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
         bool ok[3];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
-            ok[rr] = rowok[rr] && iz >= 0 && iz <= L.nz;
-            n[rr] = ok[rr] ? iz * sxy + rowoff[rr] : 0;
+            if constexpr (UNPRED) {
+                ok[rr] = rowok[rr];  // stores happen only for iz in [z0, z1), inside the grid
+                n[rr] = iz * sxy + rowoff[rr];
+            } else {
+                ok[rr] = rowok[rr] && iz >= 0 && iz <= L.nz;
+                n[rr] = ok[rr] ? iz * sxy + rowoff[rr] : 0;
+            }
             d[rr] = 0.f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) rv[rr][c] = pv[rr][c] = 0.f;
-            if (ok[rr]) {
+            if (UNPRED || ok[rr]) {
                 if (MODE == KU_PCG) {
                     d[rr] = __ldg(gd + n[rr]);
 #pragma unroll
@@ -310,12 +321,14 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
                     for (int c = 0; c < 3; ++c) A.y[n + c * cs] = V[rr][c];
                 } else {
                     const unsigned m = mrow[rr];
+                    float ds = 0.f;  // FP32 over a node's three DOFs, double-float across layers
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         const float q = ((m >> c) & 1u) ? 0.f : V[rr][c];
                         A.y[n + c * cs] = q;
-                        dot.add_prod(pcur[rr][c], q);
+                        ds = fmaf(pcur[rr][c], q, ds);
                     }
+                    dot.add(ds);
                 }
             }
         }
@@ -350,9 +363,9 @@ __device__ __forceinline__ void ku2_body(const Ku2Args &A, const Blk B) {
     }
 }
 
-template <int W, int MODE>
+template <int W, int MODE, bool UNPRED>
 __global__ void __launch_bounds__(32 * W, 2) ku2_kernel(Ku2Args A) {
-    ku2_body<W, MODE>(A, grid_blk());
+    ku2_body<W, MODE, UNPRED>(A, grid_blk());
 }
 
 }  // namespace amk

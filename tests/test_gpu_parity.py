@@ -136,6 +136,25 @@ def test_solve_cfg1_simp_density(precision):
     assert abs(F @ u - F @ ref) / abs(F @ ref) <= 1e-6
 
 
+@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 3, 3), (2, 3, 5), (7, 5, 4), (31, 8, 17), (29, 14, 6)])
+def test_mixed_solve_shapes(shape):
+    """Mixed-precision solves on grids whose K*u tiles overhang the grid on every
+    side (the FP32 PCG kernel reads the overhang without bounds predicates), with
+    and without a padding column (nx + 1 a multiple of 4 or not)."""
+    rng = np.random.default_rng(sum(shape))
+    rho = rng.uniform(0.05, 1.0, size=shape)
+    F, fixed = _cantilever(shape)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, E_min=1e-9, rho_min=0.0, precision=nat.PREC_MIXED, cg_tol=1e-8,
+                             warm_start=0)
+    u, st = p.solve(cfg, rho)
+    s = O.scales(0, rho.ravel(), None, 3.0, 1e-9, 0.0, 1.0)
+    ref, _, _ = O.pcg(shape, O.ke(), s, fixed, F, tol=1e-13)
+    assert st.converged and st.residual <= 1e-8
+    assert np.abs(u - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
 def test_sensitivities(golden):
     shape = tuple(golden["oc_py_shape"])
     grid = golden["oc_py_grid"]
