@@ -63,9 +63,11 @@ struct Scalars {
     // batched runs: |F|^2 on the free DOFs, and 1 once the problem's SIMP loop ended
     double b2;
     int frozen, pad3;
+    // set by a kernel whose bounded wait on its bulk copies ran out (ST_TIMEOUT)
+    int kerr, pad4;
 };
 
-enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4, ST_UPDATE = 5 };
+enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4, ST_UPDATE = 5, ST_TIMEOUT = 6 };
 
 // Double-float accumulator: an unevaluated sum hi + lo of two floats.  Products of
 // FP32 operands are added exactly (FMA error term) and the running sum keeps ~48

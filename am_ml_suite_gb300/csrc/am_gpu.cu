@@ -128,7 +128,9 @@ struct am_problem {
     // vectors
     DevBuf<double> r64, xw64, p64a, p64b, q64v, vstage;
     DevBuf<float> x32, r32, p32a, p32b, q32v;
-    DevBuf<double> xi64;  // FP64 iterate of the FP32 inner PCG (the flexible CG's z)
+    DevBuf<double> xi64;  // FP64 result z of an FP32 inner PCG (for the flexible CG)
+    // the inner PCG's iterate during the solve: the double-float pair x32 + xl32
+    DevBuf<float> xl32;
     DevBuf<double> partial;
     Scalars *S = nullptr;    // device
     Scalars *Sh = nullptr;   // pinned host mirror
@@ -175,6 +177,7 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
         CK(P->q64v.alloc(nv));
     } else {
         CK(P->x32.alloc(nv));
+        CK(P->xl32.alloc(nv));
         CK(P->xi64.alloc(nv));
         CK(P->r32.alloc(nv, slack));
         CK(P->p32a.alloc(nv, slack));
@@ -261,12 +264,12 @@ template <typename T>
 am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
     cudaGraph_t g = nullptr;
     const KuLaunch &K = std::is_same<T, float>::value ? P->plan32 : P->plan64;
-    double *x;
+    double *x = nullptr;
     T *r, *pa, *pb, *q;
     const T *dinv, *s;
     Modal<T> M;
     if constexpr (std::is_same<T, float>::value) {
-        x = P->xi64.p; r = P->r32.p; pa = P->p32a.p; pb = P->p32b.p; q = P->q32v.p;
+        r = P->r32.p; pa = P->p32a.p; pb = P->p32b.p; q = P->q32v.p;
         dinv = P->dinv32.p; s = P->s32.p; M = P->M32;
     } else {
         x = P->xw64.p; r = P->r64.p; pa = P->p64a.p; pb = P->p64b.p; q = P->q64v.p;
@@ -277,7 +280,11 @@ am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
     for (int k = 0; k < P->chunk; ++k) {
         // the p ping-pong member is chosen on the device from the parity of S->it
         cudaError_t e1 = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
-        cudaError_t e2 = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
+        cudaError_t e2;
+        if constexpr (std::is_same<T, float>::value)
+            e2 = pcg_update_df(P->L, P->x32.p, P->xl32.p, r, pa, pb, q, dinv, P->partial.p, P->S, P->st);
+        else
+            e2 = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
         if (e1 != cudaSuccess || e2 != cudaSuccess) {
             cudaStreamEndCapture(P->st, &g);
             if (g) cudaGraphDestroy(g);
@@ -311,6 +318,19 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
     }
     *its = P->Sh->it;
     *status = P->Sh->status;
+    if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_CUDA, "a bulk-copy wait of the PCG update timed out");
+    return AM_OK;
+}
+
+// The FP32 inner PCG iterates on the double-float pair (x32, xl32); these move
+// it to and from the FP64 vector xi64 that the flexible CG uses.
+am_status inner_iterate_zero(am_problem *P) {
+    CK(cudaMemsetAsync(P->x32.p, 0, sizeof(float) * 3 * P->L.cs, P->st));
+    CK(cudaMemsetAsync(P->xl32.p, 0, sizeof(float) * 3 * P->L.cs, P->st));
+    return AM_OK;
+}
+am_status inner_iterate_to_fp64(am_problem *P) {
+    CK(df_compose(P->x32.p, P->xl32.p, P->xi64.p, 3 * P->L.cs, P->nblocks_vec, P->st));
     return AM_OK;
 }
 
@@ -392,7 +412,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_op, P->st};
                 CKS(precond_apply(P->pre, view, P->r64.p, P->xi64.p));
                 if (!(c.inner_tol >= 1.0)) {  // inner_tol >= 1: the network alone
-                    CK(to_float(P->xi64.p, P->x32.p, 3 * P->L.cs, P->nblocks_vec, P->st));
+                    CK(df_split(P->xi64.p, P->x32.p, P->xl32.p, 3 * P->L.cs, P->nblocks_vec, P->st));
                     CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->x32.p, P->q32v.p, P->st));
                     CK(inner_resid(P->L, P->r64.p, P->q32v.p, P->mask.p, P->r32.p, P->nblocks_vec, P->st));
                     const double tgt = std::max(inner_red * rel, 0.3 * tol);
@@ -405,12 +425,14 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                         nan = true;
                         break;
                     }
+                    CKS(inner_iterate_to_fp64(P));
                     total += its;
                 }
             } else {
                 // z = M(r): FP32 PCG (FP64 iterate) on K z = r from zero, to
                 // inner_tol of |r| but not below 0.3 tol |f| (the overall goal)
-                CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->xi64.p, P->S, P->nblocks_vec, P->st));
+                CK(dc_inner_init(P->L, P->r64.p, P->r32.p, nullptr, P->S, P->nblocks_vec, P->st));
+                CKS(inner_iterate_zero(P));
                 const double tgt = std::max(inner_red * rel, 0.3 * tol);
                 CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, tgt * tgt * bnorm2, 0.0,
                                     std::min(inner_cap, maxit - total), 0, P->partial.p, P->S, P->nblocks_vec,
@@ -421,6 +443,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                     nan = true;
                     break;
                 }
+                CKS(inner_iterate_to_fp64(P));
                 total += its;
             }
             // outer step
@@ -1062,8 +1085,8 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                             P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
                 break;
             case 2:
-                CK(pcg_update<float>(P->L, P->xi64.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p, P->dinv32.p,
-                                     P->partial.p, P->S, P->nblocks_vec, P->st));
+                CK(pcg_update_df(P->L, P->x32.p, P->xl32.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p,
+                                 P->dinv32.p, P->partial.p, P->S, P->st));
                 break;
             case 3:
                 CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->q32v.p, P->st));
@@ -1116,7 +1139,8 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
     CK(cudaMemsetAsync(P->xw64.p, 0, sizeof(double) * 3 * P->L.cs, P->st));
     CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p, nullptr,
                 P->partial.p, P->S, P->st));
-    CK(dc_inner_init(P->L, P->r64.p, P->r32.p, P->xi64.p, P->S, P->nblocks_vec, P->st));
+    CK(dc_inner_init(P->L, P->r64.p, P->r32.p, nullptr, P->S, P->nblocks_vec, P->st));
+    CKS(inner_iterate_zero(P));
     const PrecondView view{P->L, P->dinv32.p, P->mask.p, P->rho_f.p, P->st};
     int did = -1;
     CKS(precond_add_density(m, view, P->M32, P->s32.p, &did));
@@ -1141,6 +1165,7 @@ am_status am_precond_harvest(am_precond *m, am_problem *P, const am_simp_config 
             if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the harvesting PCG");
         }
         CK(cudaMemcpyAsync(snap.p + nv * i, P->r32.p, nv * sizeof(float), cudaMemcpyDeviceToDevice, P->st));
+        CKS(inner_iterate_to_fp64(P));
         CK(cudaMemcpyAsync(snapx.p + nv * i, P->xi64.p, nv * sizeof(double), cudaMemcpyDeviceToDevice, P->st));
     }
     // u*: FP64-accepted solve to 1e-10 from zero

@@ -6,6 +6,7 @@
 #include "batch.cuh"
 #include "kernels.cuh"
 #include "ku.cuh"
+#include "bulk.cuh"
 #include "ku2.cuh"
 
 namespace amk {
@@ -81,6 +82,7 @@ static cudaError_t set_ku_attr() {
 }
 
 cudaError_t filter_init_attributes();
+cudaError_t update_init_attributes();
 
 cudaError_t ku_init_attributes() {
     cudaError_t e;
@@ -99,6 +101,7 @@ cudaError_t ku_init_attributes() {
     AMK_ATTR(double, 32, 4, KU_DOT)
     AMK_ATTR(double, 32, 8, KU_DOT)
 #undef AMK_ATTR
+    if ((e = update_init_attributes()) != cudaSuccess) return e;
     return filter_init_attributes();
 }
 
@@ -244,6 +247,32 @@ template cudaError_t ku_pcg<double>(const KuLaunch &, const Layout &, const Moda
 // ============================================================================
 constexpr int VEC_THREADS = 256;
 
+// Last block of a PCG update: the iteration's r.r and r.z -> beta and the stop tests.
+__device__ __forceinline__ void pcg_update_finish(Scalars *S, double rr, double rz) {
+    S->it += 1;
+    S->rr = rr;
+    S->rz_prev = S->rz;
+    S->beta = (S->rz != 0.0) ? rz / S->rz : 0.0;
+    S->rz = rz;
+    if (S->kerr) {
+        S->status = ST_TIMEOUT;
+        S->done = 1;
+    } else if (!isfinite(rr) || !isfinite(rz)) {
+        S->status = ST_NAN;
+        S->done = 1;
+    } else if (rr < S->thr) {
+        S->status = ST_CONVERGED;
+        S->done = 1;
+    } else if (rr < S->thr_update) {
+        S->status = ST_UPDATE;
+        S->done = 1;
+    } else if (S->it >= S->maxit) {
+        S->status = ST_MAXIT;
+        S->done = 1;
+    }
+    S->cnt_upd = 0;
+}
+
 // x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer the K*u
 // kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
 template <typename T>
@@ -329,28 +358,7 @@ __device__ __forceinline__ void pcg_update_body(Layout L, double *__restrict__ x
     if (!arrive_last_n(&S->cnt_upd, &last_flag, B.n)) return;
     double tot[2];
     reduce_partials<2>(partial, B.n, 2, tot, red);
-    if (threadIdx.x == 0) {
-        const double rr = tot[0], rz = tot[1];
-        S->it += 1;
-        S->rr = rr;
-        S->rz_prev = S->rz;
-        S->beta = (S->rz != 0.0) ? rz / S->rz : 0.0;
-        S->rz = rz;
-        if (!isfinite(rr) || !isfinite(rz)) {
-            S->status = ST_NAN;
-            S->done = 1;
-        } else if (rr < S->thr) {
-            S->status = ST_CONVERGED;
-            S->done = 1;
-        } else if (rr < S->thr_update) {
-            S->status = ST_UPDATE;
-            S->done = 1;
-        } else if (S->it >= S->maxit) {
-            S->status = ST_MAXIT;
-            S->done = 1;
-        }
-        S->cnt_upd = 0;
-    }
+    if (threadIdx.x == 0) pcg_update_finish(S, tot[0], tot[1]);
 }
 template <typename T>
 __global__ void __launch_bounds__(VEC_THREADS)
@@ -370,6 +378,191 @@ template cudaError_t pcg_update<float>(const Layout &, double *, float *, const 
                                        const float *, const float *, double *, Scalars *, int, cudaStream_t);
 template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *, const double *,
                                         const double *, const double *, double *, Scalars *, int, cudaStream_t);
+
+// ---- FP32 PCG update with a double-float iterate, staged by bulk copies ------
+// The iterate is the unevaluated sum xh + xl of two FP32 vectors (~48 bits, the
+// same 8 bytes per DOF as FP64).  x += alpha p is an exact product (the FMA
+// error term) and a TwoSum (Knuth) on the FP32 pipes, because GB300's FP64 pipe
+// (2 DFMA per clock and SM) would take ~19 us per launch for the FMAs and the
+// FP32 -> FP64 conversions of a 5.4M-DOF grid.  (Adding the rounded product
+// instead cost 10 % more inner iterations on the 192x96x96 bracket.)
+// The six streams (xh, xl, r, p, q and the node's D^-1) are read in chunks of
+// UPD_K DOFs by bulk asynchronous copies into shared memory, UPD_ST chunks in
+// flight per CTA, so a CTA keeps ~100 KB of reads in flight without registers.
+constexpr int UPD_K = 2048;  // DOFs per chunk (a multiple of 64, as cs is)
+constexpr int UPD_ST = 2;    // chunks in flight per CTA
+constexpr int UPD_SMEM = UPD_ST * 24 * UPD_K;
+
+// (hi, lo) += a * b, the product added exactly (its FMA rounding error joins lo)
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float a, float b) {
+    const float pr = a * b;
+    const float pe = fmaf(a, b, -pr);
+    const float s = hi + pr;
+    const float v = s - hi;
+    const float e = (hi - (s - v)) + (pr - v);
+    const float l = lo + (e + pe);
+    hi = s + l;
+    lo = l - (hi - s);
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_update_df_kernel(Layout L, float *__restrict__ xh, float *__restrict__ xl, float *__restrict__ r,
+                         const float *pa, const float *pb, const float *__restrict__ q,
+                         const float *__restrict__ dinv, double *partial, Scalars *S) {
+    extern __shared__ __align__(128) unsigned char upd_smem[];
+    __shared__ uint64_t bar[UPD_ST];
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag, fail;
+    if (S->done) return;
+    const float alpha = (float)S->alpha;
+    const float *__restrict__ p = (S->it & 1) ? pa : pb;
+    const long long cs = L.cs;
+    const int nck = (int)((cs + UPD_K - 1) / UPD_K);
+    const int nchunks = 3 * nck;
+    // stage s: xh, xl, r, p, q, dinv planes of UPD_K floats
+    auto plane = [&](int s, int a) {
+        return reinterpret_cast<float *>(upd_smem + (size_t)s * 24 * UPD_K + (size_t)4 * UPD_K * a);
+    };
+    auto chunk = [&](int g, long long &o, long long &j0, int &len) {
+        const int c = g / nck;
+        j0 = (long long)(g - c * nck) * UPD_K;
+        len = (int)min((long long)UPD_K, cs - j0);
+        o = c * cs + j0;
+    };
+    auto issue = [&](int g, int s) {
+        long long o, j0;
+        int len;
+        chunk(g, o, j0, len);
+        const unsigned b = 4u * (unsigned)len;
+        bulk::bar_expect(&bar[s], 6u * b);
+        bulk::copy_g2s(plane(s, 0), xh + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 1), xl + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 2), r + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 3), p + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 4), q + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 5), dinv + j0, b, &bar[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < UPD_ST; ++s) bulk::bar_init(&bar[s], 1);
+        bulk::bar_init_fence();
+        fail = 0;
+    }
+    __syncthreads();
+    // this CTA's chunks: blockIdx.x + i * gridDim.x, i < mine
+    const int mine = max(0, (nchunks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < UPD_ST && i < mine; ++i) issue(blockIdx.x + i * gridDim.x, i);
+    Acc<float> a0, a1;
+    int i = 0;
+    for (; i < mine; ++i) {
+        const int s = i % UPD_ST;
+        if (!bulk::bar_wait(&bar[s], (unsigned)(i / UPD_ST) & 1u)) fail = 1;
+        __syncthreads();
+        if (fail) break;
+        long long o, j0;
+        int len;
+        chunk(blockIdx.x + i * gridDim.x, o, j0, len);
+        const float4 *hs = reinterpret_cast<const float4 *>(plane(s, 0));
+        const float4 *ls = reinterpret_cast<const float4 *>(plane(s, 1));
+        const float4 *rs = reinterpret_cast<const float4 *>(plane(s, 2));
+        const float4 *ps = reinterpret_cast<const float4 *>(plane(s, 3));
+        const float4 *qs = reinterpret_cast<const float4 *>(plane(s, 4));
+        const float4 *ds = reinterpret_cast<const float4 *>(plane(s, 5));
+        for (int t = threadIdx.x; t < len / 4; t += VEC_THREADS) {
+            float4 h = hs[t], l = ls[t], rv = rs[t];
+            const float4 pv = ps[t], qv = qs[t], d = ds[t];
+            two_sum_acc(h.x, l.x, alpha, pv.x);
+            two_sum_acc(h.y, l.y, alpha, pv.y);
+            two_sum_acc(h.z, l.z, alpha, pv.z);
+            two_sum_acc(h.w, l.w, alpha, pv.w);
+            rv.x = fmaf(-alpha, qv.x, rv.x);
+            rv.y = fmaf(-alpha, qv.y, rv.y);
+            rv.z = fmaf(-alpha, qv.z, rv.z);
+            rv.w = fmaf(-alpha, qv.w, rv.w);
+            reinterpret_cast<float4 *>(xh + o)[t] = h;
+            reinterpret_cast<float4 *>(xl + o)[t] = l;
+            reinterpret_cast<float4 *>(r + o)[t] = rv;
+            a0.add_prod(rv.x, rv.x);
+            a0.add_prod(rv.y, rv.y);
+            a0.add_prod(rv.z, rv.z);
+            a0.add_prod(rv.w, rv.w);
+            a1.add_prod(rv.x, d.x * rv.x);
+            a1.add_prod(rv.y, d.y * rv.y);
+            a1.add_prod(rv.z, d.z * rv.z);
+            a1.add_prod(rv.w, d.w * rv.w);
+        }
+        __syncthreads();  // stage s read by every thread
+        if (threadIdx.x == 0 && i + UPD_ST < mine) {
+            bulk::proxy_fence();
+            issue(blockIdx.x + (i + UPD_ST) * gridDim.x, s);
+        }
+    }
+    if (fail) {
+        // a copy did not complete within its wait: drain this CTA's outstanding
+        // copies (bounded), flag the launch, and still take part in the reduction
+        if (threadIdx.x == 0) {
+            for (int j = i; j < mine && j < i + UPD_ST; ++j)
+                bulk::bar_wait(&bar[j % UPD_ST], (unsigned)(j / UPD_ST) & 1u);
+            atomicExch(&S->kerr, 1);
+        }
+    }
+    double v[2] = {a0.value(), a1.value()};
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = v[0];
+        partial[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!arrive_last_n(&S->cnt_upd, &last_flag, gridDim.x)) return;
+    double tot[2];
+    reduce_partials<2>(partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) pcg_update_finish(S, tot[0], tot[1]);
+}
+
+static int g_upd_grid = 0;
+
+cudaError_t pcg_update_df(const Layout &L, float *xh, float *xl, float *r, const float *pa, const float *pb,
+                          const float *q, const float *dinv, double *partial, Scalars *S, cudaStream_t st) {
+    if (g_upd_grid <= 0) return cudaErrorInitializationError;
+    pcg_update_df_kernel<<<g_upd_grid, VEC_THREADS, UPD_SMEM, st>>>(L, xh, xl, r, pa, pb, q, dinv, partial, S);
+    return counted(cudaGetLastError());
+}
+int pcg_update_df_grid() { return g_upd_grid; }
+
+// two CTAs of UPD_SMEM bytes per SM, one wave
+cudaError_t update_init_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(pcg_update_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    g_upd_grid = 2 * std::max(sms, 1);
+    return cudaSuccess;
+}
+
+// x64 = xh + xl (exact), and the split x64 -> (xh, xl) with xh = (float)x64
+__global__ void df_compose_kernel(const float *__restrict__ xh, const float *__restrict__ xl,
+                                  double *__restrict__ x, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        x[i] = (double)xh[i] + (double)xl[i];
+}
+__global__ void df_split_kernel(const double *__restrict__ x, float *__restrict__ xh, float *__restrict__ xl,
+                                long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float h = (float)x[i];
+        xh[i] = h;
+        xl[i] = (float)(x[i] - (double)h);
+    }
+}
+cudaError_t df_compose(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st) {
+    df_compose_kernel<<<nblocks, 256, 0, st>>>(xh, xl, x, n);
+    return counted(cudaGetLastError());
+}
+cudaError_t df_split(const double *x, float *xh, float *xl, long long n, int nblocks, cudaStream_t st) {
+    df_split_kernel<<<nblocks, 256, 0, st>>>(x, xh, xl, n);
+    return counted(cudaGetLastError());
+}
 
 // (Re)start of the PCG sequence from the residual in r: r.r, r.z -> S.
 // restart == 0: fresh sequence (beta = 0, it = 0).  restart == 1: the residual

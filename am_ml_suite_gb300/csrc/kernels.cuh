@@ -55,6 +55,16 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
 template <typename T>
 cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st);
+// The same update with the iterate held as a double-float pair xh + xl (FP32
+// vectors), the streams staged by bulk copies; one wave of 2 CTAs per SM (after
+// ku_init_attributes).  A bulk-copy wait that runs out ends the solve with
+// status ST_TIMEOUT.
+cudaError_t pcg_update_df(const Layout &L, float *xh, float *xl, float *r, const float *pa, const float *pb,
+                          const float *q, const float *dinv, double *partial, Scalars *S, cudaStream_t st);
+int pcg_update_df_grid();
+// x = xh + xl, and (xh, xl) = the double-float split of x (n entries)
+cudaError_t df_compose(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st);
+cudaError_t df_split(const double *x, float *xh, float *xl, long long n, int nblocks, cudaStream_t st);
 // (re)start from the residual r (already masked); see pcg_start_kernel
 template <typename T>
 cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,
