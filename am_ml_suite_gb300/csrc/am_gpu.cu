@@ -1072,7 +1072,13 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
     CK(cudaEventCreate(&e1));
     double tot = 0.0, mn = 1e30;
     for (int k = 0; k < reps; ++k) {
-        if (flush_l2) CK(cudaMemsetAsync(flush.p, k & 0xff, flush_bytes, P->st));
+        if (flush_l2) {
+            // write a 512 MB buffer (evicts the problem's data from the 129 MB L2),
+            // then read it back so the lines the write left dirty are written back
+            // before the timed launch rather than during it
+            CK(cudaMemsetAsync(flush.p, k & 0xff, flush_bytes, P->st));
+            CK(l2_flush_read(flush.p, flush_bytes, P->st));
+        }
         CK(cudaMemcpyAsync(&P->S->done, &run.done, sizeof(int), cudaMemcpyHostToDevice, P->st));
         CK(cudaEventRecord(e0, P->st));
         switch (which) {

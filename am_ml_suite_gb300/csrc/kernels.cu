@@ -539,6 +539,23 @@ cudaError_t update_init_attributes() {
     return cudaSuccess;
 }
 
+// reads n bytes (a multiple of 16) through L2; the sum is kept only to keep the loads
+__global__ void l2_flush_read_kernel(const uint4 *__restrict__ a, long long n16, unsigned *sink) {
+    unsigned acc = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n16;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint4 v = __ldcg(a + i);
+        acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+    if (acc == 0x9e3779b9u) *sink = acc;
+}
+cudaError_t l2_flush_read(const void *buf, size_t bytes, cudaStream_t st) {
+    // the sink is the buffer's first word: written only on an (irrelevant) hash match
+    l2_flush_read_kernel<<<1216, 256, 0, st>>>(reinterpret_cast<const uint4 *>(buf), (long long)(bytes / 16),
+                                               reinterpret_cast<unsigned *>(const_cast<void *>(buf)));
+    return counted(cudaGetLastError());
+}
+
 // x64 = xh + xl (exact), and the split x64 -> (xh, xl) with xh = (float)x64
 __global__ void df_compose_kernel(const float *__restrict__ xh, const float *__restrict__ xl,
                                   double *__restrict__ x, long long n) {

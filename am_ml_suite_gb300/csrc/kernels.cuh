@@ -62,6 +62,9 @@ cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *p
 cudaError_t pcg_update_df(const Layout &L, float *xh, float *xl, float *r, const float *pa, const float *pb,
                           const float *q, const float *dinv, double *partial, Scalars *S, cudaStream_t st);
 int pcg_update_df_grid();
+// reads `bytes` (a multiple of 16) of buf through L2 (measurement: cleans the
+// L2 lines a flush write left dirty)
+cudaError_t l2_flush_read(const void *buf, size_t bytes, cudaStream_t st);
 // x = xh + xl, and (xh, xl) = the double-float split of x (n entries)
 cudaError_t df_compose(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st);
 cudaError_t df_split(const double *x, float *xh, float *xl, long long n, int nblocks, cudaStream_t st);

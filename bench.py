@@ -534,7 +534,10 @@ def main():
     achieved = alg_bytes / (ku_ms * 1e-3) / 1e9
     traffic = ku_traffic_per_launch(W, nodes, nel)
     res_ms, _ = p.bench_kernel(1, reps=5, flush_l2=True)
-    upd_ms, _ = p.bench_kernel(2, reps=20, flush_l2=True)
+    upd_ms, upd_min = p.bench_kernel(2, reps=20, flush_l2=True)
+    # the other half of a PCG iteration: reads the double-float iterate (8 B per
+    # DOF), r, p, q (4 B each) and dinv (4 B per node); writes the iterate and r
+    upd_bytes = 100 * nodes
     p.close()
 
     # ---- end to end through the C ABI from host buffers ---------------------
@@ -592,6 +595,10 @@ def main():
                          "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
                          "avg_ms": ku_ms, "min_ms": ku_min},
             "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_fp64": res_ms, "pcg_update_fp32": upd_ms},
+            "roofline_update": {"bound": "hbm", "kernel": "pcg_update_df_kernel (double-float iterate, bulk-copy staged)",
+                                "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                                "frac": upd_bytes / (upd_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": upd_bytes,
+                                "avg_ms": upd_ms, "min_ms": upd_min},
             "gpu_launches": int(l1 - l0),
             "clocks": clk.summary(),
             "e2e": e2e,

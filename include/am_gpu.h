@@ -225,7 +225,8 @@ long long am_launch_count(void);
  * the first step, on the initial density with zero vectors): which = 0 the
  * fused FP32 PCG K*u, 1 the FP64 residual K*u, 2 the FP32 PCG vector update,
  * 3 the plain FP32 K*u.  flush_l2 != 0 overwrites a 512 MB buffer before each
- * launch so the kernel reads from HBM.  Solver state is restored afterwards. */
+ * launch so the kernel reads from HBM, then reads that buffer back so the write's
+ * dirty L2 lines are written back before the timed launch.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
 
 /* The CUDA stream (cudaStream_t) on which every kernel of the problem runs, for
