@@ -178,6 +178,19 @@ __device__ __forceinline__ bool arrive_last_n(unsigned int *counter, int *flag_s
 __device__ __forceinline__ bool arrive_last(unsigned int *counter, int *flag_smem) {
     return arrive_last_n(counter, flag_smem, (int)gridDim.x);
 }
+// The same hand-off for a block that arrives for `weight` of the `total` work
+// items at once (it published their partials together).
+__device__ __forceinline__ bool arrive_last_weighted(unsigned int *counter, int *flag_smem, int weight, int total) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int t = atomicAdd(counter, (unsigned int)weight);
+        *flag_smem = (t + (unsigned int)weight == (unsigned int)total) ? 1 : 0;
+    }
+    __syncthreads();
+    if (*flag_smem) __threadfence();
+    return *flag_smem != 0;
+}
 
 // Sum partial[b*stride + k] over b in [0, nb) in a fixed order, for k < NV.
 // Called by all threads of one block; result valid in thread 0.

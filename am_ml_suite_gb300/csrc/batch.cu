@@ -89,7 +89,7 @@ struct am_batch {
     Pool<float> s32;
     Pool<uint8_t> design;
     Pool<double> F, x64, r64, dinv64;
-    Pool<float> r32, pa, pb, q32, dinv32;
+    Pool<float> r32, pa, pb, q32, dinv32, xh, xl;
     Pool<uint8_t> mask, fixed_bits;
     Pool<long long> f_idx;
     Pool<double> f_val;
@@ -101,8 +101,8 @@ struct am_batch {
     Pool<BatchItem> items_d;
     std::vector<BatchItem> items;
     // work lists
-    Pool<int2> w_elem, w_vec, w_k2, w_k64, w_prob;
-    WorkList elem{}, vec{}, k2{}, k64{}, prob{};
+    Pool<int2> w_elem, w_vec, w_k2, w_k64, w_prob, w_chunk;
+    WorkList elem{}, vec{}, k2{}, k64{}, prob{}, chunk{};
     // FP32 K*u plan (autotuner): warps per CTA, z chunk (0 = all planes), CTAs per SM
     int warps = 8, zchunk = 0, ctas = 2;
     bool loads_set = false;
@@ -176,7 +176,7 @@ am_status build_graph(am_batch *B) {
     BCK(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
-        e = batch_pcg_iteration(B->items_d.p, B->k2, B->vec, B->C, B->warps, kSms * B->ctas, kSms * 8, B->st);
+        e = batch_pcg_iteration(B->items_d.p, B->k2, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
     cudaError_t e2 = cudaStreamEndCapture(B->st, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -214,10 +214,13 @@ am_status batch_solve(am_batch *B, int max_chunks) {
             if (all_done(B)) break;
             if (chunks > max_chunks) return bfail(AM_ERR_TIMEOUT, "batched PCG did not stop within its cap");
         }
+        BCK(batch_inner_end(B->items_d.p, B->vec, kSms * 8, B->st));
         for (int p = 0; p < B->n; ++p) {
             if (B->Sh[p].frozen) continue;
             if (B->Sh[p].status == ST_NAN)
                 return bfail(AM_ERR_NAN_DETECTED, "NaN in the PCG of batch problem " + std::to_string(p));
+            if (B->Sh[p].status == ST_TIMEOUT)
+                return bfail(AM_ERR_CUDA, "a bulk-copy wait of the batched PCG update timed out");
             B->pcg_its[p] += B->Sh[p].it;
         }
     }
@@ -242,9 +245,9 @@ am_status am_batch_destroy(am_batch *B) {
     for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi,
                     &B->F, &B->x64, &B->r64, &B->dinv64, &B->f_val, &B->tap_w, &B->partial})
         q->release();
-    for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32}) q->release();
+    for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32, &B->xh, &B->xl}) q->release();
     for (auto *q : {&B->design, &B->mask, &B->fixed_bits}) q->release();
-    for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k64, &B->w_prob}) q->release();
+    for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k64, &B->w_prob, &B->w_chunk}) q->release();
     B->f_idx.release();
     B->tap_d.release();
     B->S.release();
@@ -306,8 +309,9 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         // partials: 2 per K*u tile (either plan: at most 15x more tiles than 4-warp
         // ku2 tiles of 1 plane), 3 per element block, 2 per vector block
         const size_t k2max = (size_t)div_up_i(L.nx + 1, 30) * div_up_i(L.ny + 1, 7) * (L.nz + 1);
+        const size_t nchunk = 3 * (size_t)div_up_i(L.cs, BATCH_UPD_CHUNK);
         pp += align_up(std::max({2 * k2max, 2 * (size_t)it.n_k64, 3 * (size_t)it.n_elem, 2 * (size_t)it.n_vec,
-                                 (size_t)16}),
+                                 2 * nchunk, (size_t)16}),
                        32);
     }
     B->eoff[n] = e;
@@ -324,7 +328,7 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     A(B->design, e);
     for (auto *q : {&B->F, &B->x64, &B->r64}) A(*q, 3 * nn);
     A(B->dinv64, nn);
-    for (auto *q : {&B->r32, &B->pa, &B->pb, &B->q32}) A(*q, 3 * nn);
+    for (auto *q : {&B->r32, &B->pa, &B->pb, &B->q32, &B->xh, &B->xl}) A(*q, 3 * nn);
     A(B->dinv32, nn);
     A(B->mask, nn);
     A(B->fixed_bits, nn);
@@ -337,7 +341,7 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         return bfail(ce == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,
                      std::string("batch create: ") + cudaGetErrorString(ce));
     }
-    std::vector<int2> we, wv, w64, wp;
+    std::vector<int2> we, wv, w64, wp, wc;
     for (int p = 0; p < n; ++p) {
         BatchItem &it = B->items[p];
         const size_t eo = B->eoff[p], no = B->noff[p];
@@ -360,6 +364,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         it.pa = B->pa.p + 3 * no;
         it.pb = B->pb.p + 3 * no;
         it.q32 = B->q32.p + 3 * no;
+        it.xh = B->xh.p + 3 * no;
+        it.xl = B->xl.p + 3 * no;
         it.dinv32 = B->dinv32.p + no;
         it.mask = B->mask.p + no;
         it.fixed_bits = B->fixed_bits.p + no;
@@ -367,6 +373,7 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         it.S = B->S.p + p;
         for (int b = 0; b < it.n_elem; ++b) we.push_back(make_int2(p, b));
         for (int b = 0; b < it.n_vec; ++b) wv.push_back(make_int2(p, b));
+        for (int b = 0; b < 3 * div_up_i(it.L.cs, BATCH_UPD_CHUNK); ++b) wc.push_back(make_int2(p, b));
         for (int b = 0; b < it.n_k64; ++b) w64.push_back(make_int2(p, b));
         wp.push_back(make_int2(p, 0));
     }
@@ -374,6 +381,7 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     if (s == AM_OK) s = upload_worklist(B, B->w_vec, B->vec, wv);
     if (s == AM_OK) s = upload_worklist(B, B->w_k64, B->k64, w64);
     if (s == AM_OK) s = upload_worklist(B, B->w_prob, B->prob, wp);
+    if (s == AM_OK) s = upload_worklist(B, B->w_chunk, B->chunk, wc);
     if (s == AM_OK) s = plan_k2(B, 8, 0);
     if (s == AM_OK && ku_init_attributes() != cudaSuccess) s = bfail(AM_ERR_CUDA, "kernel attributes");
     if (s != AM_OK) {

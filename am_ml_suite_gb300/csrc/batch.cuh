@@ -26,6 +26,7 @@ struct BatchItem {
     // node arrays: [3][cs] vectors, per-node inverse diagonal / mask / constraint bits
     double *F, *x64, *r64, *dinv64;
     float *r32, *pa, *pb, *q32, *dinv32;
+    float *xh, *xl;  // the FP32 PCG's iterate as a double-float pair (x64 = xh + xl)
     uint8_t *mask, *fixed_bits;
     // nonzeros of F (node-plane index) for u.F and |F|^2
     const long long *f_idx;
@@ -70,12 +71,17 @@ cudaError_t batch_prepare_solve(const BatchItem *it, WorkList vec, WorkList prob
 // r64 = mask(F - K x64) (FP64), |r|^2 -> S->res_rr; element energies when energy != 0
 cudaError_t batch_resid(const BatchItem *it, WorkList k64, const BatchConst &C, int energy, int grid,
                         cudaStream_t st);
-// r32 = r64, then the FP32 PCG start; the sequence updates the FP64 iterate x64
-// (a problem whose FP64 residual already meets tol is marked done)
+// r32 = r64 and (xh, xl) = x64, then the FP32 PCG start (a problem whose FP64
+// residual already meets tol is marked done)
 cudaError_t batch_inner_start(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
-// one FP32 PCG iteration for every active problem: fused K*p (warps = 4 or 8) + update
-cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, const BatchConst &C, int warps,
+// x64 = xh + xl after an FP32 PCG round
+cudaError_t batch_inner_end(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
+// one FP32 PCG iteration for every active problem: fused K*p (warps = 4 or 8) +
+// the bulk-copy update over `chunks` ((problem, chunk of 2048 DOFs) items)
+cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList chunks, const BatchConst &C, int warps,
                                 int grid_k2, int grid_vec, cudaStream_t st);
+// DOFs per chunk of the batched update's work items
+constexpr int BATCH_UPD_CHUNK = 2048;
 // plain FP32 K*u (y = q32, u = pa) over the batch, for the autotuner
 cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
                            cudaStream_t st);

@@ -519,6 +519,7 @@ __global__ void __launch_bounds__(VEC_THREADS)
 }
 
 static int g_upd_grid = 0;
+__global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items, WorkList W);
 
 cudaError_t pcg_update_df(const Layout &L, float *xh, float *xl, float *r, const float *pa, const float *pb,
                           const float *q, const float *dinv, double *partial, Scalars *S, cudaStream_t st) {
@@ -531,6 +532,8 @@ int pcg_update_df_grid() { return g_upd_grid; }
 // two CTAs of UPD_SMEM bytes per SM, one wave
 cudaError_t update_init_attributes() {
     cudaError_t e = cudaFuncSetAttribute(pcg_update_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(b_update_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -1639,8 +1642,16 @@ __global__ void __launch_bounds__(256) b_inner_init_kernel(const BatchItem *item
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
-        // the FP32 sequence continues the FP64 iterate x64 (no zeroing)
+        // the FP32 sequence continues the FP64 iterate x64 (no zeroing), held as the
+        // double-float pair (xh, xl) while it runs
         dc_inner_init_body(it.L, it.r64, it.r32, nullptr, it.S, Blk{_k.y, it.n_vec});
+        const long long n = 3 * it.L.cs;
+        for (long long i = _k.y * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x) {
+            const double x = it.x64[i];
+            const float h = (float)x;
+            it.xh[i] = h;
+            it.xl[i] = (float)(x - (double)h);
+        }
     }
 }
 // FP32 PCG on K x32 = r32 to |r| <= tol/2 |F| (but at most 1e-6 below its start);
@@ -1690,15 +1701,181 @@ __global__ void __launch_bounds__(32 * W_, 2) b_ku2_kernel(const BatchItem *item
         __syncthreads();
     }
 }
-__global__ void __launch_bounds__(256) b_update_kernel(const BatchItem *items, WorkList W) {
+// The batched form of pcg_update_df_kernel: work items are (problem, chunk of
+// UPD_K DOFs), listed problem by problem.  Each CTA takes a contiguous range of
+// items and runs a two-stage bulk-copy pipeline over it; the r.r / r.z partials
+// of a run of consecutive items of one problem are reduced once and published in
+// the run's first slot (zeros in the others), and the CTA arrives for the whole
+// run, so a CTA synchronises once per problem it touches rather than per chunk.
+// Items of frozen or converged problems are skipped without a copy (their state
+// cannot change during the launch: only a problem's own last run ends it).
+__global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items, WorkList W) {
+    extern __shared__ __align__(128) unsigned char upd_smem[];
+    __shared__ uint64_t bar[UPD_ST];
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag, fail;
+    auto plane = [&](int s, int a) {
+        return reinterpret_cast<float *>(upd_smem + (size_t)s * 24 * UPD_K + (size_t)4 * UPD_K * a);
+    };
+    struct Chunk {
+        long long o, j0;
+        int len, nck;
+    };
+    auto chunk = [&](const BatchItem &it, int g) {
+        Chunk c;
+        c.nck = (int)((it.L.cs + UPD_K - 1) / UPD_K);
+        const int comp = g / c.nck;
+        c.j0 = (long long)(g - comp * c.nck) * UPD_K;
+        c.len = (int)min((long long)UPD_K, it.L.cs - c.j0);
+        c.o = comp * it.L.cs + c.j0;
+        return c;
+    };
+    const int lo = (int)((long long)W.n * blockIdx.x / gridDim.x);
+    const int hi = (int)((long long)W.n * (blockIdx.x + 1) / gridDim.x);
+    auto active = [&](int i) {
+        const Scalars *S = items[W.w[i].x].S;
+        return !S->frozen && !S->done;
+    };
+    auto issue = [&](int i, int s) {
+        const int2 k = W.w[i];
+        const BatchItem &it = items[k.x];
+        const Chunk c = chunk(it, k.y);
+        const float *p = (it.S->it & 1) ? it.pa : it.pb;
+        const unsigned b = 4u * (unsigned)c.len;
+        bulk::bar_expect(&bar[s], 6u * b);
+        bulk::copy_g2s(plane(s, 0), it.xh + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 1), it.xl + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 2), it.r32 + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 3), p + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 4), it.q32 + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 5), it.dinv32 + c.j0, b, &bar[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < UPD_ST; ++s) bulk::bar_init(&bar[s], 1);
+        bulk::bar_init_fence();
+        fail = 0;
+    }
+    __syncthreads();
+    // bit s: stage s holds issued copies / the parity stage s waits for next
+    unsigned issued = 0u, phase = 0u;
+#pragma unroll
+    for (int j = 0; j < UPD_ST; ++j) {
+        if (lo + j < hi && active(lo + j)) {
+            issued |= 1u << j;
+            if (threadIdx.x == 0) issue(lo + j, j);
+        }
+    }
+    // the current run: problem, first and last chunk index, and its partial sums
+    int run_p = -1, run_first = 0, run_last = 0;
+    Acc<float> a0, a1;
+    auto flush_run = [&]() {
+        const BatchItem &it = items[run_p];
+        double v[2] = {a0.value(), a1.value()};
+        block_sum<2>(v, red);
+        if (threadIdx.x == 0) {
+            it.partial[2 * run_first] = v[0];
+            it.partial[2 * run_first + 1] = v[1];
+        }
+        for (int g = run_first + 1 + (int)threadIdx.x; g <= run_last; g += blockDim.x) {
+            it.partial[2 * g] = 0.0;
+            it.partial[2 * g + 1] = 0.0;
+        }
+        const int nb = 3 * chunk(it, 0).nck;
+        if (arrive_last_weighted(&it.S->cnt_upd, &last_flag, run_last - run_first + 1, nb)) {
+            double tot[2];
+            reduce_partials<2>(it.partial, nb, 2, tot, red);
+            if (threadIdx.x == 0) pcg_update_finish(it.S, tot[0], tot[1]);
+        }
+        a0 = Acc<float>();
+        a1 = Acc<float>();
+        run_p = -1;
+    };
+    for (int i = lo; i < hi; ++i) {
+        const int s = (i - lo) % UPD_ST;
+        if (issued & (1u << s)) {
+            if (!fail) {
+                if (!bulk::bar_wait(&bar[s], (phase >> s) & 1u)) fail = 1;
+            }
+            phase ^= 1u << s;
+            __syncthreads();
+            const int2 k = W.w[i];
+            // a new problem (or a gap in this one's chunks) closes the current run
+            if (run_p >= 0 && (run_p != k.x || k.y != run_last + 1)) flush_run();
+            if (run_p < 0) {
+                run_p = k.x;
+                run_first = k.y;
+            }
+            run_last = k.y;
+            const BatchItem &it = items[k.x];
+            const Chunk c = chunk(it, k.y);
+            const float alpha = (float)it.S->alpha;
+            if (!fail) {
+                const float4 *hs = reinterpret_cast<const float4 *>(plane(s, 0));
+                const float4 *ls = reinterpret_cast<const float4 *>(plane(s, 1));
+                const float4 *rs = reinterpret_cast<const float4 *>(plane(s, 2));
+                const float4 *ps = reinterpret_cast<const float4 *>(plane(s, 3));
+                const float4 *qs = reinterpret_cast<const float4 *>(plane(s, 4));
+                const float4 *ds = reinterpret_cast<const float4 *>(plane(s, 5));
+                for (int t = threadIdx.x; t < c.len / 4; t += VEC_THREADS) {
+                    float4 h = hs[t], l = ls[t], rv = rs[t];
+                    const float4 pv = ps[t], qv = qs[t], d = ds[t];
+                    two_sum_acc(h.x, l.x, alpha, pv.x);
+                    two_sum_acc(h.y, l.y, alpha, pv.y);
+                    two_sum_acc(h.z, l.z, alpha, pv.z);
+                    two_sum_acc(h.w, l.w, alpha, pv.w);
+                    rv.x = fmaf(-alpha, qv.x, rv.x);
+                    rv.y = fmaf(-alpha, qv.y, rv.y);
+                    rv.z = fmaf(-alpha, qv.z, rv.z);
+                    rv.w = fmaf(-alpha, qv.w, rv.w);
+                    reinterpret_cast<float4 *>(it.xh + c.o)[t] = h;
+                    reinterpret_cast<float4 *>(it.xl + c.o)[t] = l;
+                    reinterpret_cast<float4 *>(it.r32 + c.o)[t] = rv;
+                    a0.add_prod(rv.x, rv.x);
+                    a0.add_prod(rv.y, rv.y);
+                    a0.add_prod(rv.z, rv.z);
+                    a0.add_prod(rv.w, rv.w);
+                    a1.add_prod(rv.x, d.x * rv.x);
+                    a1.add_prod(rv.y, d.y * rv.y);
+                    a1.add_prod(rv.z, d.z * rv.z);
+                    a1.add_prod(rv.w, d.w * rv.w);
+                }
+            } else if (threadIdx.x == 0) {
+                atomicExch(&it.S->kerr, 1);
+            }
+            __syncthreads();  // stage s read by every thread
+            issued &= ~(1u << s);
+        }
+        // refill stage s with item i + UPD_ST (fail is uniform here: read after a barrier)
+        if (i + UPD_ST < hi && !fail && active(i + UPD_ST)) {
+            issued |= 1u << s;
+            if (threadIdx.x == 0) {
+                bulk::proxy_fence();
+                issue(i + UPD_ST, s);
+            }
+        }
+    }
+    if (run_p >= 0) flush_run();
+    if (fail && threadIdx.x == 0) {
+        // drain what this CTA issued and did not consume (bounded waits)
+        for (int s = 0; s < UPD_ST; ++s)
+            if (issued & (1u << s)) bulk::bar_wait(&bar[s], (phase >> s) & 1u);
+    }
+}
+// x64 = xh + xl for every active problem (end of an FP32 PCG round)
+__global__ void __launch_bounds__(256) b_compose_kernel(const BatchItem *items, WorkList W) {
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
-        pcg_update_body<float>(it.L, it.x64, it.r32, it.pa, it.pb, it.q32, it.dinv32, it.partial, it.S,
-                               Blk{_k.y, it.n_vec});
-        __syncthreads();
+        const long long n = 3 * it.L.cs;
+        for (long long i = _k.y * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x)
+            it.x64[i] = (double)it.xh[i] + (double)it.xl[i];
     }
 }
+cudaError_t batch_inner_end(const BatchItem *it, WorkList vec, int grid, cudaStream_t st) {
+    b_compose_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(it, vec);
+    return counted(cudaGetLastError());
+}
+static_assert(BATCH_UPD_CHUNK == UPD_K, "batched update chunk");
 cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, const BatchConst &C, int warps,
                                 int grid_k2, int grid_vec, cudaStream_t st) {
     const int g2 = std::max(1, std::min(grid_k2, k2.n));
@@ -1706,7 +1883,7 @@ cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, 
     else if (warps == 4) b_ku2_kernel<4, KU_PCG><<<g2, 128, 0, st>>>(it, k2, C.M32);
     else return cudaErrorInvalidValue;
     if (cudaError_t e = counted(cudaGetLastError())) return e;
-    b_update_kernel<<<std::max(1, std::min(grid_vec, vec.n)), 256, 0, st>>>(it, vec);
+    b_update_df_kernel<<<std::max(1, std::min(grid_vec, vec.n)), 256, UPD_SMEM, st>>>(it, vec);
     return counted(cudaGetLastError());
 }
 cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
