@@ -273,8 +273,8 @@ __device__ __forceinline__ void pcg_update_finish(Scalars *S, double rr, double 
     S->cnt_upd = 0;
 }
 
-// x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer the K*u
-// kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
+// FP64 PCG: x += alpha p; r -= alpha q; r.r and r.z partials.  p is the buffer
+// the K*u kernel of this iteration wrote: p[(it + 1) & 1] of the ping-pong pair.
 template <typename T>
 __device__ __forceinline__ void pcg_update_body(Layout L, double *__restrict__ x, T *__restrict__ r, const T *pa, const T *pb,
                       const T *__restrict__ q, const T *__restrict__ dinv, double *partial,
@@ -286,67 +286,28 @@ __device__ __forceinline__ void pcg_update_body(Layout L, double *__restrict__ x
     const T *__restrict__ p = (S->it & 1) ? pa : pb;
     const long long cs = L.cs;
     Acc<T> a0, a1;
-    if constexpr (std::is_same<T, float>::value) {
-        // FP32 r, p, q with an FP64 iterate x: the rounding of an FP32 x (eps |K||x|
-        // at this stiffness contrast) would cap the true residual near 1e-2, FP64 x
-        // keeps the FP32 sequence converging like FP64 PCG.  One component of four
-        // nodes per thread and step (cs is a multiple of 64, rows 16-byte aligned).
-        const long long n4 = cs / 4;
-        const long long units = 3 * n4;
-        for (long long u = B.b * (long long)blockDim.x + threadIdx.x; u < units;
-             u += (long long)B.n * blockDim.x) {
-            const long long k = u - ((u >= n4) + (u >= 2 * n4)) * n4;  // node group of this unit
-            const float4 d = __ldg(reinterpret_cast<const float4 *>(dinv) + k);
-            double2 x01 = reinterpret_cast<const double2 *>(x)[2 * u];
-            double2 x23 = reinterpret_cast<const double2 *>(x)[2 * u + 1];
-            float4 rv = reinterpret_cast<const float4 *>(r)[u];
-            const float4 pv = __ldg(reinterpret_cast<const float4 *>(p) + u);
-            const float4 qv = __ldg(reinterpret_cast<const float4 *>(q) + u);
-            const double ad = (double)alpha;
-            x01.x = fma(ad, (double)pv.x, x01.x);
-            x01.y = fma(ad, (double)pv.y, x01.y);
-            x23.x = fma(ad, (double)pv.z, x23.x);
-            x23.y = fma(ad, (double)pv.w, x23.y);
-            rv.x = fmaf(-alpha, qv.x, rv.x);
-            rv.y = fmaf(-alpha, qv.y, rv.y);
-            rv.z = fmaf(-alpha, qv.z, rv.z);
-            rv.w = fmaf(-alpha, qv.w, rv.w);
-            reinterpret_cast<double2 *>(x)[2 * u] = x01;
-            reinterpret_cast<double2 *>(x)[2 * u + 1] = x23;
-            reinterpret_cast<float4 *>(r)[u] = rv;
-            a0.add_prod(rv.x, rv.x);
-            a0.add_prod(rv.y, rv.y);
-            a0.add_prod(rv.z, rv.z);
-            a0.add_prod(rv.w, rv.w);
-            a1.add_prod(rv.x, d.x * rv.x);
-            a1.add_prod(rv.y, d.y * rv.y);
-            a1.add_prod(rv.z, d.z * rv.z);
-            a1.add_prod(rv.w, d.w * rv.w);
+    // one node per thread and step, its three component planes
+    for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < cs;
+         n += (long long)B.n * blockDim.x) {
+        const T d = dinv[n];
+        T xv[3], rv[3], pv[3], qv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long i = n + c * cs;
+            xv[c] = x[i];
+            rv[c] = r[i];
+            pv[c] = p[i];
+            qv[c] = q[i];
         }
-    } else {
-        // one node per thread and step, its three component planes
-        for (long long n = B.b * (long long)blockDim.x + threadIdx.x; n < cs;
-             n += (long long)B.n * blockDim.x) {
-            const T d = dinv[n];
-            T xv[3], rv[3], pv[3], qv[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const long long i = n + c * cs;
-                xv[c] = x[i];
-                rv[c] = r[i];
-                pv[c] = p[i];
-                qv[c] = q[i];
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const long long i = n + c * cs;
-                const T xi = xv[c] + alpha * pv[c];
-                const T ri = rv[c] - alpha * qv[c];
-                x[i] = xi;
-                r[i] = ri;
-                a0.add_prod(ri, ri);
-                a1.add_prod(ri, d * ri);
-            }
+        for (int c = 0; c < 3; ++c) {
+            const long long i = n + c * cs;
+            const T xi = xv[c] + alpha * pv[c];
+            const T ri = rv[c] - alpha * qv[c];
+            x[i] = xi;
+            r[i] = ri;
+            a0.add_prod(ri, ri);
+            a1.add_prod(ri, d * ri);
         }
     }
     double v[2] = {a0.value(), a1.value()};
@@ -374,8 +335,6 @@ cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *p
     pcg_update_kernel<T><<<nblocks, VEC_THREADS, 0, st>>>(L, x, r, pa, pb, q, dinv, partial, S);
     return counted(cudaGetLastError());
 }
-template cudaError_t pcg_update<float>(const Layout &, double *, float *, const float *, const float *,
-                                       const float *, const float *, double *, Scalars *, int, cudaStream_t);
 template cudaError_t pcg_update<double>(const Layout &, double *, double *, const double *, const double *,
                                         const double *, const double *, double *, Scalars *, int, cudaStream_t);
 

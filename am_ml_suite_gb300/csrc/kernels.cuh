@@ -49,9 +49,9 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
                      double *r, double *ce, double *partial, Scalars *S, cudaStream_t st);
 
 // ---- PCG vector kernels ------------------------------------------------------
-// x += alpha p; r -= alpha q (p = the pair member written this iteration; x is
-// FP64 for both precisions of r, p, q);
-// rr, rz -> S (beta, stop tests: converged / reliable update due / max it)
+// FP64 PCG: x += alpha p; r -= alpha q (p = the pair member written this
+// iteration); rr, rz -> S (beta, stop tests: converged / reliable update due /
+// max it).  Instantiated for double; the FP32 PCG uses pcg_update_df.
 template <typename T>
 cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *pb, const T *q, const T *dinv,
                        double *partial, Scalars *S, int nblocks, cudaStream_t st);
