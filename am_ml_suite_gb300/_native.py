@@ -148,6 +148,8 @@ SIGNATURES = {
     "am_problem_destroy": (ctypes.c_int, [_vp]),
     "am_problem_set_loads": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _i64p, _i64p]),
     "am_ku_apply": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, ctypes.c_int]),
+    "am_ku_pcg_step": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                      ctypes.c_int, _dp, _dp, _dp]),
     "am_solve": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _dp,
                                 ctypes.POINTER(SolveStats)]),
     "am_sensitivities": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, _dp, _dp, _dp, _dp]),
@@ -309,6 +311,22 @@ class Problem:
         check(load().am_ku_apply(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), ptr(u), ptr(y),
                                  int(precision)), "am_ku_apply")
         return y
+
+    def ku_pcg_step(self, cfg, rho, r, p_prev, beta, impl=3, load_case=0):
+        """One FP32 inner-PCG K*u step: returns (p, q, p.q) with p = D^-1 r + beta p_prev
+        and q = mask(K p) (impl 3: the staged kernel the solver runs, 2: the
+        register-direct kernel it replaced)."""
+        r = f64(r).ravel()
+        pp = f64(p_prev).ravel()
+        if r.size != self.N or pp.size != self.N:
+            raise ValueError("vector size mismatch")
+        p_out = np.zeros(self.N)
+        q_out = np.zeros(self.N)
+        pq = ctypes.c_double(0.0)
+        check(load().am_ku_pcg_step(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), int(load_case), ptr(r),
+                                    ptr(pp), float(beta), int(impl), ptr(p_out), ptr(q_out), ctypes.byref(pq)),
+              "am_ku_pcg_step")
+        return p_out, q_out, pq.value
 
     def solve(self, cfg, rho, load_case=0):
         u = np.zeros(self.N)

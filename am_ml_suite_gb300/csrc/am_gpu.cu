@@ -108,6 +108,10 @@ struct am_problem {
     Modal<double> M64;
     Modal<float> M32;
     KuLaunch plan32, plan64;
+    KuLaunch plan3;           // TMA-staged FP32 PCG K*u (ku3)
+    int ku3_stages = 4;
+    Ku3Maps *maps3 = nullptr;  // tensor maps of the FP32 PCG vectors (built on first use)
+    bool pad_dirty = true;     // scales or constraint bits changed since the padded copies were made
     int nblocks_vec = 0;
 
     std::vector<int8_t> grid_host;  // internal layout, empty = all design
@@ -125,6 +129,10 @@ struct am_problem {
     DevBuf<double> dinv64;
     DevBuf<float> dinv32;
     DevBuf<uint8_t> mask, nofix;
+    // padded copies read by the ku3 tensor maps: element scales (rows of
+    // round_up(nx, 4)) and constraint bits (rows of round_up(nx+1, 16))
+    DevBuf<float> s32pad;
+    DevBuf<uint8_t> maskpad;
     // vectors
     DevBuf<double> r64, xw64, p64a, p64b, q64v, vstage;
     DevBuf<float> x32, r32, p32a, p32b, q32v;
@@ -183,8 +191,13 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
         CK(P->p32a.alloc(nv, slack));
         CK(P->p32b.alloc(nv, slack));
         CK(P->q32v.alloc(nv));
+        long long se = 0, mb = 0;
+        ku3_padded_sizes(P->L, &se, &mb);
+        CK(P->s32pad.alloc((size_t)se));
+        CK(P->maskpad.alloc((size_t)mb));
     }
-    const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), P->nblocks_vec, 152 * 16});
+    const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), P->plan3.ntiles(), P->nblocks_vec,
+                                            152 * 16});
     CK(P->partial.alloc(np));
     return AM_OK;
 }
@@ -242,13 +255,37 @@ am_status setup_operator(am_problem *P, const am_simp_config &c, const double *r
     const int variant = c.variant;
     const int8_t *g = (variant == AM_VARIANT_PY && !P->grid_host.empty()) ? P->grid.p : nullptr;
     CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st));
+    P->pad_dirty = true;
     return AM_OK;
 }
 
 am_status setup_mask(am_problem *P, int lc) {
     const uint8_t *fb = (lc >= 0 && lc < (int)P->cases.size()) ? P->cases[lc].fixed_bits.p : nullptr;
     CK(diag_mask(P->L, P->s64.p, P->ke00, fb, P->dinv64.p, P->dinv32.p, P->mask.p, P->st));
+    P->pad_dirty = true;
     return AM_OK;
+}
+
+// The ku3 K*u reads its inputs through tensor maps: builds them once (the FP32
+// vectors keep their addresses for the problem's lifetime) and refreshes the
+// padded scale and constraint-bit copies after the operator or mask changed.
+am_status ku3_ready(am_problem *P) {
+    if (!P->maps3) {
+        cudaError_t e = cudaSuccess;
+        P->maps3 = ku3_make_maps(P->L, P->r32.p, P->p32a.p, P->p32b.p, P->dinv32.p, P->maskpad.p, P->s32pad.p,
+                                 P->q32v.p, &e);
+        if (!P->maps3) return fail(AM_ERR_CUDA, std::string("tensor maps of the PCG vectors: ") + cudaGetErrorString(e));
+    }
+    if (P->pad_dirty) {
+        CK(ku3_pad(P->L, P->s32.p, P->mask.p, P->s32pad.p, P->maskpad.p, P->st));
+        P->pad_dirty = false;
+    }
+    return AM_OK;
+}
+
+// one FP32 PCG K*u step: p = D^-1 r + beta p_prev, q = mask(K p), p.q -> alpha
+cudaError_t pcg_ku32(am_problem *P) {
+    return ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, P->ku3_stages, P->st);
 }
 
 // ||F||^2 over the free DOFs of case lc (mask already built)
@@ -279,12 +316,14 @@ am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
     CK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < P->chunk; ++k) {
         // the p ping-pong member is chosen on the device from the parity of S->it
-        cudaError_t e1 = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
-        cudaError_t e2;
-        if constexpr (std::is_same<T, float>::value)
+        cudaError_t e1, e2;
+        if constexpr (std::is_same<T, float>::value) {
+            e1 = pcg_ku32(P);
             e2 = pcg_update_df(P->L, P->x32.p, P->xl32.p, r, pa, pb, q, dinv, P->partial.p, P->S, P->st);
-        else
+        } else {
+            e1 = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
             e2 = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
+        }
         if (e1 != cudaSuccess || e2 != cudaSuccess) {
             cudaStreamEndCapture(P->st, &g);
             if (g) cudaGraphDestroy(g);
@@ -304,6 +343,7 @@ am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
 template <typename T>
 am_status run_pcg(am_problem *P, int *its, int *status) {
     cudaGraphExec_t *gx = std::is_same<T, float>::value ? &P->g32 : &P->g64;
+    if constexpr (std::is_same<T, float>::value) CKS(ku3_ready(P));
     if (!*gx) CKS(build_pcg_graph<T>(P, gx));
     CKS(sync_scalars(P));
     // every chunk either advances the iteration count or ends the solve; the
@@ -318,7 +358,7 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
     }
     *its = P->Sh->it;
     *status = P->Sh->status;
-    if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_CUDA, "a bulk-copy wait of the PCG update timed out");
+    if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_CUDA, "a bulk-copy wait of the PCG timed out");
     return AM_OK;
 }
 
@@ -650,8 +690,10 @@ am_status am_problem_create(int nx, int ny, int nz, double h, double E0, double 
     P->ke00 = element_stiffness_entry(M, 0, 0);
     P->plan32 = ku_plan(L, false, 0);
     P->plan64 = ku_plan(L, true, 0);
+    P->plan3 = ku3_plan(L);
     P->nblocks_vec = (int)std::max<long long>(1, std::min<long long>((3 * L.cs + 255) / 256, 152LL * 8));
     cudaError_t e = ku_init_attributes();
+    if (e == cudaSuccess) e = ku3_init_attributes();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&P->S, sizeof(Scalars));
     if (e == cudaSuccess) e = cudaMemset(P->S, 0, sizeof(Scalars));
@@ -701,7 +743,10 @@ am_status am_problem_destroy(am_problem *P) {
                              &P->vstage, &P->partial, &P->tap_w};
     for (auto *b : d64) b->release();
     P->oc_a32.release(); P->oc_lo32.release(); P->oc_hi32.release();
-    DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->r32, &P->p32a, &P->p32b, &P->q32v};
+    DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->xl32, &P->r32, &P->p32a, &P->p32b, &P->q32v, &P->s32pad};
+    P->maskpad.release();
+    ku3_free_maps(P->maps3);
+    P->maps3 = nullptr;
     P->xi64.release();
     for (auto *b : d32) b->release();
     P->design.release(); P->mask.release(); P->nofix.release(); P->grid.release(); P->tap_d.release();
@@ -797,6 +842,56 @@ am_status am_ku_apply(am_problem *P, const am_simp_config *cfg, const double *rh
         CK(dev_to_dof_t<float>(P->L, P->r32.p, P->vstage.p, P->st));
     }
     CK(cudaMemcpyAsync(y, P->vstage.p, sizeof(double) * P->N, cudaMemcpyDeviceToHost, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    return AM_OK;
+}
+
+am_status am_ku_pcg_step(am_problem *P, const am_simp_config *cfg, const double *rho, int load_case,
+                         const double *r, const double *p_prev, double beta, int impl, double *p_out,
+                         double *q_out, double *pq) {
+    CKS(check_problem(P));
+    CKS(check_cfg(P, cfg));
+    if (!rho || !r || !p_prev) return fail(AM_ERR_INVALID_ARG, "null array");
+    if (impl != 2 && impl != 3) return fail(AM_ERR_INVALID_ARG, "impl must be 2 or 3");
+    if (!std::isfinite(beta)) return fail(AM_ERR_INVALID_ARG, "beta must be finite");
+    if (load_case < 0 || load_case >= (int)P->cases.size()) return fail(AM_ERR_INVALID_ARG, "load case not set");
+    if (impl == 2 && P->plan32.warps != 8) return fail(AM_ERR_INVALID_ARG, "grid too large for the impl-2 kernel");
+    CKS(ensure_elements(P));
+    CKS(ensure_vectors(P, false));
+    CKS(upload_elem(P, rho, P->rho.p, cfg->layout));
+    CKS(setup_operator(P, *cfg, P->rho.p));
+    CKS(setup_mask(P, load_case));
+    CKS(ku3_ready(P));
+    CK(cudaMemcpyAsync(P->vstage.p, r, sizeof(double) * P->N, cudaMemcpyHostToDevice, P->st));
+    CK(dof_to_dev_t<float>(P->L, P->vstage.p, P->r32.p, P->st));
+    CK(cudaMemcpyAsync(P->vstage.p, p_prev, sizeof(double) * P->N, cudaMemcpyHostToDevice, P->st));
+    CK(dof_to_dev_t<float>(P->L, P->vstage.p, P->p32a.p, P->st));
+    CKS(sync_scalars(P));
+    Scalars run = *P->Sh;
+    run.done = 0;
+    run.it = 0;  // reads p32a, writes p32b
+    run.beta = beta;
+    run.rz = 1.0;
+    run.kerr = 0;
+    run.status = ST_RUNNING;
+    run.cnt_ku = 0;
+    CK(cudaMemcpyAsync(P->S, &run, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
+    if (impl == 3)
+        CK(pcg_ku32(P));
+    else
+        CK(ku2_pcg(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p, P->mask.p,
+                   P->q32v.p, P->partial.p, P->S, P->st));
+    CKS(sync_scalars(P));
+    if (P->Sh->kerr) return fail(AM_ERR_CUDA, "a copy wait of the PCG K*u timed out");
+    if (pq) *pq = P->Sh->pq;
+    if (p_out) {
+        CK(dev_to_dof_t<float>(P->L, P->p32b.p, P->vstage.p, P->st));
+        CK(cudaMemcpyAsync(p_out, P->vstage.p, sizeof(double) * P->N, cudaMemcpyDeviceToHost, P->st));
+    }
+    if (q_out) {
+        CK(dev_to_dof_t<float>(P->L, P->q32v.p, P->vstage.p, P->st));
+        CK(cudaMemcpyAsync(q_out, P->vstage.p, sizeof(double) * P->N, cudaMemcpyDeviceToHost, P->st));
+    }
     CK(cudaStreamSynchronize(P->st));
     return AM_OK;
 }
@@ -1064,6 +1159,7 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
     run.maxit = 1 << 30;
     run.it = 0;
     CK(cudaMemcpyAsync(P->S, &run, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
+    CKS(ku3_ready(P));
     DevBuf<uint8_t> flush;
     const size_t flush_bytes = 512ull << 20;
     if (flush_l2) CK(flush.alloc(flush_bytes));
@@ -1083,8 +1179,7 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
         CK(cudaEventRecord(e0, P->st));
         switch (which) {
             case 0:
-                CK(ku_pcg<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p,
-                                 P->mask.p, P->q32v.p, P->partial.p, P->S, P->st));
+                CK(pcg_ku32(P));
                 break;
             case 1:
                 CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->cases[0].x64.p, P->cases[0].F.p, P->dinv64.p,
@@ -1096,6 +1191,13 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                 break;
             case 3:
                 CK(ku_plain<float>(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->q32v.p, P->st));
+                break;
+            case 4:
+                CK(ku2_pcg(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p,
+                           P->mask.p, P->q32v.p, P->partial.p, P->S, P->st));
+                break;
+            case 5:
+                CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 3, P->st));
                 break;
             default:
                 return fail(AM_ERR_INVALID_ARG, "unknown kernel id");

@@ -26,26 +26,11 @@ static inline cudaError_t counted(cudaError_t e) {
 // ============================================================================
 // K*u launch plans and launchers
 // ============================================================================
-KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms) {
+KuLaunch ku_plan_shape(const Layout &L, int tx, int ty, int warps, int ctas_per_sm, int tz_hint, int sms) {
     KuLaunch K;
-    int ctas_per_sm;
-    if (fp64) {
-        K.tx = 32;
-        K.ty = 4;
-        K.warps = 0;
-        ctas_per_sm = 3;
-    } else if (3 * L.cs < (1LL << 31) && L.nel < (1LL << 31)) {
-        // warp-row kernel (32-bit indices)
-        K.warps = 8;
-        K.tx = Ku2Shape<8>::TX;
-        K.ty = Ku2Shape<8>::TY;
-        ctas_per_sm = 2;
-    } else {
-        K.tx = 32;
-        K.ty = 8;
-        K.warps = 0;
-        ctas_per_sm = 2;
-    }
+    K.tx = tx;
+    K.ty = ty;
+    K.warps = warps;
     K.tiles_x = div_up(L.nx + 1, K.tx);
     K.tiles_y = div_up(L.ny + 1, K.ty);
     const long long cols = (long long)K.tiles_x * K.tiles_y;
@@ -72,6 +57,14 @@ KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms) {
     K.tz = std::min(std::max(tz, 1), planes);
     K.tiles_z = div_up(planes, K.tz);
     return K;
+}
+
+KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms) {
+    if (fp64) return ku_plan_shape(L, 32, 4, 0, 3, tz_hint, sms);
+    // warp-row kernel (32-bit indices)
+    if (3 * L.cs < (1LL << 31) && L.nel < (1LL << 31))
+        return ku_plan_shape(L, Ku2Shape<8>::TX, Ku2Shape<8>::TY, 8, 2, tz_hint, sms);
+    return ku_plan_shape(L, 32, 8, 0, 2, tz_hint, sms);
 }
 
 template <typename T, int TX, int TY, int MODE>
@@ -160,6 +153,25 @@ cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, cons
     a.u = u;
     a.y = y;
     return dispatch_ku<T, KU_PLAIN>(K, a, st);
+}
+
+cudaError_t ku2_pcg(const KuLaunch &K, const Layout &L, const Modal<float> &M, const float *s, float *pa, float *pb,
+                    const float *r, const float *dinv, const uint8_t *mask, float *q, double *partial, Scalars *S,
+                    cudaStream_t st) {
+    if (K.warps != 8) return cudaErrorInvalidValue;
+    Ku2Args a{};
+    a.L = L;
+    a.M = M;
+    a.s = s;
+    a.pa = pa;
+    a.pb = pb;
+    a.r = r;
+    a.dinv = dinv;
+    a.mask = mask;
+    a.y = q;
+    a.partial = partial;
+    a.S = S;
+    return launch_ku2<KU_PCG>(K, a, st);
 }
 
 template <typename T>

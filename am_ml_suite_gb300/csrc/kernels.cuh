@@ -31,6 +31,34 @@ struct KuLaunch {
 // picks the z chunking from a wave-quantisation cost model (resident CTAs per SM
 // `ctas_per_sm`, `sms` multiprocessors).
 KuLaunch ku_plan(const Layout &L, bool fp64, int tz_hint, int sms = 152);
+// tiles of tx owned node columns x ty owned node rows, z chunking as above
+KuLaunch ku_plan_shape(const Layout &L, int tx, int ty, int warps, int ctas_per_sm, int tz_hint, int sms = 152);
+
+// ---- TMA-staged FP32 PCG K*u (ku3.cuh) -----------------------------------------
+struct Ku3Maps;
+// tensor maps of the problem's FP32 PCG vectors; the two padded arrays are
+// ku3_padded_sizes() long and filled by ku3_pad().  Returns nullptr and sets
+// *err on failure.  Free with ku3_free_maps.
+Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const float *pb, const float *dinv,
+                       const uint8_t *mask_pad, const float *scale_pad, float *q, cudaError_t *err);
+void ku3_free_maps(Ku3Maps *m);
+// entries of the padded element-scale copy (rows of round_up(nx, 4)) and bytes of
+// the padded constraint-bit copy (rows of round_up(nx+1, 16))
+void ku3_padded_sizes(const Layout &L, long long *scale_entries, long long *mask_bytes);
+// fills the padded copies from the element scales s32 (internal layout) and the
+// per-node constraint bits
+cudaError_t ku3_pad(const Layout &L, const float *s32, const uint8_t *mask, float *scale_pad, uint8_t *mask_pad,
+                    cudaStream_t st);
+// the launch plan (28 x 15 node tiles, two CTAs per SM)
+KuLaunch ku3_plan(const Layout &L, int sms = 152);
+// p = dinv r + beta p_prev, q = mask(K p), p.q -> S->alpha (ku_pcg's contract) with
+// `stages` (3 or 4) shared-memory stages
+cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,
+                    Scalars *S, int stages, cudaStream_t st);
+// the previous register-direct kernel (ku2_kernel) for the same PCG step (measurement)
+cudaError_t ku2_pcg(const KuLaunch &K, const Layout &L, const Modal<float> &M, const float *s, float *pa, float *pb,
+                    const float *r, const float *dinv, const uint8_t *mask, float *q, double *partial, Scalars *S,
+                    cudaStream_t st);
 
 template <typename T>
 cudaError_t ku_plain(const KuLaunch &K, const Layout &L, const Modal<T> &M, const T *s, const T *u,
@@ -153,6 +181,7 @@ cudaError_t masked_sqnorm(const long long *idx, const double *val, int n, long l
 // sets the shared-memory attributes of every compiled K*u kernel (call once,
 // outside stream capture)
 cudaError_t ku_init_attributes();
+cudaError_t ku3_init_attributes();
 
 // ---- OC ------------------------------------------------------------------------------
 // Per-element terms of the OC update: a = rho sqrt(-dc), lo = rho - move,

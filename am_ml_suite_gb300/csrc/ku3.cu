@@ -1,0 +1,159 @@
+// ku3.cu -- host side of the TMA-staged FP32 PCG K*u (ku3.cuh): tensor maps,
+// the padded copies they read, the launch plan and the launcher.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <new>
+
+#include "kernels.cuh"
+#include "ku3.cuh"
+
+namespace amk {
+
+static inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+void ku3_padded_sizes(const Layout &L, long long *scale_entries, long long *mask_bytes) {
+    if (scale_entries) *scale_entries = round_up(L.nx, 4) * L.ny * L.nz;
+    if (mask_bytes) *mask_bytes = round_up(L.nx + 1, 16) * (L.ny + 1) * (L.nz + 1);
+}
+
+// scale_pad[(ez ny + ey) sxe + ex] = s32[(ez ny + ey) nx + ex];
+// mask_pad[(iz (ny+1) + iy) sxm + ix] = mask[iz sxy + iy sx + ix]
+__global__ void ku3_pad_kernel(Layout L, const float *__restrict__ s32, const uint8_t *__restrict__ mask,
+                               float *__restrict__ scale_pad, uint8_t *__restrict__ mask_pad, int sxe, int sxm) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (long long e = i0; e < L.nel; e += stride) {
+        const long long row = e / L.nx;
+        const int ex = (int)(e - row * L.nx);
+        scale_pad[row * sxe + ex] = s32[e];
+    }
+    const long long nrow = (long long)(L.ny + 1) * (L.nz + 1);
+    const long long nn = nrow * (L.nx + 1);
+    for (long long n = i0; n < nn; n += stride) {
+        const long long row = n / (L.nx + 1);  // iz (ny+1) + iy
+        const int ix = (int)(n - row * (L.nx + 1));
+        const long long iz = row / (L.ny + 1), iy = row - iz * (L.ny + 1);
+        mask_pad[row * sxm + ix] = mask[iz * L.sxy + iy * L.sx + ix];
+    }
+}
+
+cudaError_t ku3_pad(const Layout &L, const float *s32, const uint8_t *mask, float *scale_pad, uint8_t *mask_pad,
+                    cudaStream_t st) {
+    const long long n = std::max<long long>(L.nel, (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1));
+    const int nb = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8));
+    ku3_pad_kernel<<<nb, 256, 0, st>>>(L, s32, mask, scale_pad, mask_pad, (int)round_up(L.nx, 4),
+                                       (int)round_up(L.nx + 1, 16));
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn(cudaError_t *err) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+            *err = e != cudaSuccess ? e : cudaErrorSymbolNotFound;
+            return nullptr;
+        }
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// rank-3 (x, y, z) or rank-4 (x, y, z, component) tiled map without swizzle;
+// strides in bytes of dims 1..rank-1; out-of-bound elements read as zero
+bool encode(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, CUtensorMapDataType dt, int rank, const void *base,
+            const cuuint64_t *dims, const cuuint64_t *strides, const cuuint32_t *box) {
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(m, dt, (cuuint32_t)rank, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const float *pb, const float *dinv,
+                       const uint8_t *mask_pad, const float *scale_pad, float *q, cudaError_t *err) {
+    using Sh = Ku3Shape<8, 4>;
+    *err = cudaSuccess;
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn(err);
+    if (!fn) return nullptr;
+    Ku3Maps *T = new (std::nothrow) Ku3Maps;
+    if (!T) {
+        *err = cudaErrorMemoryAllocation;
+        return nullptr;
+    }
+    const cuuint64_t nx1 = L.nx + 1, ny1 = L.ny + 1, nz1 = L.nz + 1;
+    const cuuint64_t vdims[4] = {nx1, ny1, nz1, 3};
+    const cuuint64_t vstr[3] = {(cuuint64_t)L.sx * 4, (cuuint64_t)L.sxy * 4, (cuuint64_t)L.cs * 4};
+    const cuuint32_t vload[4] = {Sh::BX, Sh::BY, 1, 3};
+    const cuuint32_t vstore[4] = {Sh::TX, Sh::TY, 1, 3};
+    const cuuint64_t ndims[3] = {nx1, ny1, nz1};
+    const cuuint32_t dbox[3] = {Sh::BX, Sh::BY, 1};
+    const long long sxm = round_up(L.nx + 1, 16), sxe = round_up(L.nx, 4);
+    const cuuint64_t mstr[2] = {(cuuint64_t)sxm, (cuuint64_t)(sxm * (L.ny + 1))};
+    const cuuint32_t mbox[3] = {Sh::BXM, Sh::BY, 1};
+    const cuuint64_t edims[3] = {(cuuint64_t)L.nx, (cuuint64_t)L.ny, (cuuint64_t)L.nz};
+    const cuuint64_t estr[2] = {(cuuint64_t)sxe * 4, (cuuint64_t)(sxe * L.ny * 4)};
+    const cuuint32_t ebox[3] = {Sh::BX, Sh::BYE, 1};
+    const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const bool ok = encode(fn, &T->r, F, 4, r, vdims, vstr, vload) && encode(fn, &T->pa, F, 4, pa, vdims, vstr, vload) &&
+                    encode(fn, &T->pb, F, 4, pb, vdims, vstr, vload) &&
+                    encode(fn, &T->d, F, 3, dinv, ndims, vstr, dbox) &&
+                    encode(fn, &T->m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, mask_pad, ndims, mstr, mbox) &&
+                    encode(fn, &T->s, F, 3, scale_pad, edims, estr, ebox) &&
+                    encode(fn, &T->qst, F, 4, q, vdims, vstr, vstore) &&
+                    encode(fn, &T->past, F, 4, pa, vdims, vstr, vstore) &&
+                    encode(fn, &T->pbst, F, 4, pb, vdims, vstr, vstore);
+    if (!ok) {
+        delete T;
+        *err = cudaErrorInvalidValue;
+        return nullptr;
+    }
+    return T;
+}
+
+void ku3_free_maps(Ku3Maps *m) { delete m; }
+
+KuLaunch ku3_plan(const Layout &L, int sms) {
+    return ku_plan_shape(L, Ku3Shape<8, 4>::TX, Ku3Shape<8, 4>::TY, 8, 2, 0, sms);
+}
+
+cudaError_t ku3_init_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(ku3_kernel<8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Ku3Shape<8, 3>::SMEM_ALLOC);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(ku3_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                Ku3Shape<8, 4>::SMEM_ALLOC);
+}
+
+cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,
+                    Scalars *S, int stages, cudaStream_t st) {
+    if (!T || K.warps != 8 || K.tx != Ku3Shape<8, 4>::TX || K.ty != Ku3Shape<8, 4>::TY) return cudaErrorInvalidValue;
+    Ku3Args a{};
+    a.M = M;
+    a.partial = partial;
+    a.S = S;
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tz = K.tz;
+    a.nz = L.nz;
+    if (stages == 4)
+        ku3_kernel<8, 4><<<K.ntiles(), 256, Ku3Shape<8, 4>::SMEM_ALLOC, st>>>(*T, a);
+    else if (stages == 3)
+        ku3_kernel<8, 3><<<K.ntiles(), 256, Ku3Shape<8, 3>::SMEM_ALLOC, st>>>(*T, a);
+    else
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+}  // namespace amk

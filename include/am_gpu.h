@@ -171,6 +171,18 @@ am_status am_problem_set_loads(am_problem *p, int n_cases, const double *F,
 am_status am_ku_apply(am_problem *p, const am_simp_config *cfg, const double *rho,
                       const double *u, double *y, int precision);
 
+/* One K*u step of the FP32 inner PCG on host data (the kernel every inner
+ * iteration of am_solve / am_simp_* runs; the product part of the Eigen
+ * ConjugateGradient iteration of LinearSolver::solve linear_solver.cpp:136-155):
+ * with the operator of rho, its Jacobi diagonal D and the constraint bits of load
+ * case `load_case` (fixed and orphan DOFs), p = D^-1 r + beta p_prev and
+ * q = mask(K p) in FP32, and *pq = p.q.  Vectors in the reference DOF order, FP64
+ * in and out.  impl 3: the tensor-copy staged kernel the solver uses; impl 2: the
+ * register-direct kernel it replaced (same arithmetic). */
+am_status am_ku_pcg_step(am_problem *p, const am_simp_config *cfg, const double *rho, int load_case,
+                         const double *r, const double *p_prev, double beta, int impl, double *p_out,
+                         double *q_out, double *pq);
+
 /* Solves K(rho) u = F_case with the constrained and orphan DOFs eliminated
  * (LinearSolver::solveWithBCs linear_solver.cpp:186-203; solve_fem fem.py:251-325).
  * u_out (nullable) receives u in the reference DOF order. */
@@ -223,8 +235,9 @@ long long am_launch_count(void);
 /* Times `reps` single launches of one kernel on the problem's stream with CUDA
  * events, after am_simp_begin (on the state the last am_simp_step left, or, before
  * the first step, on the initial density with zero vectors): which = 0 the
- * fused FP32 PCG K*u, 1 the FP64 residual K*u, 2 the FP32 PCG vector update,
- * 3 the plain FP32 K*u.  flush_l2 != 0 overwrites a 512 MB buffer before each
+ * fused FP32 PCG K*u (the tensor-copy staged kernel with 4 stages), 1 the FP64
+ * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
+ * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages.  flush_l2 != 0 overwrites a 512 MB buffer before each
  * launch so the kernel reads from HBM, then reads that buffer back so the write's
  * dirty L2 lines are written back before the timed launch.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
