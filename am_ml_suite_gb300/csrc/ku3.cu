@@ -94,7 +94,7 @@ Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const f
     const cuuint64_t vdims[4] = {nx1, ny1, nz1, 3};
     const cuuint64_t vstr[3] = {(cuuint64_t)L.sx * 4, (cuuint64_t)L.sxy * 4, (cuuint64_t)L.cs * 4};
     const cuuint32_t vload[4] = {Sh::BX, Sh::BY, 1, 3};
-    const cuuint32_t vstore[4] = {Sh::TX, Sh::TY, 1, 3};
+    const cuuint32_t vstore[4] = {Sh::TX, Sh::TY, 1, 1};
     const cuuint64_t ndims[3] = {nx1, ny1, nz1};
     const cuuint32_t dbox[3] = {Sh::BX, Sh::BY, 1};
     const long long sxm = round_up(L.nx + 1, 16), sxe = round_up(L.nx, 4);

@@ -42,7 +42,7 @@ struct Ku3Maps {
     CUtensorMap d;             // load: inverse diagonal [nz+1][ny+1][nx+1], box 36 x (2W+1) x 1
     CUtensorMap m;             // load: constraint bits (padded copy, 16-byte rows), box 48 x (2W+1) x 1
     CUtensorMap s;             // load: element scales (padded copy) [nz][ny][nx], box 36 x 2W x 1
-    CUtensorMap qst, past, pbst;  // stores: box 28 x (2W-1) x 1 x 3
+    CUtensorMap qst, past, pbst;  // stores: box 28 x (2W-1) x 1 x 1 (one per component)
 };
 
 struct Ku3Args {
@@ -72,10 +72,15 @@ struct Ku3Shape {
     static constexpr int OFF_M = OFF_D + r128(DIN_B);
     static constexpr int OFF_S = OFF_M + r128(MSK_B);
     static constexpr int STAGE = OFF_S + r128(SCL_B);
-    static constexpr int OUT_B = 3 * TY * TX * 4;  // one output tile [3][TY][TX]
-    static constexpr int OFF_OUT = S * STAGE;      // q[2], p[2]
+    // one output tile [3][TY+1][TX]: row TY of each component is a scratch row
+    // that lanes and rows owning no node write to, so the stores need no branch
+    static constexpr int OUT_CS = (TY + 1) * TX;  // component stride (floats)
+    static constexpr int OUT_B = 3 * OUT_CS * 4;
+    static constexpr int OFF_OUT = S * STAGE;  // q[2], p[2]
     static constexpr int OFF_XCH = OFF_OUT + 4 * r128(OUT_B);
-    static constexpr int XCH_B = 2 * W * 3 * 32 * 4;
+    // row exchange between warps [2][W+1][3][32]: slot 0 stays zero, warp w
+    // writes slot w+1 and reads slot w
+    static constexpr int XCH_B = 2 * (W + 1) * 3 * 32 * 4;
     static constexpr int OFF_RED = OFF_XCH + XCH_B;
     static constexpr int OFF_BAR = OFF_RED + r128(2 * W * 8);
     static constexpr int OFF_FLAG = OFF_BAR + 8 * S;  // two ints: copy-wait failure, last-block flag
@@ -122,12 +127,12 @@ template <int W, int S>
 __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ Ku3Maps T, const Ku3Args A) {
     using namespace k2;
     using Sh = Ku3Shape<W, S>;
-    constexpr int TX = Sh::TX, BX = Sh::BX, BY = Sh::BY, BXM = Sh::BXM, TY = Sh::TY;
+    constexpr int TX = Sh::TX, BX = Sh::BX, BY = Sh::BY, BXM = Sh::BXM, TY = Sh::TY, OCS = Sh::OUT_CS;
     extern __shared__ __align__(1024) unsigned char ku3_smem[];
     // tensor-copy destinations want 128-byte alignment: align the base to 1024
     unsigned char *smem = ku3_smem + ((1024u - (bulk::smem_addr(ku3_smem) & 1023u)) & 1023u);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::OFF_BAR);
-    float(*xch)[W][3][32] = reinterpret_cast<float(*)[W][3][32]>(smem + Sh::OFF_XCH);
+    float(*xch)[W + 1][3][32] = reinterpret_cast<float(*)[W + 1][3][32]>(smem + Sh::OFF_XCH);
     double *red = reinterpret_cast<double *>(smem + Sh::OFF_RED);
     int &s_fail = reinterpret_cast<int *>(smem + Sh::OFF_FLAG)[0];
     int &last_flag = reinterpret_cast<int *>(smem + Sh::OFF_FLAG)[1];
@@ -147,11 +152,19 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
     const bool use_p = beta != 0.f;
     const CUtensorMap *map_pin = odd ? &T.pb : &T.pa;
     const CUtensorMap *map_pout = odd ? &T.past : &T.pbst;
-    const int xm0 = (x0 - 1) & ~15;       // constraint-bit box origin (x0-1 rounded down to 16)
-    const int col = lane + 3;             // this lane's column in a staged node / element row
+    const int xm0 = (x0 - 1) & ~15;        // constraint-bit box origin (x0-1 rounded down to 16)
+    const int col = lane + 3;              // this lane's column in a staged node / element row
     const int mcol = x0 - 1 - xm0 + lane;  // ... and in a staged constraint-bit row (< 47)
     const bool own_lane = lane >= 1 && lane <= TX;
     const unsigned tx_bytes = (unsigned)(Sh::VEC_B * (use_p ? 2 : 1) + Sh::DIN_B + Sh::MSK_B + Sh::SCL_B);
+    // output offsets (floats, component 0) of this lane's q rows 0, 1 and p rows
+    // 1, 2; the scratch row where the lane or the warp owns no node
+    const int scratch = TY * TX + (lane & 15);
+    const int oq0 = (own_lane && w >= 1) ? (2 * w - 1) * TX + lane - 1 : scratch;
+    const int oq1 = own_lane ? (2 * w) * TX + lane - 1 : scratch;
+    const int op2 = (own_lane && w < W - 1) ? (2 * w + 1) * TX + lane - 1 : scratch;
+    const float f0 = (own_lane && w >= 1) ? 1.f : 0.f;  // p.q weights of rows 0 and 1
+    const float f1 = own_lane ? 1.f : 0.f;
 
     // plane z0-1+j (and element layer z0-2+j) into stage j % S
     auto issue = [&](int j) {
@@ -164,49 +177,34 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
         tma::load3(sb + Sh::OFF_M, &T.m, xm0, y0 - 1, iz, &bar[st]);
         tma::load3(sb + Sh::OFF_S, &T.s, x0 - 4, y0 - 1, iz - 1, &bar[st]);
     };
-    // output tile o (0/1) of q or p: [3][TY][TX]
+    // output tile o (0/1) of q or p: [3][TY+1][TX]
     auto qout = [&](int o) { return reinterpret_cast<float *>(smem + Sh::OFF_OUT + o * Sh::r128(Sh::OUT_B)); };
     auto pout = [&](int o) { return reinterpret_cast<float *>(smem + Sh::OFF_OUT + (2 + o) * Sh::r128(Sh::OUT_B)); };
-    // the tensor stores of the outputs written at iteration j (tile j & 1)
+    // the tensor stores of the outputs written at iteration j (tile j & 1):
+    // q of plane z0-2+j (an owned plane for j >= 2), p of plane z0-1+j (owned for j <= z1-z0)
     auto store_outputs = [&](int j) {
         bool any = false;
-        if (j >= 2) {  // q of plane z0-2+j
-            tma::store4(&T.qst, x0, y0, z0 - 2 + j, 0, qout(j & 1));
+        if (j >= 2) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) tma::store4(&T.qst, x0, y0, z0 - 2 + j, c, qout(j & 1) + c * OCS);
             any = true;
         }
-        if (j >= 1 && j <= z1 - z0) {  // p of plane z0-1+j
-            tma::store4(map_pout, x0, y0, z0 - 1 + j, 0, pout(j & 1));
+        if (j >= 1 && j <= z1 - z0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) tma::store4(map_pout, x0, y0, z0 - 1 + j, c, pout(j & 1) + c * OCS);
             any = true;
         }
         if (any) tma::commit();
     };
-
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < S; ++k) bulk::bar_init(&bar[k], 1);
-        bulk::bar_init_fence();
-        s_fail = 0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-        for (int j = 0; j < S && j < np; ++j) issue(j);
-
-    const float2 lam = splat(A.M.lam), mu = splat(A.M.mu), twomu = splat(2.f * A.M.mu), thrmu = splat(3.f * A.M.mu);
-    Face FB[3], CT[3];
-    float pcur[2][3];   // p of rows 0, 1 of the plane the current layer completes
-    unsigned mcur = 0;  // constraint bits of those rows (row 0: bits 0-2, row 1: bits 8-10)
-    Acc<float> dot;
-    int j = 0;
-    for (; j < np; ++j) {
-        const int st = j % S;
-        if (!bulk::bar_wait(&bar[st], (unsigned)(j / S) & 1u)) s_fail = 1;
+    // p on rows 2w .. 2w+2 of the plane in stage st, its constraint bits (rows 2w,
+    // 2w+1) and the scales of the element layer below it
+    auto read_plane = [&](int st, float (&v)[3][3], unsigned &mbits, float &sA, float &sB) {
         const unsigned char *sb = smem + st * Sh::STAGE;
         const float *Rs = reinterpret_cast<const float *>(sb + Sh::OFF_R);
         const float *Ps = reinterpret_cast<const float *>(sb + Sh::OFF_P);
         const float *Ds = reinterpret_cast<const float *>(sb + Sh::OFF_D);
         const float *Ss = reinterpret_cast<const float *>(sb + Sh::OFF_S);
         const uint8_t *Ms = sb + Sh::OFF_M;
-        // p on rows 2w .. 2w+2 of this plane
-        float v[3][3];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
             const int o = (2 * w + rr) * BX + col;
@@ -218,80 +216,109 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
                 v[rr][c] = fmaf(beta, pv, d * rv);
             }
         }
-        const unsigned mnew = (unsigned)Ms[(2 * w) * BXM + mcol] | ((unsigned)Ms[(2 * w + 1) * BXM + mcol] << 8);
-        const float sA = Ss[(2 * w) * BX + col], sB = Ss[(2 * w + 1) * BX + col];
-        Face FT[3];
+        mbits = (unsigned)Ms[(2 * w) * BXM + mcol] | ((unsigned)Ms[(2 * w + 1) * BXM + mcol] << 8);
+        sA = Ss[(2 * w) * BX + col];
+        sB = Ss[(2 * w + 1) * BX + col];
+    };
+    auto faces = [&](const float (&v)[3][3], Face (&F)[3]) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float n0 = __shfl_down_sync(0xffffffffu, v[0][c], 1);
             const float n1 = __shfl_down_sync(0xffffffffu, v[1][c], 1);
             const float n2 = __shfl_down_sync(0xffffffffu, v[2][c], 1);
-            FT[c] = face_modes(v[0][c], v[1][c], v[2][c], n0, n1, n2);
+            F[c] = face_modes(v[0][c], v[1][c], v[2][c], n0, n1, n2);
         }
-        float V[3][3];
-        if (j == 0) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) CT[c].ss = CT[c].sd = CT[c].ds = CT[c].dd = make_float2(0.f, 0.f);
-        } else {
-            layer_math(FB, FT, CT, make_float2(sA, sB), A.M, lam, mu, twomu, thrmu, V);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) xch[j & 1][w][c][lane] = V[2][c];
-        }
-        // the stores issued after the previous barrier have read their tile
-        if (threadIdx.x == 0) tma::wait_read_all();
-        __syncthreads();
-        if (s_fail) break;
-        if (threadIdx.x == 0) {
-            if (j + S < np) {
-                bulk::proxy_fence();
-                issue(j + S);
-            }
-            store_outputs(j - 1);
-        }
-        if (j >= 1) {
-            const int o = j & 1;
-            if (w >= 1) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) V[0][c] += xch[o][w - 1][c][lane];
-            }
-            if (j >= 2) {
-                // q of plane z0-2+j: rows 0 (w >= 1) and 1 -> output rows 2w-1, 2w
-                float *Q = qout(o);
-                float ds0 = 0.f, ds1 = 0.f;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float q0 = ((mcur >> c) & 1u) ? 0.f : V[0][c];
-                    const float q1 = ((mcur >> (8 + c)) & 1u) ? 0.f : V[1][c];
-                    if (own_lane) {
-                        if (w >= 1) Q[(c * TY + 2 * w - 1) * TX + lane - 1] = q0;
-                        Q[(c * TY + 2 * w) * TX + lane - 1] = q1;
-                    }
-                    ds0 = fmaf(pcur[0][c], q0, ds0);
-                    ds1 = fmaf(pcur[1][c], q1, ds1);
-                }
-                if (own_lane) {
-                    if (w >= 1) dot.add(ds0);
-                    dot.add(ds1);
-                }
-            }
-            if (j <= z1 - z0 && own_lane) {
-                // p of plane z0-1+j: rows 1 and 2 (w < W-1) -> output rows 2w, 2w+1
-                float *Pp = pout(o);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    Pp[(c * TY + 2 * w) * TX + lane - 1] = v[1][c];
-                    if (w < W - 1) Pp[(c * TY + 2 * w + 1) * TX + lane - 1] = v[2][c];
-                }
-            }
-            bulk::proxy_fence();  // this thread's tile writes before the copy engine reads them
-        }
+    };
+
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S; ++k) bulk::bar_init(&bar[k], 1);
+        bulk::bar_init_fence();
+        s_fail = 0;
+    }
+    if (threadIdx.x < 2 * 3 * 32) xch[threadIdx.x / 96][0][(threadIdx.x / 32) % 3][threadIdx.x & 31] = 0.f;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int j = 0; j < S && j < np; ++j) issue(j);
+
+    const float2 lam = splat(A.M.lam), mu = splat(A.M.mu), twomu = splat(2.f * A.M.mu), thrmu = splat(3.f * A.M.mu);
+    Face FB[3], CT[3];
+    float pcur[2][3];  // p of rows 0, 1 of the plane the current layer completes
+    unsigned mcur;     // constraint bits of those rows (row 0: bits 0-2, row 1: bits 8-10)
+    Acc<float> dot;
+    {
+        // plane z0-1: face modes only
+        if (!bulk::bar_wait(&bar[0], 0u)) s_fail = 1;
+        float v[3][3], sA, sB;
+        read_plane(0, v, mcur, sA, sB);
+        faces(v, FB);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            FB[c] = FT[c];
+            CT[c].ss = CT[c].sd = CT[c].ds = CT[c].dd = make_float2(0.f, 0.f);
             pcur[0][c] = v[0][c];
             pcur[1][c] = v[1][c];
         }
-        mcur = mnew;
+        __syncthreads();
+        if (threadIdx.x == 0 && !s_fail && S < np) {
+            bulk::proxy_fence();
+            issue(S);
+        }
+    }
+    int j = 1;
+    if (!s_fail) {
+        // two planes per trip: the carried face modes, p and constraint bits are
+        // renamed instead of copied
+#pragma unroll 2
+        for (; j < np; ++j) {
+            const int st = j % S;
+            if (!bulk::bar_wait(&bar[st], (unsigned)(j / S) & 1u)) s_fail = 1;
+            float v[3][3], sA, sB;
+            unsigned mnew;
+            read_plane(st, v, mnew, sA, sB);
+            Face FT[3];
+            faces(v, FT);
+            float V[3][3];
+            layer_math(FB, FT, CT, make_float2(sA, sB), A.M, lam, mu, twomu, thrmu, V);
+            const int o = j & 1;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) xch[o][w + 1][c][lane] = V[2][c];
+            // the stores issued after the previous barrier have read their tile
+            if (threadIdx.x == 0) tma::wait_read_all();
+            __syncthreads();
+            if (s_fail) break;
+            if (threadIdx.x == 0) {
+                if (j + S < np) {
+                    bulk::proxy_fence();
+                    issue(j + S);
+                }
+                store_outputs(j - 1);
+            }
+            // q of plane z0-2+j (rows 0, 1) and p of plane z0-1+j (rows 1, 2) into
+            // tile o; rows or planes this tile does not own land in rows it never
+            // stores
+            float *Q = qout(o), *Pp = pout(o);
+            float ds0 = 0.f, ds1 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float v0 = V[0][c] + xch[o][w][c][lane];
+                const float q0 = ((mcur >> c) & 1u) ? 0.f : v0;
+                const float q1 = ((mcur >> (8 + c)) & 1u) ? 0.f : V[1][c];
+                Q[c * OCS + oq0] = q0;
+                Q[c * OCS + oq1] = q1;
+                Pp[c * OCS + oq1] = v[1][c];
+                Pp[c * OCS + op2] = v[2][c];
+                ds0 = fmaf(pcur[0][c], q0, ds0);
+                ds1 = fmaf(pcur[1][c], q1, ds1);
+            }
+            if (j >= 2) dot.add(fmaf(f0, ds0, f1 * ds1));
+            bulk::proxy_fence();  // this thread's tile writes before the copy engine reads them
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                FB[c] = FT[c];
+                pcur[0][c] = v[0][c];
+                pcur[1][c] = v[1][c];
+            }
+            mcur = mnew;
+        }
     }
     if (s_fail) {
         // a stage did not arrive in time: wait (bounded) for this CTA's copies
