@@ -45,6 +45,7 @@ struct Scalars {
     double rz, rr, pq, alpha, beta, thr;
     double rz_prev;     // r.z of the previous iteration (beta after a residual replacement)
     double thr_update;  // mixed precision: recursive |r|^2 that triggers a reliable update
+    double alpha_prev;  // FP32 PCG: alpha of an even iteration whose alpha p is still owed to x
     int it, maxit, done, status;      // status: 0 ok, 1 converged, 2 max it, 3 breakdown, 4 nan,
                                       // 5 reliable update due
     // residual kernel results

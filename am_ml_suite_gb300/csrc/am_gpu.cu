@@ -356,6 +356,12 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
         count_launches(2LL * P->chunk);
         CKS(sync_scalars(P));
     }
+    if constexpr (std::is_same<T, float>::value) {
+        // the iterate folds every second iteration: pay the term a solve that
+        // stopped after an even iteration still owes
+        if (P->Sh->it & 1)
+            CK(pcg_df_settle(3 * P->L.cs, P->x32.p, P->xl32.p, P->p32a.p, P->p32b.p, P->S, P->nblocks_vec, P->st));
+    }
     *its = P->Sh->it;
     *status = P->Sh->status;
     if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_CUDA, "a bulk-copy wait of the PCG timed out");

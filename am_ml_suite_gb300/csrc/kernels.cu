@@ -357,12 +357,20 @@ template cudaError_t pcg_update<double>(const Layout &, double *, double *, cons
 // (2 DFMA per clock and SM) would take ~19 us per launch for the FMAs and the
 // FP32 -> FP64 conversions of a 5.4M-DOF grid.  (Adding the rounded product
 // instead cost 10 % more inner iterations on the 192x96x96 bracket.)
-// The six streams (xh, xl, r, p, q and the node's D^-1) are read in chunks of
-// UPD_K DOFs by bulk asynchronous copies into shared memory, UPD_ST chunks in
-// flight per CTA, so a CTA keeps ~100 KB of reads in flight without registers.
+// The iterate is folded every second iteration: an even iteration k only updates
+// r and owes alpha_k p_k to x (kept in Scalars::alpha_prev); the odd iteration
+// k+1 adds alpha_k p_k and alpha_{k+1} p_{k+1} in that order -- the same two
+// TwoSum steps, so x is bitwise that of a per-iteration update -- and a solve
+// that stops after an even iteration settles the debt with pcg_df_settle.  An
+// even iteration moves 40 bytes per DOF, an odd one 112 (76 on average instead
+// of 100).
+// The streams are read in chunks of UPD_K DOFs by bulk asynchronous copies
+// into shared memory: on a folding iteration 7 streams (xh, xl, r, p_prev, p, q
+// and the node's D^-1) in 2 stages, otherwise 3 (r, q, D^-1) in 4 stages, so a
+// CTA keeps 96-112 KB of reads in flight without registers.
 constexpr int UPD_K = 2048;  // DOFs per chunk (a multiple of 64, as cs is)
-constexpr int UPD_ST = 2;    // chunks in flight per CTA
-constexpr int UPD_SMEM = UPD_ST * 24 * UPD_K;
+constexpr int UPD_PLANES = 14;  // chunk planes of shared memory: 2 stages x 7 or 4 stages x 3
+constexpr int UPD_SMEM = UPD_PLANES * 4 * UPD_K;
 
 // (hi, lo) += a * b, the product added exactly (its FMA rounding error joins lo)
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float a, float b) {
@@ -376,23 +384,22 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float a, float
     lo = l - (hi - s);
 }
 
-__global__ void __launch_bounds__(VEC_THREADS)
-    pcg_update_df_kernel(Layout L, float *__restrict__ xh, float *__restrict__ xl, float *__restrict__ r,
-                         const float *pa, const float *pb, const float *__restrict__ q,
-                         const float *__restrict__ dinv, double *partial, Scalars *S) {
-    extern __shared__ __align__(128) unsigned char upd_smem[];
-    __shared__ uint64_t bar[UPD_ST];
-    __shared__ double red[2 * (VEC_THREADS / 32)];
-    __shared__ int last_flag, fail;
-    if (S->done) return;
-    const float alpha = (float)S->alpha;
-    const float *__restrict__ p = (S->it & 1) ? pa : pb;
+template <bool FOLD>
+__device__ __forceinline__ void pcg_update_df_body(const Layout &L, float *__restrict__ xh, float *__restrict__ xl,
+                                                   float *__restrict__ r, const float *__restrict__ p_prev,
+                                                   const float *__restrict__ p, const float *__restrict__ q,
+                                                   const float *__restrict__ dinv, double *partial, Scalars *S,
+                                                   float alpha_prev, float alpha, unsigned char *smem,
+                                                   uint64_t *bar, double *red, int &last_flag, int &fail) {
+    constexpr int NP = FOLD ? 7 : 3;          // streams per chunk
+    constexpr int NST = UPD_PLANES / NP;      // stages
+    // plane index of each stream within a stage
+    constexpr int P_R = FOLD ? 2 : 0, P_Q = FOLD ? 5 : 1, P_D = FOLD ? 6 : 2;
     const long long cs = L.cs;
     const int nck = (int)((cs + UPD_K - 1) / UPD_K);
     const int nchunks = 3 * nck;
-    // stage s: xh, xl, r, p, q, dinv planes of UPD_K floats
     auto plane = [&](int s, int a) {
-        return reinterpret_cast<float *>(upd_smem + (size_t)s * 24 * UPD_K + (size_t)4 * UPD_K * a);
+        return reinterpret_cast<float *>(smem + ((size_t)s * NP + a) * 4 * UPD_K);
     };
     auto chunk = [&](int g, long long &o, long long &j0, int &len) {
         const int c = g / nck;
@@ -405,16 +412,19 @@ __global__ void __launch_bounds__(VEC_THREADS)
         int len;
         chunk(g, o, j0, len);
         const unsigned b = 4u * (unsigned)len;
-        bulk::bar_expect(&bar[s], 6u * b);
-        bulk::copy_g2s(plane(s, 0), xh + o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 1), xl + o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 2), r + o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 3), p + o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 4), q + o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 5), dinv + j0, b, &bar[s]);
+        bulk::bar_expect(&bar[s], (unsigned)NP * b);
+        if (FOLD) {
+            bulk::copy_g2s(plane(s, 0), xh + o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 1), xl + o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 3), p_prev + o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 4), p + o, b, &bar[s]);
+        }
+        bulk::copy_g2s(plane(s, P_R), r + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, P_Q), q + o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, P_D), dinv + j0, b, &bar[s]);
     };
     if (threadIdx.x == 0) {
-        for (int s = 0; s < UPD_ST; ++s) bulk::bar_init(&bar[s], 1);
+        for (int s = 0; s < NST; ++s) bulk::bar_init(&bar[s], 1);
         bulk::bar_init_fence();
         fail = 0;
     }
@@ -422,36 +432,43 @@ __global__ void __launch_bounds__(VEC_THREADS)
     // this CTA's chunks: blockIdx.x + i * gridDim.x, i < mine
     const int mine = max(0, (nchunks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x);
     if (threadIdx.x == 0)
-        for (int i = 0; i < UPD_ST && i < mine; ++i) issue(blockIdx.x + i * gridDim.x, i);
+        for (int i = 0; i < NST && i < mine; ++i) issue(blockIdx.x + i * gridDim.x, i);
     Acc<float> a0, a1;
     int i = 0;
     for (; i < mine; ++i) {
-        const int s = i % UPD_ST;
-        if (!bulk::bar_wait(&bar[s], (unsigned)(i / UPD_ST) & 1u)) fail = 1;
+        const int s = i % NST;
+        if (!bulk::bar_wait(&bar[s], (unsigned)(i / NST) & 1u)) fail = 1;
         __syncthreads();
         if (fail) break;
         long long o, j0;
         int len;
         chunk(blockIdx.x + i * gridDim.x, o, j0, len);
-        const float4 *hs = reinterpret_cast<const float4 *>(plane(s, 0));
-        const float4 *ls = reinterpret_cast<const float4 *>(plane(s, 1));
-        const float4 *rs = reinterpret_cast<const float4 *>(plane(s, 2));
-        const float4 *ps = reinterpret_cast<const float4 *>(plane(s, 3));
-        const float4 *qs = reinterpret_cast<const float4 *>(plane(s, 4));
-        const float4 *ds = reinterpret_cast<const float4 *>(plane(s, 5));
+        const float4 *rs = reinterpret_cast<const float4 *>(plane(s, P_R));
+        const float4 *qs = reinterpret_cast<const float4 *>(plane(s, P_Q));
+        const float4 *ds = reinterpret_cast<const float4 *>(plane(s, P_D));
         for (int t = threadIdx.x; t < len / 4; t += VEC_THREADS) {
-            float4 h = hs[t], l = ls[t], rv = rs[t];
-            const float4 pv = ps[t], qv = qs[t], d = ds[t];
-            two_sum_acc(h.x, l.x, alpha, pv.x);
-            two_sum_acc(h.y, l.y, alpha, pv.y);
-            two_sum_acc(h.z, l.z, alpha, pv.z);
-            two_sum_acc(h.w, l.w, alpha, pv.w);
+            float4 rv = rs[t];
+            const float4 qv = qs[t], d = ds[t];
+            if (FOLD) {
+                float4 h = reinterpret_cast<const float4 *>(plane(s, 0))[t];
+                float4 l = reinterpret_cast<const float4 *>(plane(s, 1))[t];
+                const float4 pp = reinterpret_cast<const float4 *>(plane(s, 3))[t];
+                const float4 pv = reinterpret_cast<const float4 *>(plane(s, 4))[t];
+                two_sum_acc(h.x, l.x, alpha_prev, pp.x);
+                two_sum_acc(h.y, l.y, alpha_prev, pp.y);
+                two_sum_acc(h.z, l.z, alpha_prev, pp.z);
+                two_sum_acc(h.w, l.w, alpha_prev, pp.w);
+                two_sum_acc(h.x, l.x, alpha, pv.x);
+                two_sum_acc(h.y, l.y, alpha, pv.y);
+                two_sum_acc(h.z, l.z, alpha, pv.z);
+                two_sum_acc(h.w, l.w, alpha, pv.w);
+                reinterpret_cast<float4 *>(xh + o)[t] = h;
+                reinterpret_cast<float4 *>(xl + o)[t] = l;
+            }
             rv.x = fmaf(-alpha, qv.x, rv.x);
             rv.y = fmaf(-alpha, qv.y, rv.y);
             rv.z = fmaf(-alpha, qv.z, rv.z);
             rv.w = fmaf(-alpha, qv.w, rv.w);
-            reinterpret_cast<float4 *>(xh + o)[t] = h;
-            reinterpret_cast<float4 *>(xl + o)[t] = l;
             reinterpret_cast<float4 *>(r + o)[t] = rv;
             a0.add_prod(rv.x, rv.x);
             a0.add_prod(rv.y, rv.y);
@@ -463,17 +480,16 @@ __global__ void __launch_bounds__(VEC_THREADS)
             a1.add_prod(rv.w, d.w * rv.w);
         }
         __syncthreads();  // stage s read by every thread
-        if (threadIdx.x == 0 && i + UPD_ST < mine) {
+        if (threadIdx.x == 0 && i + NST < mine) {
             bulk::proxy_fence();
-            issue(blockIdx.x + (i + UPD_ST) * gridDim.x, s);
+            issue(blockIdx.x + (i + NST) * gridDim.x, s);
         }
     }
     if (fail) {
         // a copy did not complete within its wait: drain this CTA's outstanding
         // copies (bounded), flag the launch, and still take part in the reduction
         if (threadIdx.x == 0) {
-            for (int j = i; j < mine && j < i + UPD_ST; ++j)
-                bulk::bar_wait(&bar[j % UPD_ST], (unsigned)(j / UPD_ST) & 1u);
+            for (int j = i; j < mine && j < i + NST; ++j) bulk::bar_wait(&bar[j % NST], (unsigned)(j / NST) & 1u);
             atomicExch(&S->kerr, 1);
         }
     }
@@ -486,7 +502,59 @@ __global__ void __launch_bounds__(VEC_THREADS)
     if (!arrive_last_n(&S->cnt_upd, &last_flag, gridDim.x)) return;
     double tot[2];
     reduce_partials<2>(partial, gridDim.x, 2, tot, red);
-    if (threadIdx.x == 0) pcg_update_finish(S, tot[0], tot[1]);
+    if (threadIdx.x == 0) {
+        // an even iteration leaves alpha_k p_k owed to x; an odd one paid it
+        S->alpha_prev = FOLD ? 0.0 : S->alpha;
+        pcg_update_finish(S, tot[0], tot[1]);
+    }
+}
+
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_update_df_kernel(Layout L, float *__restrict__ xh, float *__restrict__ xl, float *__restrict__ r,
+                         const float *pa, const float *pb, const float *__restrict__ q,
+                         const float *__restrict__ dinv, double *partial, Scalars *S) {
+    extern __shared__ __align__(128) unsigned char upd_smem[];
+    __shared__ uint64_t bar[4];
+    __shared__ double red[2 * (VEC_THREADS / 32)];
+    __shared__ int last_flag, fail;
+    if (S->done) return;
+    const int it = S->it;
+    const float alpha = (float)S->alpha;
+    // p of this iteration is the ping-pong member its K*u wrote, p_prev the other
+    const float *p = (it & 1) ? pa : pb;
+    const float *p_prev = (it & 1) ? pb : pa;
+    if (it & 1)
+        pcg_update_df_body<true>(L, xh, xl, r, p_prev, p, q, dinv, partial, S, (float)S->alpha_prev, alpha,
+                                 upd_smem, bar, red, last_flag, fail);
+    else
+        pcg_update_df_body<false>(L, xh, xl, r, p_prev, p, q, dinv, partial, S, 0.f, alpha, upd_smem, bar, red,
+                                  last_flag, fail);
+}
+
+// x += alpha_prev p_prev when the last PCG iteration left that term owed (S->it
+// odd): p_prev is the ping-pong member the last K*u wrote
+__global__ void __launch_bounds__(VEC_THREADS)
+    pcg_df_settle_kernel(long long n, float *__restrict__ xh, float *__restrict__ xl, const float *pa,
+                         const float *pb, const Scalars *S) {
+    const int it = S->it;
+    if (!(it & 1)) return;
+    const float a = (float)S->alpha_prev;
+    const float *p = (it & 1) ? pb : pa;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float h = xh[i], l = xl[i];
+        two_sum_acc(h, l, a, p[i]);
+        xh[i] = h;
+        xl[i] = l;
+    }
+}
+cudaError_t pcg_df_settle(long long n, float *xh, float *xl, const float *pa, const float *pb, Scalars *S,
+                          int nblocks, cudaStream_t st) {
+    pcg_df_settle_kernel<<<nblocks, VEC_THREADS, 0, st>>>(n, xh, xl, pa, pb, S);
+    cudaError_t e = counted(cudaGetLastError());
+    if (e != cudaSuccess) return e;
+    // paid: a later folding iteration must not add it again
+    return cudaMemsetAsync(&S->alpha_prev, 0, sizeof(double), st);
 }
 
 static int g_upd_grid = 0;
@@ -1680,6 +1748,7 @@ __global__ void __launch_bounds__(32 * W_, 2) b_ku2_kernel(const BatchItem *item
 // run, so a CTA synchronises once per problem it touches rather than per chunk.
 // Items of frozen or converged problems are skipped without a copy (their state
 // cannot change during the launch: only a problem's own last run ends it).
+constexpr int UPD_ST = 2;  // batched update: stages of 6 chunk planes (xh, xl, r, p, q, D^-1)
 __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items, WorkList W) {
     extern __shared__ __align__(128) unsigned char upd_smem[];
     __shared__ uint64_t bar[UPD_ST];

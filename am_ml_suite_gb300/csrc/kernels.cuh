@@ -87,8 +87,14 @@ cudaError_t pcg_update(const Layout &L, double *x, T *r, const T *pa, const T *p
 // vectors), the streams staged by bulk copies; one wave of 2 CTAs per SM (after
 // ku_init_attributes).  A bulk-copy wait that runs out ends the solve with
 // status ST_TIMEOUT.
+// The iterate is folded every second iteration (even iterations owe alpha p to
+// x in S->alpha_prev); pcg_df_settle pays an owed term once a solve stopped.
 cudaError_t pcg_update_df(const Layout &L, float *xh, float *xl, float *r, const float *pa, const float *pb,
                           const float *q, const float *dinv, double *partial, Scalars *S, cudaStream_t st);
+// x += S->alpha_prev p (p the last iteration's ping-pong member) if S->it is odd,
+// then S->alpha_prev = 0; n = 3 cs entries
+cudaError_t pcg_df_settle(long long n, float *xh, float *xl, const float *pa, const float *pb, Scalars *S,
+                          int nblocks, cudaStream_t st);
 int pcg_update_df_grid();
 // reads `bytes` (a multiple of 16) of buf through L2 (measurement: cleans the
 // L2 lines a flush write left dirty)

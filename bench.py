@@ -529,17 +529,20 @@ def main():
     # ---- roofline of the dominant kernel (fused FP32 PCG K*u) ---------------
     nodes, nel = lay["nodes"], lay["elements"]
     ku_ms, ku_min = p.bench_kernel(0, reps=20, flush_l2=True)
-    # reads p, r (3 x 4 B each per node), dinv (4 B), mask (1 B), scale (4 B per
-    # element); writes p, q (3 x 4 B each per node)
+    # reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B), scale
+    # (4 B per element); writes p, q (3 x 4 B each per node)
     alg_bytes = 53 * nodes + 4 * nel
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (ku_ms * 1e-3) / 1e9
     traffic = ku_traffic_per_launch(W, nodes, nel)
     res_ms, _ = p.bench_kernel(1, reps=5, flush_l2=True)
     upd_ms, upd_min = p.bench_kernel(2, reps=20, flush_l2=True)
-    # the other half of a PCG iteration: reads the double-float iterate (8 B per
-    # DOF), r, p, q (4 B each) and dinv (4 B per node); writes the iterate and r
-    upd_bytes = 100 * nodes
+    # the other half of a PCG iteration, averaged over the even / odd pair the
+    # timed launches alternate between: an even iteration reads r, q (3 x 4 B each
+    # per node) and dinv (4 B) and writes r (40 B per node); an odd one also reads
+    # the double-float iterate (3 x 8 B), p_prev and p (3 x 4 B each) and writes
+    # the iterate (112 B per node)
+    upd_bytes = 76 * nodes
     p.close()
 
     # ---- end to end through the C ABI from host buffers ---------------------
@@ -592,12 +595,12 @@ def main():
             "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,
             "solver_residual_max": max(r.solver_residual for r in res),
             "compliance_last": res[-1].compliance,
-            "roofline": {"bound": "hbm", "kernel": "ku2_kernel<8,KU_PCG> (fused p-update + FP32 K*p + p.q)",
+            "roofline": {"bound": "hbm", "kernel": "ku3_kernel<8,4> (tensor-copy staged p-update + FP32 K*p + p.q)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
                          "avg_ms": ku_ms, "min_ms": ku_min},
             "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_fp64": res_ms, "pcg_update_fp32": upd_ms},
-            "roofline_update": {"bound": "hbm", "kernel": "pcg_update_df_kernel (double-float iterate, bulk-copy staged)",
+            "roofline_update": {"bound": "hbm", "kernel": "pcg_update_df_kernel (double-float iterate folded every 2nd iteration, bulk-copy staged)",
                                 "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                                 "frac": upd_bytes / (upd_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": upd_bytes,
                                 "avg_ms": upd_ms, "min_ms": upd_min},
