@@ -1182,6 +1182,11 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
             CK(l2_flush_read(flush.p, flush_bytes, P->st));
         }
         CK(cudaMemcpyAsync(&P->S->done, &run.done, sizeof(int), cudaMemcpyHostToDevice, P->st));
+        if (which == 6 || which == 7) {
+            // the update of an even (6: r only) or odd (7: r and the folded iterate) iteration
+            const int parity = which - 6;
+            CK(cudaMemcpyAsync(&P->S->it, &parity, sizeof(int), cudaMemcpyHostToDevice, P->st));
+        }
         CK(cudaEventRecord(e0, P->st));
         switch (which) {
             case 0:
@@ -1192,6 +1197,8 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                             P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
                 break;
             case 2:
+            case 6:
+            case 7:
                 CK(pcg_update_df(P->L, P->x32.p, P->xl32.p, P->r32.p, P->p32a.p, P->p32b.p, P->q32v.p,
                                  P->dinv32.p, P->partial.p, P->S, P->st));
                 break;

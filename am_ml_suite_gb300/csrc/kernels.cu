@@ -470,14 +470,11 @@ __device__ __forceinline__ void pcg_update_df_body(const Layout &L, float *__res
             rv.z = fmaf(-alpha, qv.z, rv.z);
             rv.w = fmaf(-alpha, qv.w, rv.w);
             reinterpret_cast<float4 *>(r + o)[t] = rv;
-            a0.add_prod(rv.x, rv.x);
-            a0.add_prod(rv.y, rv.y);
-            a0.add_prod(rv.z, rv.z);
-            a0.add_prod(rv.w, rv.w);
-            a1.add_prod(rv.x, d.x * rv.x);
-            a1.add_prod(rv.y, d.y * rv.y);
-            a1.add_prod(rv.z, d.z * rv.z);
-            a1.add_prod(rv.w, d.w * rv.w);
+            // r.r and r.D^-1 r: the four non-negative terms of a float4 summed in
+            // FP32 (no cancellation: within a few ulps), the float4 sums in
+            // double-float
+            a0.add(fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, rv.w * rv.w))));
+            a1.add(fmaf(rv.x, d.x * rv.x, fmaf(rv.y, d.y * rv.y, fmaf(rv.z, d.z * rv.z, rv.w * (d.w * rv.w)))));
         }
         __syncthreads();  // stage s read by every thread
         if (threadIdx.x == 0 && i + NST < mine) {

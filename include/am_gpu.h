@@ -237,7 +237,9 @@ long long am_launch_count(void);
  * the first step, on the initial density with zero vectors): which = 0 the
  * fused FP32 PCG K*u (the tensor-copy staged kernel with 4 stages), 1 the FP64
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
- * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages.  flush_l2 != 0 overwrites a 512 MB buffer before each
+ * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
+ * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
+ * and folded iterate) iteration.  flush_l2 != 0 overwrites a 512 MB buffer before each
  * launch so the kernel reads from HBM, then reads that buffer back so the write's
  * dirty L2 lines are written back before the timed launch.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
