@@ -364,13 +364,16 @@ template cudaError_t pcg_update<double>(const Layout &, double *, double *, cons
 // that stops after an even iteration settles the debt with pcg_df_settle.  An
 // even iteration moves 40 bytes per DOF, an odd one 112 (76 on average instead
 // of 100).
-// The streams are read in chunks of UPD_K DOFs by bulk asynchronous copies
-// into shared memory: on a folding iteration 7 streams (xh, xl, r, p_prev, p, q
-// and the node's D^-1) in 2 stages, otherwise 3 (r, q, D^-1) in 4 stages, so a
-// CTA keeps 96-112 KB of reads in flight without registers.
-constexpr int UPD_K = 2048;  // DOFs per chunk (a multiple of 64, as cs is)
-constexpr int UPD_PLANES = 14;  // chunk planes of shared memory: 2 stages x 7 or 4 stages x 3
-constexpr int UPD_SMEM = UPD_PLANES * 4 * UPD_K;
+// The streams are read in chunks by bulk asynchronous copies into shared memory:
+// on a folding iteration 7 streams (xh, xl, r, p_prev, p, q and the node's D^-1),
+// otherwise 3 (r, q, D^-1), two chunks in flight per CTA (96-112 KB of reads)
+// without registers.
+constexpr int UPD_K = 2048;  // DOFs per chunk of the batched update (a multiple of 64, as cs is)
+constexpr int UPD_SMEM = 14 * 4 * UPD_K;  // shared memory of either update: 112 KB, two CTAs per SM
+// single-problem update: two stages of chunks, 2048 DOFs x 7 streams on odd
+// iterations, 4096 DOFs x 3 streams on even ones (1024-DOF chunks in 4 / 9 stages
+// were slower: 40.9 / 26.2 us against 39.4 / 23.7 us on the 192x96x96 bracket)
+constexpr int UPD1_ST = 2;
 
 // (hi, lo) += a * b, the product added exactly (its FMA rounding error joins lo)
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float a, float b) {
@@ -392,19 +395,21 @@ __device__ __forceinline__ void pcg_update_df_body(const Layout &L, float *__res
                                                    float alpha_prev, float alpha, unsigned char *smem,
                                                    uint64_t *bar, double *red, int &last_flag, int &fail) {
     constexpr int NP = FOLD ? 7 : 3;          // streams per chunk
-    constexpr int NST = UPD_PLANES / NP;      // stages
+    constexpr int NST = UPD1_ST;              // stages
+    constexpr int UPD1_K = FOLD ? 2048 : 4096;  // DOFs per chunk
+    static_assert(NST * NP * 4 * UPD1_K <= UPD_SMEM, "update stages exceed the shared memory");
     // plane index of each stream within a stage
     constexpr int P_R = FOLD ? 2 : 0, P_Q = FOLD ? 5 : 1, P_D = FOLD ? 6 : 2;
     const long long cs = L.cs;
-    const int nck = (int)((cs + UPD_K - 1) / UPD_K);
+    const int nck = (int)((cs + UPD1_K - 1) / UPD1_K);
     const int nchunks = 3 * nck;
     auto plane = [&](int s, int a) {
-        return reinterpret_cast<float *>(smem + ((size_t)s * NP + a) * 4 * UPD_K);
+        return reinterpret_cast<float *>(smem + ((size_t)s * NP + a) * 4 * UPD1_K);
     };
     auto chunk = [&](int g, long long &o, long long &j0, int &len) {
         const int c = g / nck;
-        j0 = (long long)(g - c * nck) * UPD_K;
-        len = (int)min((long long)UPD_K, cs - j0);
+        j0 = (long long)(g - c * nck) * UPD1_K;
+        len = (int)min((long long)UPD1_K, cs - j0);
         o = c * cs + j0;
     };
     auto issue = [&](int g, int s) {
@@ -511,7 +516,7 @@ __global__ void __launch_bounds__(VEC_THREADS)
                          const float *pa, const float *pb, const float *__restrict__ q,
                          const float *__restrict__ dinv, double *partial, Scalars *S) {
     extern __shared__ __align__(128) unsigned char upd_smem[];
-    __shared__ uint64_t bar[4];
+    __shared__ uint64_t bar[UPD1_ST];
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag, fail;
     if (S->done) return;
