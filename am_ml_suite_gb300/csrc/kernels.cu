@@ -673,6 +673,7 @@ __device__ __forceinline__ void pcg_start_body(Layout L, const T *__restrict__ r
         S->thr = thr >= 0.0 ? thr : -thr * tot[0];  // negative: relative to this |r|^2
         S->thr_update = upd_factor * tot[0];
         S->alpha = 0.0;
+        S->alpha_prev = 0.0;  // no iterate term owed at a (re)start
         S->maxit = maxit;
         S->status = ST_RUNNING;
         S->done = 0;
@@ -1750,14 +1751,14 @@ __global__ void __launch_bounds__(32 * W_, 2) b_ku2_kernel(const BatchItem *item
 // run, so a CTA synchronises once per problem it touches rather than per chunk.
 // Items of frozen or converged problems are skipped without a copy (their state
 // cannot change during the launch: only a problem's own last run ends it).
-constexpr int UPD_ST = 2;  // batched update: stages of 6 chunk planes (xh, xl, r, p, q, D^-1)
+constexpr int UPD_ST = 2;  // batched update: stages of 7 chunk planes (xh, xl, r, p_prev, p, q, D^-1)
 __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items, WorkList W) {
     extern __shared__ __align__(128) unsigned char upd_smem[];
     __shared__ uint64_t bar[UPD_ST];
     __shared__ double red[2 * (VEC_THREADS / 32)];
     __shared__ int last_flag, fail;
     auto plane = [&](int s, int a) {
-        return reinterpret_cast<float *>(upd_smem + (size_t)s * 24 * UPD_K + (size_t)4 * UPD_K * a);
+        return reinterpret_cast<float *>(upd_smem + (size_t)s * 28 * UPD_K + (size_t)4 * UPD_K * a);
     };
     struct Chunk {
         long long o, j0;
@@ -1778,19 +1779,25 @@ __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items
         const Scalars *S = items[W.w[i].x].S;
         return !S->frozen && !S->done;
     };
+    // an odd iteration of a problem folds its iterate (x += alpha_prev p_prev +
+    // alpha p, as the single-problem update): 7 streams; an even one 3 (r, q, D^-1)
     auto issue = [&](int i, int s) {
         const int2 k = W.w[i];
         const BatchItem &it = items[k.x];
         const Chunk c = chunk(it, k.y);
-        const float *p = (it.S->it & 1) ? it.pa : it.pb;
+        const bool fold = (it.S->it & 1) != 0;
         const unsigned b = 4u * (unsigned)c.len;
-        bulk::bar_expect(&bar[s], 6u * b);
-        bulk::copy_g2s(plane(s, 0), it.xh + c.o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 1), it.xl + c.o, b, &bar[s]);
+        bulk::bar_expect(&bar[s], (fold ? 7u : 3u) * b);
+        if (fold) {
+            const float *p = it.pa, *pp = it.pb;  // it odd: this iteration's K*u wrote pa
+            bulk::copy_g2s(plane(s, 0), it.xh + c.o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 1), it.xl + c.o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 3), pp + c.o, b, &bar[s]);
+            bulk::copy_g2s(plane(s, 4), p + c.o, b, &bar[s]);
+        }
         bulk::copy_g2s(plane(s, 2), it.r32 + c.o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 3), p + c.o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 4), it.q32 + c.o, b, &bar[s]);
-        bulk::copy_g2s(plane(s, 5), it.dinv32 + c.j0, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 5), it.q32 + c.o, b, &bar[s]);
+        bulk::copy_g2s(plane(s, 6), it.dinv32 + c.j0, b, &bar[s]);
     };
     if (threadIdx.x == 0) {
         for (int s = 0; s < UPD_ST; ++s) bulk::bar_init(&bar[s], 1);
@@ -1826,7 +1833,11 @@ __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items
         if (arrive_last_weighted(&it.S->cnt_upd, &last_flag, run_last - run_first + 1, nb)) {
             double tot[2];
             reduce_partials<2>(it.partial, nb, 2, tot, red);
-            if (threadIdx.x == 0) pcg_update_finish(it.S, tot[0], tot[1]);
+            if (threadIdx.x == 0) {
+                // an even iteration leaves alpha_k p_k owed to the iterate; an odd one paid it
+                it.S->alpha_prev = (it.S->it & 1) ? 0.0 : it.S->alpha;
+                pcg_update_finish(it.S, tot[0], tot[1]);
+            }
         }
         a0 = Acc<float>();
         a1 = Acc<float>();
@@ -1851,35 +1862,41 @@ __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items
             const BatchItem &it = items[k.x];
             const Chunk c = chunk(it, k.y);
             const float alpha = (float)it.S->alpha;
+            const bool fold = (it.S->it & 1) != 0;
+            const float alpha_prev = (float)it.S->alpha_prev;
             if (!fail) {
                 const float4 *hs = reinterpret_cast<const float4 *>(plane(s, 0));
                 const float4 *ls = reinterpret_cast<const float4 *>(plane(s, 1));
                 const float4 *rs = reinterpret_cast<const float4 *>(plane(s, 2));
-                const float4 *ps = reinterpret_cast<const float4 *>(plane(s, 3));
-                const float4 *qs = reinterpret_cast<const float4 *>(plane(s, 4));
-                const float4 *ds = reinterpret_cast<const float4 *>(plane(s, 5));
+                const float4 *pps = reinterpret_cast<const float4 *>(plane(s, 3));
+                const float4 *ps = reinterpret_cast<const float4 *>(plane(s, 4));
+                const float4 *qs = reinterpret_cast<const float4 *>(plane(s, 5));
+                const float4 *ds = reinterpret_cast<const float4 *>(plane(s, 6));
                 for (int t = threadIdx.x; t < c.len / 4; t += VEC_THREADS) {
-                    float4 h = hs[t], l = ls[t], rv = rs[t];
-                    const float4 pv = ps[t], qv = qs[t], d = ds[t];
-                    two_sum_acc(h.x, l.x, alpha, pv.x);
-                    two_sum_acc(h.y, l.y, alpha, pv.y);
-                    two_sum_acc(h.z, l.z, alpha, pv.z);
-                    two_sum_acc(h.w, l.w, alpha, pv.w);
+                    float4 rv = rs[t];
+                    const float4 qv = qs[t], d = ds[t];
+                    if (fold) {
+                        float4 h = hs[t], l = ls[t];
+                        const float4 pp = pps[t], pv = ps[t];
+                        two_sum_acc(h.x, l.x, alpha_prev, pp.x);
+                        two_sum_acc(h.y, l.y, alpha_prev, pp.y);
+                        two_sum_acc(h.z, l.z, alpha_prev, pp.z);
+                        two_sum_acc(h.w, l.w, alpha_prev, pp.w);
+                        two_sum_acc(h.x, l.x, alpha, pv.x);
+                        two_sum_acc(h.y, l.y, alpha, pv.y);
+                        two_sum_acc(h.z, l.z, alpha, pv.z);
+                        two_sum_acc(h.w, l.w, alpha, pv.w);
+                        reinterpret_cast<float4 *>(it.xh + c.o)[t] = h;
+                        reinterpret_cast<float4 *>(it.xl + c.o)[t] = l;
+                    }
                     rv.x = fmaf(-alpha, qv.x, rv.x);
                     rv.y = fmaf(-alpha, qv.y, rv.y);
                     rv.z = fmaf(-alpha, qv.z, rv.z);
                     rv.w = fmaf(-alpha, qv.w, rv.w);
-                    reinterpret_cast<float4 *>(it.xh + c.o)[t] = h;
-                    reinterpret_cast<float4 *>(it.xl + c.o)[t] = l;
                     reinterpret_cast<float4 *>(it.r32 + c.o)[t] = rv;
-                    a0.add_prod(rv.x, rv.x);
-                    a0.add_prod(rv.y, rv.y);
-                    a0.add_prod(rv.z, rv.z);
-                    a0.add_prod(rv.w, rv.w);
-                    a1.add_prod(rv.x, d.x * rv.x);
-                    a1.add_prod(rv.y, d.y * rv.y);
-                    a1.add_prod(rv.z, d.z * rv.z);
-                    a1.add_prod(rv.w, d.w * rv.w);
+                    a0.add(fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, rv.w * rv.w))));
+                    a1.add(fmaf(rv.x, d.x * rv.x,
+                                fmaf(rv.y, d.y * rv.y, fmaf(rv.z, d.z * rv.z, rv.w * (d.w * rv.w)))));
                 }
             } else if (threadIdx.x == 0) {
                 atomicExch(&it.S->kerr, 1);
@@ -1903,14 +1920,22 @@ __global__ void __launch_bounds__(256) b_update_df_kernel(const BatchItem *items
             if (issued & (1u << s)) bulk::bar_wait(&bar[s], (phase >> s) & 1u);
     }
 }
-// x64 = xh + xl for every active problem (end of an FP32 PCG round)
+// x64 = xh + xl for every active problem (end of an FP32 PCG round), after the
+// term alpha_prev p an even last iteration left owed (the next round's start
+// clears alpha_prev)
 __global__ void __launch_bounds__(256) b_compose_kernel(const BatchItem *items, WorkList W) {
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
         const long long n = 3 * it.L.cs;
-        for (long long i = _k.y * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x)
-            it.x64[i] = (double)it.xh[i] + (double)it.xl[i];
+        const bool owed = (it.S->it & 1) != 0;
+        const float a = (float)it.S->alpha_prev;
+        const float *p = it.pb;  // it odd: the last K*u wrote pb
+        for (long long i = _k.y * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)it.n_vec * blockDim.x) {
+            float h = it.xh[i], l = it.xl[i];
+            if (owed) two_sum_acc(h, l, a, p[i]);
+            it.x64[i] = (double)h + (double)l;
+        }
     }
 }
 cudaError_t batch_inner_end(const BatchItem *it, WorkList vec, int grid, cudaStream_t st) {
