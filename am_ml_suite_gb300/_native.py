@@ -22,6 +22,7 @@ STATUS = {0: "AM_OK", 1: "AM_ERR_INVALID_ARG", 2: "AM_ERR_SIZE_MISMATCH", 3: "AM
 LAYOUT_ZFASTEST, LAYOUT_XFASTEST = 0, 1
 VARIANT_CPP, VARIANT_PY = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+MIXED_RELIABLE, MIXED_FLEXIBLE = 0, 1
 PRECOND_JACOBI, PRECOND_LEARNED = 0, 1
 
 
@@ -56,6 +57,7 @@ class SimpConfig(ctypes.Structure):
         ("max_outer", ctypes.c_int),
         ("layout", ctypes.c_int),
         ("verbose", ctypes.c_int),
+        ("mixed_solver", ctypes.c_int),
     ]
 
 

@@ -428,6 +428,57 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         o.residual = std::sqrt(P->Sh->res_rr / bnorm2);
         o.converged = (stt == ST_CONVERGED) ? 1 : 0;
         if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the PCG iteration");
+    } else if (!learned0 && c.mixed_solver == AM_MIXED_RELIABLE) {
+        // Mixed precision, one FP32 Jacobi-PCG sequence with reliable updates
+        // (residual replacement, van der Vorst and Ye): the FP32 iteration runs
+        // until its recursive residual has fallen by inner_tol; then the
+        // double-float iterate is added to the FP64 displacement, the residual is
+        // recomputed in FP64 and replaces the recursive one, and the sequence
+        // continues along its last search direction (beta from the replaced
+        // residual) instead of restarting, so the Krylov space built so far is kept.
+        // The solve is accepted on the recomputed FP64 residual.
+        CKS(ensure_vectors(P, true));
+        const int max_rounds = c.max_outer > 0 ? c.max_outer : 200;
+        const double red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
+        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
+                    want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+        CKS(sync_scalars(P));
+        double rel = std::sqrt(P->Sh->res_rr / bnorm2);
+        int total = 0, rounds = 0, restart = 0, stt = ST_RUNNING;
+        bool nan = !std::isfinite(rel);
+        while (!nan && rel > tol && rounds < max_rounds && total < maxit) {
+            CK(dc_inner_init(P->L, P->r64.p, P->r32.p, nullptr, P->S, P->nblocks_vec, P->st));
+            CKS(inner_iterate_zero(P));
+            // stop the FP32 sequence at half the goal (the recursive residual runs
+            // ahead of the true one) or after a reduction by inner_tol
+            CK(pcg_start<float>(P->L, P->r32.p, P->dinv32.p, 0.25 * tol * tol * bnorm2, red * red,
+                                maxit, restart, P->partial.p, P->S, P->nblocks_vec, P->st));
+            int its = 0;
+            CKS(run_pcg<float>(P, &its, &stt));
+            total = its;  // S->it runs on across replacements
+            ++rounds;
+            if (stt == ST_NAN) {
+                nan = true;
+                break;
+            }
+            CK(df_accumulate(P->x32.p, P->xl32.p, C.x64.p, 3 * P->L.cs, P->nblocks_vec, P->st));
+            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
+                        want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+            CKS(sync_scalars(P));
+            rel = std::sqrt(P->Sh->res_rr / bnorm2);
+            nan = !std::isfinite(rel);
+            if (c.verbose >= 2)
+                std::printf("  round %d: PCG iterations %d, status %d, rel-res %.3e\n", rounds, total, stt, rel);
+            if (stt == ST_MAXIT) break;
+            // continue the sequence along p (residual replacement); after a
+            // breakdown take a fresh direction from the replaced residual
+            restart = (stt == ST_BREAKDOWN) ? 2 : 1;
+        }
+        if (nan) return fail(AM_ERR_NAN_DETECTED, "NaN in the mixed-precision solve");
+        o.iterations = total;
+        o.outer = rounds;
+        o.residual = rel;
+        o.converged = rel <= tol ? 1 : 0;
     } else {
         // Mixed precision: flexible CG in FP64 (FP64 K*u, vectors and dot
         // products, so the accepted iterate has the energy-norm quality of FP64 CG
@@ -572,6 +623,8 @@ am_status check_cfg(am_problem *P, const am_simp_config *c) {
         return fail(AM_ERR_INVALID_ARG, "unknown variant");
     if (c->precision != AM_PREC_FP64 && c->precision != AM_PREC_MIXED)
         return fail(AM_ERR_INVALID_ARG, "unknown precision");
+    if (c->mixed_solver != AM_MIXED_RELIABLE && c->mixed_solver != AM_MIXED_FLEXIBLE)
+        return fail(AM_ERR_INVALID_ARG, "unknown mixed_solver");
     if (c->layout != AM_LAYOUT_ZFASTEST && c->layout != AM_LAYOUT_XFASTEST)
         return fail(AM_ERR_INVALID_ARG, "unknown layout");
     if (c->preconditioner != AM_PRECOND_JACOBI && c->preconditioner != AM_PRECOND_LEARNED)

@@ -607,6 +607,16 @@ __global__ void df_compose_kernel(const float *__restrict__ xh, const float *__r
          i += (long long)gridDim.x * blockDim.x)
         x[i] = (double)xh[i] + (double)xl[i];
 }
+__global__ void df_accumulate_kernel(const float *__restrict__ xh, const float *__restrict__ xl,
+                                     double *__restrict__ x, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        x[i] += (double)xh[i] + (double)xl[i];
+}
+cudaError_t df_accumulate(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st) {
+    df_accumulate_kernel<<<nblocks, 256, 0, st>>>(xh, xl, x, n);
+    return counted(cudaGetLastError());
+}
 __global__ void df_split_kernel(const double *__restrict__ x, float *__restrict__ xh, float *__restrict__ xl,
                                 long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;

@@ -102,6 +102,8 @@ cudaError_t l2_flush_read(const void *buf, size_t bytes, cudaStream_t st);
 // x = xh + xl, and (xh, xl) = the double-float split of x (n entries)
 cudaError_t df_compose(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st);
 cudaError_t df_split(const double *x, float *xh, float *xl, long long n, int nblocks, cudaStream_t st);
+// x += xh + xl (n entries)
+cudaError_t df_accumulate(const float *xh, const float *xl, double *x, long long n, int nblocks, cudaStream_t st);
 // (re)start from the residual r (already masked); see pcg_start_kernel
 template <typename T>
 cudaError_t pcg_start(const Layout &L, const T *r, const T *dinv, double thr, double upd_factor, int maxit,

@@ -235,11 +235,15 @@ def run_batch(args, nat, world, rank):
         print(json.dumps(line))
 
 
+MIXED_SOLVER = {"reliable": 0, "flexible": 1}
+_mixed_solver = "reliable"
+
+
 def simp_config(nat, W, max_iterations=100):
     return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
                               precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=0.01,
-                              cg_max_iterations=200000)
+                              cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver])
 
 
 class ClockSampler:
@@ -388,8 +392,13 @@ def main():
     ap.add_argument("--compare-fp64", action="store_true",
                     help="time --steps SIMP iterations in mixed precision and in FP64 plain Jacobi from the same "
                          "start and report the ratio and the compliance / density agreement")
+    ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
+                    help="mixed precision: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
+                         "flexible CG over FP32 inner solves (flexible)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global _mixed_solver
+    _mixed_solver = args.mixed_solver
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -589,7 +598,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
-                       "description": W["desc"], "precision": "mixed", "preconditioner": "jacobi",
+                       "description": W["desc"], "precision": "mixed", "mixed_solver": _mixed_solver, "preconditioner": "jacobi",
                        "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probe flushes L2",
                        "parallelism": f"replicas x{world}"},
             "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,

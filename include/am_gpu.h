@@ -64,13 +64,15 @@ enum { AM_LAYOUT_ZFASTEST = 0, AM_LAYOUT_XFASTEST = 1 };
 enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
 
 /* AM_PREC_FP64: every kernel in FP64 (the parity mode).
- * AM_PREC_MIXED: FP64 flexible CG (outer K*u, vectors, dots) preconditioned by FP32
- *   Jacobi PCG inner solves (FP32 K*u, r and p, FP64 iterate, double-float dot
- *   accumulation); a solve is
+ * AM_PREC_MIXED: FP32 Jacobi PCG (FP32 K*u, r and p, double-float iterate and dot
+ *   accumulation) with FP64 residual replacement (AM_MIXED_RELIABLE, the default), or
+ *   an FP64 flexible CG preconditioned by FP32 Jacobi-PCG inner solves
+ *   (AM_MIXED_FLEXIBLE; always with the learned preconditioner); a solve is
  *   accepted on its recomputed FP64 residual r = f - K u.  Compliance, element
  *   energies, filter and the new densities are FP64; the OC bisection passes run in
  *   double-float. */
 enum { AM_PREC_FP64 = 0, AM_PREC_MIXED = 1 };
+enum { AM_MIXED_RELIABLE = 0, AM_MIXED_FLEXIBLE = 1 };
 
 enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1 };
 
@@ -91,18 +93,22 @@ typedef struct am_simp_config {
     double cg_tol;            /* relative residual ||f - K u|| / ||f|| of every solve */
     int cg_max_iterations;    /* cap on (inner) PCG iterations per solve (100000 by default) */
     int warm_start;           /* 1: each solve starts from the previous displacement */
-    double inner_tol;         /* MIXED: residual reduction of each FP32 inner solve that
-                                 preconditions the FP64 flexible CG; an inner solve stops at
-                                 max(inner_tol |r|, 0.3 cg_tol |f|) (0.01 by default) */
-    int max_outer;            /* MIXED: cap on outer FP64 flexible-CG iterations per solve */
+    double inner_tol;         /* MIXED: residual reduction of the FP32 sequence between two FP64
+                                 residual replacements (RELIABLE), or of each FP32 inner solve
+                                 that preconditions the flexible CG (FLEXIBLE; it stops at
+                                 max(inner_tol |r|, 0.3 cg_tol |f|)); 0.01 by default */
+    int max_outer;            /* MIXED: cap on FP64 replacements / outer flexible-CG iterations
+                                 per solve */
     int layout;               /* AM_LAYOUT_* of density arrays */
     int verbose;
+    int mixed_solver;         /* MIXED with the Jacobi preconditioner: AM_MIXED_* */
 } am_simp_config;
 
 /* Per-solve statistics (SolveStats, linear_solver.hpp:48-56). */
 typedef struct am_solve_stats {
     int iterations;           /* PCG iterations (sum of inner iterations in MIXED) */
-    int outer_iterations;     /* outer FP64 flexible-CG iterations (MIXED), 1 in FP64 */
+    int outer_iterations;     /* MIXED: FP64 residual replacements or outer flexible-CG
+                                 iterations; 1 in FP64 */
     double residual;          /* final ||f - K u|| / ||f||, computed in FP64 */
     int converged;
     double solve_time_s;

@@ -75,13 +75,15 @@ def _cantilever(shape):
     return F, fixed
 
 
-@pytest.mark.parametrize("precision", [nat.PREC_FP64, nat.PREC_MIXED])
-def test_solve_matches_oracle(golden, precision):
+@pytest.mark.parametrize("precision,solver", [(nat.PREC_FP64, 0), (nat.PREC_MIXED, nat.MIXED_RELIABLE),
+                                              (nat.PREC_MIXED, nat.MIXED_FLEXIBLE)])
+def test_solve_matches_oracle(golden, precision, solver):
     shape = tuple(golden["solve_shape"])
     grid = golden["solve_grid"]
     p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=grid)
     p.set_loads([golden["solve_F"]], [golden["solve_fixed"]])
-    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9, precision=precision, cg_tol=1e-9, warm_start=0)
+    cfg = nat.default_config(nat.VARIANT_PY, E_min=1e-9, precision=precision, cg_tol=1e-9, warm_start=0,
+                             mixed_solver=solver)
     u, st = p.solve(cfg, golden["solve_rho"])
     ref = golden["solve_u"]
     assert st.converged and st.residual <= 1e-9
