@@ -439,7 +439,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         // The solve is accepted on the recomputed FP64 residual.
         CKS(ensure_vectors(P, true));
         const int max_rounds = c.max_outer > 0 ? c.max_outer : 200;
-        const double red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
+        const double red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.1;
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
                     want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
         CKS(sync_scalars(P));
@@ -702,7 +702,7 @@ void am_simp_config_default(am_simp_config *c, int variant) {
     c->cg_tol = 1e-6;
     c->cg_max_iterations = 100000;
     c->warm_start = 1;
-    c->inner_tol = 0.01;
+    c->inner_tol = 0.0;  // the solver's own default: 0.1 (reliable updates), 0.01 (flexible CG)
     c->max_outer = 200;
     c->layout = AM_LAYOUT_ZFASTEST;
     c->verbose = 0;

@@ -96,7 +96,8 @@ typedef struct am_simp_config {
     double inner_tol;         /* MIXED: residual reduction of the FP32 sequence between two FP64
                                  residual replacements (RELIABLE), or of each FP32 inner solve
                                  that preconditions the flexible CG (FLEXIBLE; it stops at
-                                 max(inner_tol |r|, 0.3 cg_tol |f|)); 0.01 by default */
+                                 max(inner_tol |r|, 0.3 cg_tol |f|)); <= 0 (the default) picks
+                                 0.1 (RELIABLE) or 0.01 (FLEXIBLE) */
     int max_outer;            /* MIXED: cap on FP64 replacements / outer flexible-CG iterations
                                  per solve */
     int layout;               /* AM_LAYOUT_* of density arrays */
