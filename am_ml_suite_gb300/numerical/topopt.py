@@ -7,8 +7,8 @@ loop runs on the device (variant AM_VARIANT_PY of include/am_gpu.h): density
 pre-filter and clip, per-load-case solve / compliance / sensitivities, the
 normalised reflect-mode cone filter of dc*rho / max(rho, 1e-3), the OC
 bisection with the Python constants.  The direct sparse solve of the reference
-is replaced by PCG to ``cg_tol`` (FP64) or mixed precision with an FP64
-defect-correction loop.
+is replaced by PCG to ``cg_tol`` (FP64) or mixed precision (FP32 PCG with FP64
+residual replacement, every solve accepted on its FP64 residual).
 """
 from __future__ import annotations
 
