@@ -23,7 +23,7 @@ LAYOUT_ZFASTEST, LAYOUT_XFASTEST = 0, 1
 VARIANT_CPP, VARIANT_PY = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 MIXED_RELIABLE, MIXED_FLEXIBLE = 0, 1
-PRECOND_JACOBI, PRECOND_LEARNED = 0, 1
+PRECOND_JACOBI, PRECOND_LEARNED, PRECOND_MG = 0, 1, 2
 
 
 class AmError(RuntimeError):

@@ -14,6 +14,7 @@
 #include "../../include/am_gpu.h"
 #include "host_util.h"
 #include "kernels.cuh"
+#include "mg.h"
 #include "ku.cuh"
 #include "precond.h"
 
@@ -155,6 +156,12 @@ struct am_problem {
     // SIMP state
     bool simp_begun = false;
     am_precond *pre = nullptr;       // learned preconditioner (AM_PRECOND_LEARNED)
+    // multigrid preconditioner (AM_PRECOND_MG): built on first use; nullptr if
+    // the grid does not coarsen far enough
+    Mg *mg = nullptr;
+    bool mg_tried = false;
+    bool mg_dirty = true;  // operator or constraints changed since the last set-up
+    int mg_lc = -1;        // load case whose fixed DOFs the coarse levels carry
     const double *rho_op = nullptr;  // element densities of the current operator
     am_simp_config cfg{};
     double n_design = 0.0;
@@ -256,6 +263,7 @@ am_status setup_operator(am_problem *P, const am_simp_config &c, const double *r
     const int8_t *g = (variant == AM_VARIANT_PY && !P->grid_host.empty()) ? P->grid.p : nullptr;
     CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st));
     P->pad_dirty = true;
+    P->mg_dirty = true;
     return AM_OK;
 }
 
@@ -263,6 +271,7 @@ am_status setup_mask(am_problem *P, int lc) {
     const uint8_t *fb = (lc >= 0 && lc < (int)P->cases.size()) ? P->cases[lc].fixed_bits.p : nullptr;
     CK(diag_mask(P->L, P->s64.p, P->ke00, fb, P->dinv64.p, P->dinv32.p, P->mask.p, P->st));
     P->pad_dirty = true;
+    P->mg_dirty = true;
     return AM_OK;
 }
 
@@ -380,6 +389,32 @@ am_status inner_iterate_to_fp64(am_problem *P) {
     return AM_OK;
 }
 
+// The multigrid hierarchy for the current operator and load case lc: true when
+// it is ready, false when the grid does not coarsen far enough (the solve then
+// uses the Jacobi path).
+am_status mg_ready(am_problem *P, int lc, bool *ok) {
+    *ok = false;
+    if (!P->mg_tried) {
+        P->mg_tried = true;
+        cudaError_t e = cudaSuccess;
+        P->mg = mg_create(P->L, P->E0, P->nu, P->h, &e);
+        if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,
+                                          std::string("multigrid levels: ") + cudaGetErrorString(e));
+    }
+    if (!P->mg) return AM_OK;
+    if (P->mg_dirty || P->mg_lc != lc) {
+        CKS(ensure_vectors(P, false));
+        const cudaError_t e = mg_setup(P->mg, P->s64.p, P->s32.p, P->dinv32.p, P->mask.p, P->cases[lc].fixed_bits.p,
+                                       P->st);
+        if (e == cudaErrorInvalidValue) return fail(AM_ERR_SINGULAR, "multigrid coarsest matrix is not positive definite");
+        CK(e);
+        P->mg_dirty = false;
+        P->mg_lc = lc;
+    }
+    *ok = true;
+    return AM_OK;
+}
+
 struct SolveOut {
     int iterations = 0, outer = 0, converged = 0, learned = 0;
     double residual = 0.0, time_s = 0.0;
@@ -410,7 +445,9 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
     const double tol = c.cg_tol;
     const int maxit = c.cg_max_iterations > 0 ? c.cg_max_iterations : 100000;
     const bool learned0 = c.preconditioner == AM_PRECOND_LEARNED && P->pre;
-    if (fp64 && !learned0) {
+    bool mg0 = false;
+    if (c.preconditioner == AM_PRECOND_MG) CKS(mg_ready(P, lc, &mg0));
+    if (fp64 && !learned0 && !mg0) {
         CK(cudaMemcpyAsync(P->xw64.p, C.x64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p,
                     P->r64.p, nullptr, P->partial.p, P->S, P->st));
@@ -428,7 +465,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         o.residual = std::sqrt(P->Sh->res_rr / bnorm2);
         o.converged = (stt == ST_CONVERGED) ? 1 : 0;
         if (stt == ST_NAN) return fail(AM_ERR_NAN_DETECTED, "NaN in the PCG iteration");
-    } else if (!learned0 && c.mixed_solver == AM_MIXED_RELIABLE) {
+    } else if (!learned0 && !mg0 && c.mixed_solver == AM_MIXED_RELIABLE) {
         // Mixed precision, one FP32 Jacobi-PCG sequence with reliable updates
         // (residual replacement, van der Vorst and Ye): the FP32 iteration runs
         // until its recursive residual has fallen by inner_tol; then the
@@ -490,6 +527,10 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         // solve; if the outer residual stops falling (< 10 % over 5 outer
         // iterations) the solve continues with Jacobi PCG alone
         bool learned = learned0;
+        // multigrid likewise: a V-cycle whose coarse grids do not represent the
+        // operator (rediscretisation of a rough density field) stops helping; the
+        // solve then continues with Jacobi-PCG inner solves
+        bool mg_on = mg0;
         std::vector<double> hist;
         const int max_outer = c.max_outer > 0 ? c.max_outer : 200;
         const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
@@ -525,6 +566,11 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                     CKS(inner_iterate_to_fp64(P));
                     total += its;
                 }
+            } else if (mg_on) {
+                // z = M(r): one FP32 multigrid V-cycle
+                CK(mg_apply(P->mg, P->r64.p, P->xi64.p, P->st));
+                its = 1;
+                total += its;
             } else {
                 // z = M(r): FP32 PCG (FP64 iterate) on K z = r from zero, to
                 // inner_tol of |r| but not below 0.3 tol |f| (the overall goal)
@@ -565,6 +611,9 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 ++o.learned;
                 hist.push_back(rel);
                 if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) learned = false;  // Jacobi from here
+            } else if (mg_on) {
+                hist.push_back(rel);
+                if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) mg_on = false;  // Jacobi from here
             }
             if (rel <= tol) {
                 // accept on the recomputed FP64 residual (and element energies)
@@ -627,7 +676,8 @@ am_status check_cfg(am_problem *P, const am_simp_config *c) {
         return fail(AM_ERR_INVALID_ARG, "unknown mixed_solver");
     if (c->layout != AM_LAYOUT_ZFASTEST && c->layout != AM_LAYOUT_XFASTEST)
         return fail(AM_ERR_INVALID_ARG, "unknown layout");
-    if (c->preconditioner != AM_PRECOND_JACOBI && c->preconditioner != AM_PRECOND_LEARNED)
+    if (c->preconditioner != AM_PRECOND_JACOBI && c->preconditioner != AM_PRECOND_LEARNED &&
+        c->preconditioner != AM_PRECOND_MG)
         return fail(AM_ERR_INVALID_ARG, "unknown preconditioner");
     if (c->preconditioner == AM_PRECOND_LEARNED && !P->pre)
         return fail(AM_ERR_INVALID_ARG, "AM_PRECOND_LEARNED needs am_problem_set_preconditioner");
@@ -804,6 +854,8 @@ am_status am_problem_destroy(am_problem *P) {
     P->oc_a32.release(); P->oc_lo32.release(); P->oc_hi32.release();
     DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->xl32, &P->r32, &P->p32a, &P->p32b, &P->q32v, &P->s32pad};
     P->maskpad.release();
+    mg_destroy(P->mg);
+    P->mg = nullptr;
     ku3_free_maps(P->maps3);
     P->maps3 = nullptr;
     P->xi64.release();

@@ -236,15 +236,18 @@ def run_batch(args, nat, world, rank):
 
 
 MIXED_SOLVER = {"reliable": 0, "flexible": 1}
+PRECOND = {"jacobi": 0, "mg": 2}
 _mixed_solver = "reliable"
 _inner_tol = 0.0
+_precond = "jacobi"
 
 
 def simp_config(nat, W, max_iterations=100):
     return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
                               precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=_inner_tol,
-                              cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver])
+                              cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver],
+                              preconditioner=PRECOND[_precond])
 
 
 class ClockSampler:
@@ -396,14 +399,17 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=0.0,
                     help="mixed precision: residual reduction between FP64 replacements / per inner solve "
                          "(0: the solver's default, 0.1 reliable / 0.01 flexible)")
+    ap.add_argument("--precond", default="jacobi", choices=sorted(PRECOND),
+                    help="jacobi: Jacobi PCG (the headline); mg: multigrid V-cycle in the FP64 flexible CG")
     ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
                     help="mixed precision: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
                          "flexible CG over FP32 inner solves (flexible)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global _mixed_solver, _inner_tol
+    global _mixed_solver, _inner_tol, _precond
     _mixed_solver = args.mixed_solver
     _inner_tol = args.inner_tol
+    _precond = args.precond
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -599,13 +605,15 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": "SIMP iters/s @ rel-res 1e-6 (Jacobi PCG); PCG solve ms in pcg_solve_ms",
+            "metric": ("SIMP iters/s @ rel-res 1e-6 (Jacobi PCG); PCG solve ms in pcg_solve_ms" if _precond == "jacobi"
+                       else "SIMP iters/s @ rel-res 1e-6 (multigrid-preconditioned flexible CG); solve ms in "
+                            "pcg_solve_ms"),
             "value": value, "unit": "SIMP iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
-                       "description": W["desc"], "precision": "mixed", "mixed_solver": _mixed_solver, "preconditioner": "jacobi",
+                       "description": W["desc"], "precision": "mixed", "mixed_solver": _mixed_solver, "preconditioner": _precond,
                        "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probe flushes L2",
                        "parallelism": f"replicas x{world}"},
             "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,

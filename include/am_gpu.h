@@ -74,7 +74,14 @@ enum { AM_VARIANT_CPP = 0, AM_VARIANT_PY = 1 };
 enum { AM_PREC_FP64 = 0, AM_PREC_MIXED = 1 };
 enum { AM_MIXED_RELIABLE = 0, AM_MIXED_FLEXIBLE = 1 };
 
-enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1 };
+/* AM_PRECOND_JACOBI: the diagonal; AM_PRECOND_LEARNED: the network of
+ * am_problem_set_preconditioner; AM_PRECOND_MG: a geometric multigrid V-cycle (FP32;
+ * rediscretised coarse grids of averaged element scales, trilinear transfers,
+ * damped-Jacobi smoothing, dense coarsest solve) inside the FP64 flexible CG, for
+ * grids whose dimensions halve down to at most 1000 coarse DOFs -- other grids
+ * solve with the Jacobi path.  In place of the reference's IncompleteCholesky
+ * (linear_solver.cpp:133-140). */
+enum { AM_PRECOND_JACOBI = 0, AM_PRECOND_LEARNED = 1, AM_PRECOND_MG = 2 };
 
 /* SIMP configuration: SIMPConfig (topology_optimizer.hpp:49-59) + SIMPParams
  * (topopt.py:30-52) + the solver knobs of SolverConfig (linear_solver.hpp:66-75). */
