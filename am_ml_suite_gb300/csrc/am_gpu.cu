@@ -531,6 +531,9 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         // operator (rediscretisation of a rough density field) stops helping; the
         // solve then continues with Jacobi-PCG inner solves
         bool mg_on = mg0;
+        // with the V-cycle the outer product K p runs in FP32 until the FP32
+        // rounding of K p stalls the residual (near 1e-7 relative), then in FP64
+        bool mg_f32 = mg0;
         std::vector<double> hist;
         const int max_outer = c.max_outer > 0 ? c.max_outer : 200;
         const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
@@ -593,8 +596,12 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             CK(fcg_dots(P->L, P->xi64.p, P->r64.p, P->q64v.p, outer == 0 ? 1 : 0, P->partial.p, P->S,
                         P->nblocks_vec, P->st));
             CK(fcg_direction(P->L, P->xi64.p, P->p64a.p, P->S, P->nblocks_vec, P->st));
-            CK(ku_dot(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p, P->S,
-                      P->st));
+            if (mg_on && mg_f32)  // the V-cycle is FP32: its outer product need not be FP64 either
+                CK(ku_dot_f32(P->plan32, P->L, P->M32, P->s32.p, P->p64a.p, P->mask.p, P->x32.p, P->q32v.p,
+                              P->q64v.p, P->partial.p, P->S, P->nblocks_vec, P->st));
+            else
+                CK(ku_dot(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p, P->S,
+                          P->st));
             CK(fcg_update(P->L, C.x64.p, P->r64.p, P->p64a.p, P->q64v.p, P->partial.p, P->S, P->nblocks_vec,
                           P->st));
             CKS(sync_scalars(P));
@@ -613,7 +620,13 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) learned = false;  // Jacobi from here
             } else if (mg_on) {
                 hist.push_back(rel);
-                if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) mg_on = false;  // Jacobi from here
+                if (hist.size() > 5 && rel > 0.9 * hist[hist.size() - 6]) {
+                    if (mg_f32)
+                        mg_f32 = false;  // FP64 outer product from here
+                    else
+                        mg_on = false;  // Jacobi from here
+                    hist.clear();
+                }
             }
             if (rel <= tol) {
                 // accept on the recomputed FP64 residual (and element energies)

@@ -243,6 +243,58 @@ cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, c
     return dispatch_ku<double, KU_DOT>(K, a, st);
 }
 
+// q = mask(q32) in FP64 and p.q -> S->o_pq, S->o_alpha (the finish of KU_DOT)
+__global__ void __launch_bounds__(256) dot_from_f32_kernel(Layout L, const double *__restrict__ p,
+                                                          const float *__restrict__ q32,
+                                                          const uint8_t *__restrict__ mask, double *__restrict__ q,
+                                                          double *partial, Scalars *S) {
+    __shared__ double red[8];
+    __shared__ int last_flag;
+    double acc = 0.0;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < L.cs;
+         n += (long long)gridDim.x * blockDim.x) {
+        const unsigned m = mask[n];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long i = n + c * L.cs;
+            const double v = ((m >> c) & 1u) ? 0.0 : (double)q32[i];
+            q[i] = v;
+            acc = fma(p[i], v, acc);
+        }
+    }
+    double v[1] = {acc};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partial[2 * blockIdx.x] = v[0];
+    if (!arrive_last(&S->cnt_ku, &last_flag)) return;
+    double tot[1];
+    reduce_partials<1>(partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) {
+        const double pq = tot[0];
+        S->o_pq = pq;
+        if (!(pq > 0.0) || !isfinite(pq)) {
+            S->o_status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+            S->o_alpha = 0.0;
+        } else {
+            S->o_alpha = S->o_zr / pq;
+        }
+        S->cnt_ku = 0;
+    }
+}
+__global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+cudaError_t ku_dot_f32(const KuLaunch &K32, const Layout &L, const Modal<float> &M, const float *s32, const double *p,
+                       const uint8_t *mask, float *p32, float *q32, double *q, double *partial, Scalars *S,
+                       int nblocks, cudaStream_t st) {
+    f64_to_f32_kernel<<<nblocks, 256, 0, st>>>(p, p32, 3 * L.cs);
+    cudaError_t e = counted(cudaGetLastError());
+    if (e == cudaSuccess) e = ku_plain<float>(K32, L, M, s32, p32, q32, st);
+    if (e != cudaSuccess) return e;
+    dot_from_f32_kernel<<<nblocks, 256, 0, st>>>(L, p, q32, mask, q, partial, S);
+    return counted(cudaGetLastError());
+}
+
 template cudaError_t ku_plain<float>(const KuLaunch &, const Layout &, const Modal<float> &,
                                      const float *, const float *, float *, cudaStream_t);
 template cudaError_t ku_plain<double>(const KuLaunch &, const Layout &, const Modal<double> &,

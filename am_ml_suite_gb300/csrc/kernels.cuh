@@ -129,6 +129,11 @@ cudaError_t fcg_direction(const Layout &L, const double *z, double *p, const Sca
                           cudaStream_t st);
 cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
                    const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st);
+// the same q = mask(K p), p.q -> S->o_pq / o_alpha with the product in FP32
+// (p rounded into p32, K p into q32, q and the dot in FP64)
+cudaError_t ku_dot_f32(const KuLaunch &K32, const Layout &L, const Modal<float> &M, const float *s32, const double *p,
+                       const uint8_t *mask, float *p32, float *q32, double *q, double *partial, Scalars *S,
+                       int nblocks, cudaStream_t st);
 cudaError_t fcg_update(const Layout &L, double *x, double *r, const double *p, const double *q, double *partial,
                        Scalars *S, int nblocks, cudaStream_t st);
 
