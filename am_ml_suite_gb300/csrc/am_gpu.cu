@@ -1284,6 +1284,20 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
     run.it = 0;
     CK(cudaMemcpyAsync(P->S, &run, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
     CKS(ku3_ready(P));
+    // filter (8) and OC pass (9) time the mixed-precision forms on the state the
+    // last SIMP step left (densities, sensitivities, design mask, filter taps)
+    const am_simp_config &cf = P->cfg;
+    OcBuffers ocb{P->L.nel, P->oc_a64.p, P->oc_lo64.p, P->oc_hi64.p, P->oc_a32.p, P->oc_lo32.p, P->oc_hi32.p};
+    if (which == 8 || which == 9) {
+        if (P->iter < 1) return fail(AM_ERR_INVALID_ARG, "the filter / OC probes need a SIMP step first");
+        CKS(build_taps(P, cf.filter_radius, cf.variant));
+    }
+    if (which == 9) {
+        const size_t ne = (size_t)P->L.nel;
+        CK(P->oc_a32.alloc(ne)); CK(P->oc_lo32.alloc(ne)); CK(P->oc_hi32.alloc(ne));
+        ocb = OcBuffers{P->L.nel, P->oc_a64.p, P->oc_lo64.p, P->oc_hi64.p, P->oc_a32.p, P->oc_lo32.p, P->oc_hi32.p};
+        CK(oc_prepare(ocb, P->rho.p, P->dcf.p, cf.move_limit, 0, cf.variant, P->S, P->st));
+    }
     DevBuf<uint8_t> flush;
     const size_t flush_bytes = 512ull << 20;
     if (flush_l2) CK(flush.alloc(flush_bytes));
@@ -1330,6 +1344,16 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
             case 5:
                 CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 3, P->st));
                 break;
+            case 8:  // the SIMP loop's FP64 shared-memory stencil
+                CK(filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));
+                break;
+            case 9: {
+                const int zero = 0;
+                CK(cudaMemcpyAsync(&P->S->oc_done, &zero, sizeof(int), cudaMemcpyHostToDevice, P->st));
+                CK(oc_pass(ocb, P->design.p, 0, cf.variant, cf.rho_min, cf.volume_fraction, P->n_design,
+                           P->partial.p, P->S, P->nblocks_vec, P->st));
+                break;
+            }
             default:
                 return fail(AM_ERR_INVALID_ARG, "unknown kernel id");
         }

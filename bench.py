@@ -390,7 +390,7 @@ def main():
     ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS) + ["batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd"],
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd", "filter", "oc"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--compare-fp64", action="store_true",
@@ -506,7 +506,10 @@ def main():
         p.simp_begin(cfg, W["rho0"])
         # ku: the staged PCG K*u the solver runs; ku2: the register-direct kernel it
         # replaced; ku3s3: the staged kernel with 3 stages instead of 4
-        which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7}[args.probe]
+        which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7,
+                 "filter": 8, "oc": 9}[args.probe]
+        if which >= 8:
+            p.simp_step()  # the filter and OC probes time the state a SIMP step leaves
         avg, mn = p.bench_kernel(which, reps=args.reps, flush_l2=True)
         lay = p.layout_info()
         p.close()

@@ -253,7 +253,9 @@ long long am_launch_count(void);
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
  * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
- * and folded iterate) iteration.  flush_l2 != 0 overwrites a 512 MB buffer before each
+ * and folded iterate) iteration, 8 the C++ cone sensitivity filter
+ * (shared-memory stencil), 9 one OC bisection pass (double-float) -- these two
+ * on the state of the last am_simp_step.  flush_l2 != 0 overwrites a 512 MB buffer before each
  * launch so the kernel reads from HBM, then reads that buffer back so the write's
  * dirty L2 lines are written back before the timed launch.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
