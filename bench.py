@@ -393,6 +393,9 @@ def main():
     ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd", "filter", "oc"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--compare-mg", action="store_true",
+                    help="time --steps SIMP iterations with the Jacobi and the multigrid mixed-precision solvers "
+                         "from the same start and report the ratio and the compliance / density agreement")
     ap.add_argument("--compare-fp64", action="store_true",
                     help="time --steps SIMP iterations in mixed precision and in FP64 plain Jacobi from the same "
                          "start and report the ratio and the compliance / density agreement")
@@ -449,6 +452,40 @@ def main():
         return
     shape = W["shape"]
     cfg = simp_config(nat, W)
+
+    if args.compare_mg:
+        import torch
+
+        out = {}
+        for name, pc in (("jacobi", nat.PRECOND_JACOBI), ("mg", nat.PRECOND_MG)):
+            p = nat.Problem(shape, 1.0, 1.0, 0.3)
+            p.set_loads([W["F"]], [W["fixed"]])
+            c = simp_config(nat, W, max_iterations=args.steps)
+            c.preconditioner = pc
+            p.simp_begin(c, W["rho0"])
+            st = torch.cuda.ExternalStream(p.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            res = [p.simp_step() for _ in range(args.steps)]
+            e1.record(st)
+            torch.cuda.synchronize()
+            out[name] = dict(s=e0.elapsed_time(e1) * 1e-3, comp=np.array([r.compliance for r in res]),
+                             its=[r.solver_iterations for r in res], res=max(r.solver_residual for r in res),
+                             rho=p.simp_density())
+            p.close()
+        j, m = out["jacobi"], out["mg"]
+        rel = np.abs(m["comp"] - j["comp"]) / np.abs(j["comp"])
+        print(json.dumps({
+            "metric": "SIMP s/iteration: mixed precision, multigrid vs Jacobi preconditioner, same GPU",
+            "workload": args.workload, "steps": args.steps, "jacobi_s_per_step": j["s"] / args.steps,
+            "mg_s_per_step": m["s"] / args.steps, "speedup": j["s"] / m["s"],
+            "compliance_rel_diff_max": float(rel.max()), "compliance_rel_diff_final": float(rel[-1]),
+            "compliance_final": float(j["comp"][-1]),
+            "density_max_abs_diff": float(np.max(np.abs(m["rho"] - j["rho"]))),
+            "pcg_iterations_jacobi_mean": float(np.mean(j["its"])), "pcg_iterations_mg_mean": float(np.mean(m["its"])),
+            "residual_max": max(j["res"], m["res"])}))
+        return
 
     if args.compare_fp64:
         import torch
