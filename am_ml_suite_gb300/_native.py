@@ -162,6 +162,7 @@ SIGNATURES = {
     "am_simp_step": (ctypes.c_int, [_vp, ctypes.POINTER(IterationResult)]),
     "am_simp_get_density": (ctypes.c_int, [_vp, _dp]),
     "am_launch_count": (ctypes.c_longlong, []),
+    "am_selftest_copy_wait": (ctypes.c_int, [ctypes.c_double, _ip, _dp]),
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "am_problem_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "am_precond_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_longlong, ctypes.POINTER(_vp)]),
@@ -640,3 +641,11 @@ def write_metadata_json(path, **fields):
 
 def launch_count() -> int:
     return int(load().am_launch_count())
+
+
+def selftest_copy_wait(limit_ms: float = 5.0):
+    """Runs the bounded copy-wait self-test: (timed_out, waited_ms)."""
+    t = ctypes.c_int(0)
+    w = ctypes.c_double(0.0)
+    check(load().am_selftest_copy_wait(float(limit_ms), ctypes.byref(t), ctypes.byref(w)), "am_selftest_copy_wait")
+    return bool(t.value), w.value

@@ -46,12 +46,13 @@ __device__ __forceinline__ unsigned long long now_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// waits for phase `parity` of `bar`; false after one second without it
-__device__ __forceinline__ bool bar_wait(uint64_t *bar, unsigned parity) {
+// waits for phase `parity` of `bar`; false after `limit_ns` (one second) without it
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, unsigned parity,
+                                         unsigned long long limit_ns = 1000000000ull) {
     if (bar_try(bar, parity)) return true;
     const unsigned long long t0 = now_ns();
     while (!bar_try(bar, parity))
-        if (now_ns() - t0 > 1000000000ull) return false;
+        if (now_ns() - t0 > limit_ns) return false;
     return true;
 }
 

@@ -242,6 +242,14 @@ am_status am_simp_get_density(am_problem *p, double *rho_out);
 /* ---- measurement (no counterpart in the reference, whose timers are the
  * std::chrono phase times of IterationResult, topology_optimizer.hpp:65-74) ---- */
 
+/* Self-test of the bounded copy waits (no reference counterpart).  Every stage
+ * of the solver's copy pipelines waits on its barrier for at most one second and
+ * then ends the solve with an error instead of spinning; this launches one
+ * thread that waits, with the same code shortened to limit_ms (0 < limit_ms <=
+ * 100), on a barrier that nothing completes.  *timed_out = 1 and *waited_ms about
+ * limit_ms when the wait gave up as it should. */
+am_status am_selftest_copy_wait(double limit_ms, int *timed_out, double *waited_ms);
+
 /* Kernel launches this library has issued so far (CUDA-graph replays add the
  * kernel nodes they contain). */
 long long am_launch_count(void);
