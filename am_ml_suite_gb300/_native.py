@@ -58,6 +58,7 @@ class SimpConfig(ctypes.Structure):
         ("layout", ctypes.c_int),
         ("verbose", ctypes.c_int),
         ("mixed_solver", ctypes.c_int),
+        ("mg_deflation", ctypes.c_int),
     ]
 
 

@@ -14,6 +14,7 @@
 #include "../../include/am_gpu.h"
 #include "host_util.h"
 #include "kernels.cuh"
+#include "defl.h"
 #include "mg.h"
 #include "ku.cuh"
 #include "precond.h"
@@ -162,6 +163,11 @@ struct am_problem {
     bool mg_tried = false;
     bool mg_dirty = true;  // operator or constraints changed since the last set-up
     int mg_lc = -1;        // load case whose fixed DOFs the coarse levels carry
+    // rigid-body deflation of the passive solid inclusions around the V-cycle:
+    // built on first use after the design mask is known; nullptr if there is none
+    Defl *defl = nullptr;
+    bool defl_tried = false;
+    bool defl_set = false;  // set up for the current operator and load case
     const double *rho_op = nullptr;  // element densities of the current operator
     am_simp_config cfg{};
     double n_design = 0.0;
@@ -392,7 +398,25 @@ am_status inner_iterate_to_fp64(am_problem *P) {
 // The multigrid hierarchy for the current operator and load case lc: true when
 // it is ready, false when the grid does not coarsen far enough (the solve then
 // uses the Jacobi path).
-am_status mg_ready(am_problem *P, int lc, bool *ok) {
+// Passive solid elements (held at density 1 by the design mask: CPP elements whose
+// initial density is >= 0.99, PY grid == 1; outside a SIMP run, grid == 1).
+am_status passive_solid(am_problem *P, std::vector<uint8_t> &solid) {
+    const size_t nel = (size_t)P->L.nel;
+    solid.assign(nel, 0);
+    if (P->simp_begun) {
+        std::vector<uint8_t> dm(nel);
+        std::vector<double> rho(nel);
+        CK(cudaMemcpyAsync(dm.data(), P->design.p, nel, cudaMemcpyDeviceToHost, P->st));
+        CK(cudaMemcpyAsync(rho.data(), P->rho.p, sizeof(double) * nel, cudaMemcpyDeviceToHost, P->st));
+        CK(cudaStreamSynchronize(P->st));
+        for (size_t e = 0; e < nel; ++e) solid[e] = !dm[e] && rho[e] >= 0.99;
+    } else if (!P->grid_host.empty()) {
+        for (size_t e = 0; e < nel; ++e) solid[e] = P->grid_host[e] == 1;
+    }
+    return AM_OK;
+}
+
+am_status mg_ready(am_problem *P, int lc, bool deflate, bool *ok) {
     *ok = false;
     if (!P->mg_tried) {
         P->mg_tried = true;
@@ -410,6 +434,22 @@ am_status mg_ready(am_problem *P, int lc, bool *ok) {
         CK(e);
         P->mg_dirty = false;
         P->mg_lc = lc;
+        P->defl_set = false;
+    }
+    if (deflate && !P->defl_tried) {
+        P->defl_tried = true;
+        std::vector<uint8_t> solid;
+        CKS(passive_solid(P, solid));
+        cudaError_t e = cudaSuccess;
+        P->defl = defl_create(P->L, solid.data(), &e);
+        if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA,
+                                          std::string("deflation space: ") + cudaGetErrorString(e));
+        P->defl_set = false;
+    }
+    if (deflate && P->defl && !P->defl_set) {
+        CKS(ensure_vectors(P, true));
+        CK(defl_setup(P->defl, P->plan64, P->M64, P->s64.p, P->mask.p, P->p64a.p, P->q64v.p, P->st));
+        P->defl_set = true;
     }
     *ok = true;
     return AM_OK;
@@ -446,7 +486,8 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
     const int maxit = c.cg_max_iterations > 0 ? c.cg_max_iterations : 100000;
     const bool learned0 = c.preconditioner == AM_PRECOND_LEARNED && P->pre;
     bool mg0 = false;
-    if (c.preconditioner == AM_PRECOND_MG) CKS(mg_ready(P, lc, &mg0));
+    if (c.preconditioner == AM_PRECOND_MG) CKS(mg_ready(P, lc, c.mg_deflation != 0, &mg0));
+    Defl *defl = (mg0 && c.mg_deflation) ? P->defl : nullptr;
     if (fp64 && !learned0 && !mg0) {
         CK(cudaMemcpyAsync(P->xw64.p, C.x64.p, sizeof(double) * 3 * P->L.cs, cudaMemcpyDeviceToDevice, P->st));
         CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, P->xw64.p, C.F.p, P->dinv64.p, P->mask.p,
@@ -570,8 +611,10 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                     total += its;
                 }
             } else if (mg_on) {
-                // z = M(r): one FP32 multigrid V-cycle
-                CK(mg_apply(P->mg, P->r64.p, P->xi64.p, P->st));
+                // z = M(r): one FP32 multigrid V-cycle, balanced by the rigid-body
+                // modes of the passive solid inclusions when there are any
+                if (defl) CK(defl_apply(defl, P->mg, P->r64.p, P->xi64.p, P->xw64.p, P->st));
+                else CK(mg_apply(P->mg, P->r64.p, P->xi64.p, P->st));
                 its = 1;
                 total += its;
             } else {
@@ -612,8 +655,11 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             }
             rel = std::sqrt(P->Sh->o_rr / bnorm2);
             if (c.verbose >= 2)
-                std::printf("  outer %d: %s %d (total %d) rel-res %.3e\n", outer, learned ? "learned" : "inner", its,
-                            total, rel);
+                std::printf("  outer %d: %s %d (total %d) rel-res %.3e\n", outer,
+                            learned  ? "learned"
+                            : mg_on ? (mg_f32 ? "v-cycle, fp32 K p" : "v-cycle, fp64 K p")
+                                     : "inner",
+                            its, total, rel);
             if (learned) {
                 ++o.learned;
                 hist.push_back(rel);
@@ -769,6 +815,7 @@ void am_simp_config_default(am_simp_config *c, int variant) {
     c->max_outer = 200;
     c->layout = AM_LAYOUT_ZFASTEST;
     c->verbose = 0;
+    c->mg_deflation = 1;
 }
 
 am_status am_element_stiffness(double E, double nu, double h, double *ke) {
@@ -868,6 +915,7 @@ am_status am_problem_destroy(am_problem *P) {
     DevBuf<float> *d32[] = {&P->s32, &P->dinv32, &P->x32, &P->xl32, &P->r32, &P->p32a, &P->p32b, &P->q32v, &P->s32pad};
     P->maskpad.release();
     mg_destroy(P->mg);
+    defl_destroy(P->defl);
     P->mg = nullptr;
     ku3_free_maps(P->maps3);
     P->maps3 = nullptr;
@@ -1179,6 +1227,10 @@ am_status am_simp_begin(am_problem *P, const am_simp_config *cfg, const double *
     CKS(build_taps(P, cfg->filter_radius, cfg->variant == AM_VARIANT_CPP ? 0 : 1));
     for (auto &c : P->cases) c.have_x = false;
     CK(cudaStreamSynchronize(P->st));
+    // a new design mask: the passive solid inclusions are found again on first use
+    defl_destroy(P->defl);
+    P->defl = nullptr;
+    P->defl_tried = false;
     P->simp_begun = true;
     P->iter = 0;
     return AM_OK;

@@ -1,0 +1,389 @@
+// defl.cu -- rigid-body deflation of stiff passive inclusions (see defl.h).
+//
+// Deflation with rigid-body modes: Jonsthovel, van Gijzen, Vuik, Scarpas, "On the
+// use of rigid body modes in the deflated preconditioned conjugate gradient
+// method", SIAM J. Sci. Comput. 35 (2013).  Balancing form of the two-level
+// preconditioner: Tang, Nabben, Vuik, Erlangga, "Comparison of two-level
+// preconditioners derived from deflation, domain decomposition and multigrid
+// methods", J. Sci. Comput. 39 (2009).
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "defl.h"
+
+namespace amk {
+
+namespace {
+
+constexpr int DEFL_THREADS = 256;
+constexpr int DEFL_MERGE = 3;  // components closer than this many elements are merged
+
+inline int blocks_for(long long n) {
+    return (int)std::max<long long>(1, std::min<long long>((n + DEFL_THREADS - 1) / DEFL_THREADS, 152 * 8));
+}
+
+// z[t][k][u] = z0[t][k][u] on free DOFs, 0 on constrained / orphan ones
+__global__ void defl_mask_kernel(long long nU, const long long *__restrict__ unode, const uint8_t *__restrict__ mask,
+                                 const double *__restrict__ z0, double *__restrict__ z) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const unsigned m = mask[unode[u]];
+#pragma unroll
+        for (int t = 0; t < 6; ++t)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const long long i = (t * 3 + k) * nU + u;
+                z[i] = ((m >> k) & 1u) ? 0.0 : z0[i];
+            }
+    }
+}
+
+// v[k cs + node(u)] = z[t][k][u]: mode t of every component, one full-grid vector
+__global__ void defl_spread_kernel(long long nU, long long cs, const long long *__restrict__ unode,
+                                   const double *__restrict__ z, int t, double *__restrict__ v) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long n = unode[u];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[k * cs + n] = z[(t * 3 + k) * nU + u];
+    }
+}
+
+// kz[t][k][u] = (K v)[k cs + node(u)] on free DOFs, 0 on constrained ones
+__global__ void defl_gather_kernel(long long nU, long long cs, const long long *__restrict__ unode,
+                                   const uint8_t *__restrict__ mask, const double *__restrict__ w, int t,
+                                   double *__restrict__ kz) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long n = unode[u];
+        const unsigned m = mask[n];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) kz[(t * 3 + k) * nU + u] = ((m >> k) & 1u) ? 0.0 : w[k * cs + n];
+    }
+}
+
+// s[6 c + t] = sum over component c's support of V[t] . x ; one block per (c, t)
+__global__ void __launch_bounds__(DEFL_THREADS)
+    defl_dots_kernel(long long nU, long long cs, const long long *__restrict__ off,
+                     const long long *__restrict__ unode, const double *__restrict__ V, const double *__restrict__ x,
+                     double *__restrict__ s) {
+    __shared__ double red[DEFL_THREADS / 32];
+    const int c = blockIdx.x / 6, t = blockIdx.x - 6 * c;
+    double acc = 0.0;
+    for (long long u = off[c] + threadIdx.x; u < off[c + 1]; u += DEFL_THREADS) {
+        const long long n = unode[u];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc = fma(V[(t * 3 + k) * nU + u], x[k * cs + n], acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < DEFL_THREADS / 32; ++w) tot += red[w];
+        s[blockIdx.x] = tot;
+    }
+}
+
+// out = E^-1 s (block c: E_c^-1 s[6c .. 6c+5]), or base - E^-1 s when base is given
+__global__ void defl_solve_kernel(int nm, const double *__restrict__ einv, const double *__restrict__ s,
+                                  const double *__restrict__ base, double *__restrict__ out) {
+    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int c = i / 6, t = i - 6 * c;
+        double v = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) v = fma(einv[(c * 6 + t) * 6 + j], s[c * 6 + j], v);
+        out[i] = base ? base[i] - v : v;
+    }
+}
+
+// x[k cs + node(u)] += sign * sum_t V[t][k][u] coef[6 comp(u) + t]
+__global__ void defl_scatter_kernel(long long nU, long long cs, const long long *__restrict__ unode,
+                                    const int *__restrict__ ucomp, const double *__restrict__ V,
+                                    const double *__restrict__ coef, double sign, double *__restrict__ x) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long n = unode[u];
+        const double *cf = coef + 6 * ucomp[u];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double v = 0.0;
+#pragma unroll
+            for (int t = 0; t < 6; ++t) v = fma(V[(t * 3 + k) * nU + u], cf[t], v);
+            x[k * cs + n] = fma(sign, v, x[k * cs + n]);
+        }
+    }
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(T));
+    return e;
+}
+
+// Cholesky inverse of the 6 x 6 SPD matrix a (row-major) in place; false if a
+// pivot is not positive
+bool inverse6(double *a) {
+    double l[36] = {}, li[36] = {};
+    for (int j = 0; j < 6; ++j) {
+        double d = a[j * 6 + j];
+        for (int k = 0; k < j; ++k) d -= l[j * 6 + k] * l[j * 6 + k];
+        if (!(d > 0.0) || !std::isfinite(d)) return false;
+        d = std::sqrt(d);
+        l[j * 6 + j] = d;
+        for (int i = j + 1; i < 6; ++i) {
+            double s = a[i * 6 + j];
+            for (int k = 0; k < j; ++k) s -= l[i * 6 + k] * l[j * 6 + k];
+            l[i * 6 + j] = s / d;
+        }
+    }
+    for (int j = 0; j < 6; ++j) {
+        li[j * 6 + j] = 1.0 / l[j * 6 + j];
+        for (int i = j + 1; i < 6; ++i) {
+            double s = 0.0;
+            for (int k = j; k < i; ++k) s -= l[i * 6 + k] * li[k * 6 + j];
+            li[i * 6 + j] = s / l[i * 6 + i];
+        }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double s = 0.0;
+            for (int k = std::max(i, j); k < 6; ++k) s += li[k * 6 + i] * li[k * 6 + j];
+            a[i * 6 + j] = s;
+        }
+    return true;
+}
+
+}  // namespace
+
+struct Defl {
+    Layout L;
+    int ncomp = 0;
+    long long nU = 0;                 // support nodes of all components
+    std::vector<long long> off_h;     // component c owns entries [off[c], off[c+1])
+    long long *off = nullptr;
+    long long *unode = nullptr;       // device node index of each entry
+    int *ucomp = nullptr;             // component of each entry
+    double *z0 = nullptr, *z = nullptr, *kz = nullptr;  // [6][3][nU]
+    double *einv = nullptr;           // [ncomp][6][6]
+    double *s = nullptr, *a = nullptr, *d = nullptr;   // [6 ncomp]
+};
+
+Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
+    *err = cudaSuccess;
+    const int nx = L.nx, ny = L.ny, nz = L.nz;
+    std::vector<long long> elems;
+    for (long long e = 0; e < L.nel; ++e)
+        if (solid[e]) elems.push_back(e);
+    if (elems.empty()) return nullptr;
+    // union-find over the solid elements, merging those within DEFL_MERGE elements
+    std::vector<int> pos((size_t)L.nel, -1);
+    for (size_t i = 0; i < elems.size(); ++i) pos[(size_t)elems[i]] = (int)i;
+    std::vector<int> parent(elems.size());
+    std::iota(parent.begin(), parent.end(), 0);
+    auto find = [&](int i) {
+        while (parent[i] != i) i = parent[i] = parent[parent[i]];
+        return i;
+    };
+    for (size_t i = 0; i < elems.size(); ++i) {
+        const long long e = elems[i];
+        const int ex = (int)(e % nx), ey = (int)((e / nx) % ny), ez = (int)(e / ((long long)nx * ny));
+        for (int dz = -DEFL_MERGE; dz <= DEFL_MERGE; ++dz)
+            for (int dy = -DEFL_MERGE; dy <= DEFL_MERGE; ++dy)
+                for (int dx = -DEFL_MERGE; dx <= DEFL_MERGE; ++dx) {
+                    const int x = ex + dx, y = ey + dy, z = ez + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
+                    const int j = pos[(size_t)elem_index(L, x, y, z)];
+                    if (j > (int)i) {
+                        const int a = find((int)i), b = find(j);
+                        if (a != b) parent[std::max(a, b)] = std::min(a, b);
+                    }
+                }
+    }
+    std::vector<int> label(elems.size()), root_id(elems.size(), -1);
+    int ncomp = 0;
+    for (size_t i = 0; i < elems.size(); ++i) {
+        const int r = find((int)i);
+        if (root_id[r] < 0) root_id[r] = ncomp++;
+        label[i] = root_id[r];
+    }
+    if (ncomp > DEFL_MAX_COMPONENTS) return nullptr;
+    // core nodes (nodes of the component's elements) and support (core + one ring)
+    const long long nnx = nx + 1, nny = ny + 1, nnz = nz + 1, nn = nnx * nny * nnz;
+    auto nid = [&](long long x, long long y, long long z) { return (z * nny + y) * nnx + x; };
+    std::vector<int> core((size_t)nn, -1), supp((size_t)nn, -1);
+    for (size_t i = 0; i < elems.size(); ++i) {
+        const long long e = elems[i];
+        const int ex = (int)(e % nx), ey = (int)((e / nx) % ny), ez = (int)(e / ((long long)nx * ny));
+        for (int c = 0; c < 8; ++c) core[(size_t)nid(ex + (c & 1), ey + ((c >> 1) & 1), ez + (c >> 2))] = label[i];
+    }
+    std::vector<double> cen((size_t)ncomp * 3, 0.0), cnt((size_t)ncomp, 0.0);
+    std::vector<double> lo((size_t)ncomp * 3, 1e300), hi((size_t)ncomp * 3, -1e300);
+    for (long long n = 0; n < nn; ++n) {
+        const int c = core[(size_t)n];
+        if (c < 0) continue;
+        const long long x = n % nnx, y = (n / nnx) % nny, z = n / (nnx * nny);
+        const double p[3] = {(double)x, (double)y, (double)z};
+        for (int k = 0; k < 3; ++k) {
+            cen[(size_t)c * 3 + k] += p[k];
+            lo[(size_t)c * 3 + k] = std::min(lo[(size_t)c * 3 + k], p[k]);
+            hi[(size_t)c * 3 + k] = std::max(hi[(size_t)c * 3 + k], p[k]);
+        }
+        cnt[(size_t)c] += 1.0;
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const long long X = x + dx, Y = y + dy, Z = z + dz;
+                    if (X < 0 || Y < 0 || Z < 0 || X >= nnx || Y >= nny || Z >= nnz) continue;
+                    supp[(size_t)nid(X, Y, Z)] = c;  // supports of merged-apart components are disjoint
+                }
+    }
+    std::vector<double> scale((size_t)ncomp);
+    for (int c = 0; c < ncomp; ++c) {
+        double ext = 1.0;
+        for (int k = 0; k < 3; ++k) {
+            cen[(size_t)c * 3 + k] /= cnt[(size_t)c];
+            ext = std::max(ext, 0.5 * (hi[(size_t)c * 3 + k] - lo[(size_t)c * 3 + k]));
+        }
+        scale[(size_t)c] = 1.0 / ext;  // rotations of unit size at the component's edge
+    }
+    // entries grouped by component
+    std::vector<std::vector<long long>> members((size_t)ncomp);
+    for (long long n = 0; n < nn; ++n)
+        if (supp[(size_t)n] >= 0) members[(size_t)supp[(size_t)n]].push_back(n);
+    Defl *d = new Defl;
+    d->L = L;
+    d->ncomp = ncomp;
+    d->off_h.assign((size_t)ncomp + 1, 0);
+    for (int c = 0; c < ncomp; ++c) d->off_h[(size_t)c + 1] = d->off_h[(size_t)c] + (long long)members[(size_t)c].size();
+    const long long nU = d->off_h.back();
+    d->nU = nU;
+    std::vector<long long> un((size_t)nU);
+    std::vector<int> uc((size_t)nU);
+    std::vector<double> z0((size_t)18 * nU, 0.0);
+    for (int c = 0; c < ncomp; ++c)
+        for (size_t q = 0; q < members[(size_t)c].size(); ++q) {
+            const long long u = d->off_h[(size_t)c] + (long long)q, n = members[(size_t)c][q];
+            const long long x = n % nnx, y = (n / nnx) % nny, z = n / (nnx * nny);
+            un[(size_t)u] = node_index(L, (int)x, (int)y, (int)z);
+            uc[(size_t)u] = c;
+            if (core[(size_t)n] != c) continue;  // ring nodes: Z = 0, K Z may not be
+            // coordinates in node steps, scaled so the rotations are of unit size at the edge
+            const double s = scale[(size_t)c];
+            const double dx = s * (x - cen[(size_t)c * 3]), dy = s * (y - cen[(size_t)c * 3 + 1]),
+                         dz = s * (z - cen[(size_t)c * 3 + 2]);
+            // translations, then rotations e_k x d
+            const double modes[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, -dz, dy}, {dz, 0, -dx}, {-dy, dx, 0}};
+            for (int t = 0; t < 6; ++t)
+                for (int k = 0; k < 3; ++k) z0[(size_t)(t * 3 + k) * nU + u] = modes[t][k];
+        }
+    const int nm = 6 * ncomp;
+    cudaError_t e = dalloc(&d->off, (size_t)ncomp + 1);
+    if (e == cudaSuccess) e = dalloc(&d->unode, (size_t)nU);
+    if (e == cudaSuccess) e = dalloc(&d->ucomp, (size_t)nU);
+    if (e == cudaSuccess) e = dalloc(&d->z0, (size_t)18 * nU);
+    if (e == cudaSuccess) e = dalloc(&d->z, (size_t)18 * nU);
+    if (e == cudaSuccess) e = dalloc(&d->kz, (size_t)18 * nU);
+    if (e == cudaSuccess) e = dalloc(&d->einv, (size_t)36 * ncomp);
+    if (e == cudaSuccess) e = dalloc(&d->s, (size_t)nm);
+    if (e == cudaSuccess) e = dalloc(&d->a, (size_t)nm);
+    if (e == cudaSuccess) e = dalloc(&d->d, (size_t)nm);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d->off, d->off_h.data(), sizeof(long long) * d->off_h.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d->unode, un.data(), sizeof(long long) * un.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d->ucomp, uc.data(), sizeof(int) * uc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d->z0, z0.data(), sizeof(double) * z0.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        *err = e;
+        defl_destroy(d);
+        return nullptr;
+    }
+    return d;
+}
+
+void defl_destroy(Defl *d) {
+    if (!d) return;
+    for (void *p : {(void *)d->off, (void *)d->unode, (void *)d->ucomp, (void *)d->z0, (void *)d->z, (void *)d->kz,
+                    (void *)d->einv, (void *)d->s, (void *)d->a, (void *)d->d})
+        if (p) cudaFree(p);
+    delete d;
+}
+
+int defl_components(const Defl *d) { return d ? d->ncomp : 0; }
+
+cudaError_t defl_setup(Defl *d, const KuLaunch &plan64, const Modal<double> &M64, const double *s64,
+                       const uint8_t *mask, double *v, double *w, cudaStream_t st) {
+    const Layout &L = d->L;
+    const long long nU = d->nU;
+    defl_mask_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, d->unode, mask, d->z0, d->z);
+    count_launches(1);
+    cudaError_t e = cudaGetLastError();
+    for (int t = 0; t < 6 && e == cudaSuccess; ++t) {
+        e = cudaMemsetAsync(v, 0, sizeof(double) * 3 * L.cs, st);
+        if (e != cudaSuccess) break;
+        defl_spread_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->z, t, v);
+        count_launches(1);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = ku_plain<double>(plan64, L, M64, s64, v, w, st);
+        if (e != cudaSuccess) break;
+        defl_gather_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, mask, w, t, d->kz);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return e;
+    std::vector<double> z((size_t)18 * nU), kz((size_t)18 * nU);
+    e = cudaMemcpyAsync(z.data(), d->z, sizeof(double) * z.size(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(kz.data(), d->kz, sizeof(double) * kz.size(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    // E_c = Z_c^T K Z_c (symmetrised), inverted block by block; a block that is not
+    // positive definite (a component with no free DOF) is left out (zero inverse)
+    std::vector<double> einv((size_t)36 * d->ncomp, 0.0);
+    for (int c = 0; c < d->ncomp; ++c) {
+        double E[36] = {};
+        for (long long u = d->off_h[(size_t)c]; u < d->off_h[(size_t)c + 1]; ++u)
+            for (int t = 0; t < 6; ++t)
+                for (int q = 0; q < 6; ++q)
+                    for (int k = 0; k < 3; ++k)
+                        E[t * 6 + q] += z[(size_t)(t * 3 + k) * nU + u] * kz[(size_t)(q * 3 + k) * nU + u];
+        double S[36];
+        for (int t = 0; t < 6; ++t)
+            for (int q = 0; q < 6; ++q) S[t * 6 + q] = 0.5 * (E[t * 6 + q] + E[q * 6 + t]);
+        if (inverse6(S)) std::copy(S, S + 36, einv.begin() + (size_t)36 * c);
+    }
+    e = cudaMemcpyAsync(d->einv, einv.data(), sizeof(double) * einv.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+cudaError_t defl_apply(Defl *d, Mg *mg, const double *r, double *z, double *rt, cudaStream_t st) {
+    const Layout &L = d->L;
+    const long long nU = d->nU;
+    const int nm = 6 * d->ncomp;
+    // a = E^-1 Z^T r ; rt = P r = r - (K Z) a
+    defl_dots_kernel<<<nm, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->z, r, d->s);
+    defl_solve_kernel<<<1, 384, 0, st>>>(nm, d->einv, d->s, nullptr, d->a);
+    count_launches(2);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rt, r, sizeof(double) * 3 * L.cs, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+    defl_scatter_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->ucomp, d->kz, d->a, -1.0, rt);
+    count_launches(1);
+    e = cudaGetLastError();
+    // y = M P r
+    if (e == cudaSuccess) e = mg_apply(mg, rt, z, st);
+    if (e != cudaSuccess) return e;
+    // z = P^T y + Q r = y + Z (a - E^-1 (K Z)^T y)
+    defl_dots_kernel<<<nm, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->kz, z, d->s);
+    defl_solve_kernel<<<1, 384, 0, st>>>(nm, d->einv, d->s, d->a, d->d);
+    defl_scatter_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->ucomp, d->z, d->d, 1.0, z);
+    count_launches(3);
+    return cudaGetLastError();
+}
+
+}  // namespace amk

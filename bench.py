@@ -240,6 +240,7 @@ PRECOND = {"jacobi": 0, "mg": 2}
 _mixed_solver = "reliable"
 _inner_tol = 0.0
 _precond = "jacobi"
+_mg_deflation = 1
 
 
 def simp_config(nat, W, max_iterations=100):
@@ -247,7 +248,7 @@ def simp_config(nat, W, max_iterations=100):
                               rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
                               precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=_inner_tol,
                               cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver],
-                              preconditioner=PRECOND[_precond])
+                              preconditioner=PRECOND[_precond], mg_deflation=_mg_deflation)
 
 
 class ClockSampler:
@@ -404,13 +405,17 @@ def main():
                          "(0: the solver's default, 0.1 reliable / 0.01 flexible)")
     ap.add_argument("--precond", default="jacobi", choices=sorted(PRECOND),
                     help="jacobi: Jacobi PCG (the headline); mg: multigrid V-cycle in the FP64 flexible CG")
+    ap.add_argument("--mg-deflation", type=int, default=1, choices=[0, 1],
+                    help="multigrid: balance the V-cycle with the rigid-body modes of the passive solid "
+                         "inclusions (1, the default) or not (0)")
     ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
                     help="mixed precision: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
                          "flexible CG over FP32 inner solves (flexible)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global _mixed_solver, _inner_tol, _precond
+    global _mixed_solver, _inner_tol, _precond, _mg_deflation
     _mixed_solver = args.mixed_solver
+    _mg_deflation = args.mg_deflation
     _inner_tol = args.inner_tol
     _precond = args.precond
 
@@ -472,7 +477,7 @@ def main():
             torch.cuda.synchronize()
             out[name] = dict(s=e0.elapsed_time(e1) * 1e-3, comp=np.array([r.compliance for r in res]),
                              its=[r.solver_iterations for r in res], res=max(r.solver_residual for r in res),
-                             rho=p.simp_density())
+                             outer=[r.solver_outer_iterations for r in res], rho=p.simp_density())
             p.close()
         j, m = out["jacobi"], out["mg"]
         rel = np.abs(m["comp"] - j["comp"]) / np.abs(j["comp"])
@@ -484,6 +489,7 @@ def main():
             "compliance_final": float(j["comp"][-1]),
             "density_max_abs_diff": float(np.max(np.abs(m["rho"] - j["rho"]))),
             "pcg_iterations_jacobi_mean": float(np.mean(j["its"])), "pcg_iterations_mg_mean": float(np.mean(m["its"])),
+            "mg_deflation": _mg_deflation, "mg_iterations": m["its"], "mg_outer_iterations": m["outer"],
             "residual_max": max(j["res"], m["res"])}))
         return
 
@@ -657,6 +663,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
                        "description": W["desc"], "precision": "mixed", "mixed_solver": _mixed_solver, "preconditioner": _precond,
+                       **({"mg_deflation": _mg_deflation} if _precond == "mg" else {}),
                        "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probe flushes L2",
                        "parallelism": f"replicas x{world}"},
             "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,

@@ -110,6 +110,11 @@ typedef struct am_simp_config {
     int layout;               /* AM_LAYOUT_* of density arrays */
     int verbose;
     int mixed_solver;         /* MIXED with the Jacobi preconditioner: AM_MIXED_* */
+    int mg_deflation;         /* AM_PRECOND_MG: 1 (the default) balances the V-cycle with the
+                                 rigid-body modes of the passive solid inclusions (elements
+                                 held at density 1), whose near-free motion once their
+                                 surroundings turn void no coarse grid represents; 0: the
+                                 V-cycle alone */
 } am_simp_config;
 
 /* Per-solve statistics (SolveStats, linear_solver.hpp:48-56). */

@@ -105,3 +105,60 @@ def test_mg_on_a_grid_that_does_not_coarsen_uses_jacobi():
     ref, _, _ = O.pcg(shape, O.ke(), s, fixed, F, tol=1e-13)
     assert st.converged
     assert np.linalg.norm(u - ref) / np.linalg.norm(ref) <= 1e-6
+
+
+def _floating_pad(shape):
+    """A passive solid column (grid = 1, full height) inside a two-element ring of
+    near-void design material (rho 0.011: 1e-6 of the pad's stiffness), the rest at
+    0.5: the pad's rigid-body motions are near-null modes of K."""
+    nx, ny, nz = shape
+    grid = np.zeros(shape, dtype=np.int8)
+    x0, y0 = 3 * nx // 4 - 2, ny // 2 - 2
+    grid[x0:x0 + 4, y0:y0 + 4, :] = 1
+    rho = np.full(shape, 0.5)
+    rho[x0 - 2:x0 + 6, y0 - 2:y0 + 6, :] = 0.011
+    rho[grid == 1] = 1.0
+    return grid, rho
+
+
+def test_mg_deflation_of_a_floating_pad_matches_oracle():
+    shape = (48, 24, 24)
+    grid, rho = _floating_pad(shape)
+    F, fixed = _cantilever(shape)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3, grid=grid)
+    p.set_loads([F], [fixed])
+    base = dict(E_min=1e-9, rho_min=0.01, cg_tol=1e-8, warm_start=0, preconditioner=nat.PRECOND_MG)
+    u_d, st_d = p.solve(nat.default_config(nat.VARIANT_CPP, mg_deflation=1, **base), rho)
+    u_0, st_0 = p.solve(nat.default_config(nat.VARIANT_CPP, mg_deflation=0, **base), rho)
+    s = O.scales(0, rho.ravel(), grid.ravel(), 3.0, 1e-9, 0.01, 1.0)
+    ref, _, _ = O.pcg(shape, O.ke(), s, fixed, F, tol=1e-13)
+    for u, st in ((u_d, st_d), (u_0, st_0)):
+        assert st.converged and st.residual <= 1e-8
+        assert np.linalg.norm(u - ref) / np.linalg.norm(ref) <= 1e-6
+    # the balanced V-cycle carries the whole solve (no Jacobi fallback) and needs
+    # no more iterations than the V-cycle alone
+    assert st_d.iterations == st_d.outer_iterations, (st_d.iterations, st_d.outer_iterations)
+    assert st_d.iterations <= st_0.iterations, (st_d.iterations, st_0.iterations)
+
+
+def test_mg_deflation_simp_with_passive_pads_matches_oracle():
+    """SIMP with two passive solid columns (rho0 = 1: outside the design mask) and
+    the balanced V-cycle: compliance history and densities as the FP64 oracle."""
+    shape = (32, 16, 8)
+    F, fixed = _cantilever(shape)
+    rho0 = np.full(shape, 0.3)
+    rho0[22:25, 2:5, :] = 1.0
+    rho0[22:25, 11:14, :] = 1.0
+    iters = 8
+    prm = O.make_params(volume_fraction=0.3, filter_radius=1.5, move_limit=0.2, rho_min=0.01, E_min=1e-9,
+                        convergence_tol=0.0, max_iterations=iters, cg_tol=1e-12, warm_start=1)
+    ref = O.simp_cpp(shape, 1.0, 1.0, 0.3, prm, rho0, F, fixed)
+    p = nat.Problem(shape, 1.0, 1.0, 0.3)
+    p.set_loads([F], [fixed])
+    cfg = nat.default_config(nat.VARIANT_CPP, volume_fraction=0.3, filter_radius=1.5, move_limit=0.2, rho_min=0.01,
+                             E_min=1e-9, convergence_tol=0.0, max_iterations=iters, cg_tol=1e-10,
+                             preconditioner=nat.PRECOND_MG, mg_deflation=1)
+    r = p.simp_run(cfg, rho0)
+    rel = np.abs(r["compliance"] - ref["compliance"]) / ref["compliance"]
+    assert rel.max() <= 1e-6, rel
+    assert np.abs(r["density"] - ref["density"].ravel()).max() <= 1e-4
