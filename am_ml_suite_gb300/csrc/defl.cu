@@ -180,7 +180,9 @@ Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
     std::vector<long long> elems;
     for (long long e = 0; e < L.nel; ++e)
         if (solid[e]) elems.push_back(e);
-    if (elems.empty()) return nullptr;
+    // none, or so many that the coarse grids represent them (and the mode arrays
+    // would span most of the grid): no deflation
+    if (elems.empty() || (long long)elems.size() > L.nel / 4) return nullptr;
     // union-find over the solid elements, merging those within DEFL_MERGE elements
     std::vector<int> pos((size_t)L.nel, -1);
     for (size_t i = 0; i < elems.size(); ++i) pos[(size_t)elems[i]] = (int)i;

@@ -34,8 +34,9 @@ constexpr int DEFL_MAX_COMPONENTS = 64;
 struct Defl;
 
 // Components of the elements flagged in solid (host, nel entries, element order of
-// the device layout).  nullptr with *err = cudaSuccess when there is none (or more
-// than DEFL_MAX_COMPONENTS); *err set on an allocation failure.
+// the device layout).  nullptr with *err = cudaSuccess when there is none, when
+// they are more than a quarter of the elements or form more than
+// DEFL_MAX_COMPONENTS components; *err set on an allocation failure.
 Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err);
 void defl_destroy(Defl *d);
 int defl_components(const Defl *d);
