@@ -398,12 +398,13 @@ am_status inner_iterate_to_fp64(am_problem *P) {
 // The multigrid hierarchy for the current operator and load case lc: true when
 // it is ready, false when the grid does not coarsen far enough (the solve then
 // uses the Jacobi path).
-// Passive solid elements (held at density 1 by the design mask: CPP elements whose
-// initial density is >= 0.99, PY grid == 1; outside a SIMP run, grid == 1).
+// Passive solid elements: CPP elements outside the design mask at density >= 0.99
+// (their scale is rho^p = 1 for the whole run); PY and outside a SIMP run, grid == 1
+// (scale 1 whatever the density, fem.py:175-248).
 am_status passive_solid(am_problem *P, std::vector<uint8_t> &solid) {
     const size_t nel = (size_t)P->L.nel;
     solid.assign(nel, 0);
-    if (P->simp_begun) {
+    if (P->simp_begun && P->cfg.variant == AM_VARIANT_CPP) {
         std::vector<uint8_t> dm(nel);
         std::vector<double> rho(nel);
         CK(cudaMemcpyAsync(dm.data(), P->design.p, nel, cudaMemcpyDeviceToHost, P->st));
