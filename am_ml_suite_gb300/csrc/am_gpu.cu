@@ -614,7 +614,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             } else if (mg_on) {
                 // z = M(r): one FP32 multigrid V-cycle, balanced by the rigid-body
                 // modes of the passive solid inclusions when there are any
-                if (defl) CK(defl_apply(defl, P->mg, P->r64.p, P->xi64.p, P->xw64.p, P->st));
+                if (defl) CK(defl_apply(defl, P->mg, P->r64.p, P->xi64.p, P->st));
                 else CK(mg_apply(P->mg, P->r64.p, P->xi64.p, P->st));
                 its = 1;
                 total += its;
@@ -1351,6 +1351,14 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
         ocb = OcBuffers{P->L.nel, P->oc_a64.p, P->oc_lo64.p, P->oc_hi64.p, P->oc_a32.p, P->oc_lo32.p, P->oc_hi32.p};
         CK(oc_prepare(ocb, P->rho.p, P->dcf.p, cf.move_limit, 0, cf.variant, P->S, P->st));
     }
+    if (which == 10 || which == 11) {
+        // one V-cycle (10) or the V-cycle balanced by the passive inclusions'
+        // rigid-body modes (11) on the residual vector
+        bool ok = false;
+        CKS(mg_ready(P, 0, which == 11, &ok));
+        if (!ok) return fail(AM_ERR_INVALID_ARG, "the grid does not coarsen for multigrid");
+        if (which == 11 && !P->defl) return fail(AM_ERR_INVALID_ARG, "no passive solid inclusion to deflate");
+    }
     DevBuf<uint8_t> flush;
     const size_t flush_bytes = 512ull << 20;
     if (flush_l2) CK(flush.alloc(flush_bytes));
@@ -1407,6 +1415,12 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                            P->partial.p, P->S, P->nblocks_vec, P->st));
                 break;
             }
+            case 10:
+                CK(mg_apply(P->mg, P->r64.p, P->xi64.p, P->st));
+                break;
+            case 11:
+                CK(defl_apply(P->defl, P->mg, P->r64.p, P->xi64.p, P->st));
+                break;
             default:
                 return fail(AM_ERR_INVALID_ARG, "unknown kernel id");
         }

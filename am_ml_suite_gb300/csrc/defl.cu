@@ -19,6 +19,7 @@ namespace {
 
 constexpr int DEFL_THREADS = 256;
 constexpr int DEFL_MERGE = 3;  // components closer than this many elements are merged
+constexpr int DEFL_CHUNK = 256;  // support entries per block of the dot products
 
 inline int blocks_for(long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + DEFL_THREADS - 1) / DEFL_THREADS, 152 * 8));
@@ -64,39 +65,78 @@ __global__ void defl_gather_kernel(long long nU, long long cs, const long long *
     }
 }
 
-// s[6 c + t] = sum over component c's support of V[t] . x ; one block per (c, t)
+// part[c][chunk][t] = sum over entries [chunk DEFL_CHUNK, +DEFL_CHUNK) of component
+// c's support of V[t] . x; block (chunk, c), one warp per mode t (warps 6, 7 idle)
 __global__ void __launch_bounds__(DEFL_THREADS)
     defl_dots_kernel(long long nU, long long cs, const long long *__restrict__ off,
                      const long long *__restrict__ unode, const double *__restrict__ V, const double *__restrict__ x,
-                     double *__restrict__ s) {
-    __shared__ double red[DEFL_THREADS / 32];
-    const int c = blockIdx.x / 6, t = blockIdx.x - 6 * c;
+                     int nchunk, double *__restrict__ part) {
+    const int c = blockIdx.y, t = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (t >= 6) return;
+    const long long b = off[c] + (long long)blockIdx.x * DEFL_CHUNK;
+    const long long e = min(off[c + 1], b + DEFL_CHUNK);
     double acc = 0.0;
-    for (long long u = off[c] + threadIdx.x; u < off[c + 1]; u += DEFL_THREADS) {
+#pragma unroll 4
+    for (long long u = b + lane; u < e; u += 32) {
         const long long n = unode[u];
 #pragma unroll
         for (int k = 0; k < 3; ++k) acc = fma(V[(t * 3 + k) * nU + u], x[k * cs + n], acc);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < DEFL_THREADS / 32; ++w) tot += red[w];
-        s[blockIdx.x] = tot;
-    }
+    if (lane == 0) part[((long long)c * nchunk + blockIdx.x) * 6 + t] = acc;
 }
 
-// out = E^-1 s (block c: E_c^-1 s[6c .. 6c+5]), or base - E^-1 s when base is given
-__global__ void defl_solve_kernel(int nm, const double *__restrict__ einv, const double *__restrict__ s,
-                                  const double *__restrict__ base, double *__restrict__ out) {
-    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+// s = the chunk sums in chunk order; out = E^-1 s (block c: E_c^-1 s[6c .. 6c+5]),
+// or base - E^-1 s when base is given
+__global__ void defl_solve_kernel(int ncomp, int nchunk, const double *__restrict__ einv,
+                                  const double *__restrict__ part, const double *__restrict__ base,
+                                  double *__restrict__ out) {
+    __shared__ double s[6 * DEFL_MAX_COMPONENTS];
+    for (int i = threadIdx.x; i < 6 * ncomp; i += blockDim.x) {
+        const int c = i / 6, t = i - 6 * c;
+        double v = 0.0;
+        for (int q = 0; q < nchunk; ++q) v += part[((long long)c * nchunk + q) * 6 + t];
+        s[i] = v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 6 * ncomp; i += blockDim.x) {
         const int c = i / 6, t = i - 6 * c;
         double v = 0.0;
 #pragma unroll
         for (int j = 0; j < 6; ++j) v = fma(einv[(c * 6 + t) * 6 + j], s[c * 6 + j], v);
         out[i] = base ? base[i] - v : v;
+    }
+}
+
+// keep[k][u] = x[k cs + node(u)], then x[k cs + node(u)] -= sum_t KZ[t][k][u] a[...]
+__global__ void defl_project_kernel(long long nU, long long cs, const long long *__restrict__ unode,
+                                    const int *__restrict__ ucomp, const double *__restrict__ kz,
+                                    const double *__restrict__ a, double *__restrict__ keep, double *__restrict__ x) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long n = unode[u];
+        const double *cf = a + 6 * ucomp[u];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double v = 0.0;
+#pragma unroll
+            for (int t = 0; t < 6; ++t) v = fma(kz[(t * 3 + k) * nU + u], cf[t], v);
+            const double xv = x[k * cs + n];
+            keep[k * nU + u] = xv;
+            x[k * cs + n] = xv - v;
+        }
+    }
+}
+
+// x[k cs + node(u)] = keep[k][u]: the entries defl_project_kernel changed, restored
+__global__ void defl_restore_kernel(long long nU, long long cs, const long long *__restrict__ unode,
+                                    const double *__restrict__ keep, double *__restrict__ x) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nU;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long n = unode[u];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[k * cs + n] = keep[k * nU + u];
     }
 }
 
@@ -171,7 +211,10 @@ struct Defl {
     int *ucomp = nullptr;             // component of each entry
     double *z0 = nullptr, *z = nullptr, *kz = nullptr;  // [6][3][nU]
     double *einv = nullptr;           // [ncomp][6][6]
-    double *s = nullptr, *a = nullptr, *d = nullptr;   // [6 ncomp]
+    int nchunk = 1;                   // dot-product blocks per component (the largest support)
+    double *part = nullptr;           // [ncomp][nchunk][6] chunk sums
+    double *a = nullptr, *d = nullptr;  // [6 ncomp]
+    double *keep = nullptr;           // [3][nU]: entries of r changed during an application
 };
 
 Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
@@ -285,6 +328,9 @@ Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
                 for (int k = 0; k < 3; ++k) z0[(size_t)(t * 3 + k) * nU + u] = modes[t][k];
         }
     const int nm = 6 * ncomp;
+    long long longest = 1;
+    for (int c = 0; c < ncomp; ++c) longest = std::max(longest, d->off_h[(size_t)c + 1] - d->off_h[(size_t)c]);
+    d->nchunk = (int)((longest + DEFL_CHUNK - 1) / DEFL_CHUNK);
     cudaError_t e = dalloc(&d->off, (size_t)ncomp + 1);
     if (e == cudaSuccess) e = dalloc(&d->unode, (size_t)nU);
     if (e == cudaSuccess) e = dalloc(&d->ucomp, (size_t)nU);
@@ -292,9 +338,10 @@ Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
     if (e == cudaSuccess) e = dalloc(&d->z, (size_t)18 * nU);
     if (e == cudaSuccess) e = dalloc(&d->kz, (size_t)18 * nU);
     if (e == cudaSuccess) e = dalloc(&d->einv, (size_t)36 * ncomp);
-    if (e == cudaSuccess) e = dalloc(&d->s, (size_t)nm);
+    if (e == cudaSuccess) e = dalloc(&d->part, (size_t)6 * ncomp * d->nchunk);
     if (e == cudaSuccess) e = dalloc(&d->a, (size_t)nm);
     if (e == cudaSuccess) e = dalloc(&d->d, (size_t)nm);
+    if (e == cudaSuccess) e = dalloc(&d->keep, (size_t)3 * nU);
     if (e == cudaSuccess)
         e = cudaMemcpy(d->off, d->off_h.data(), sizeof(long long) * d->off_h.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d->unode, un.data(), sizeof(long long) * un.size(), cudaMemcpyHostToDevice);
@@ -311,7 +358,7 @@ Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
 void defl_destroy(Defl *d) {
     if (!d) return;
     for (void *p : {(void *)d->off, (void *)d->unode, (void *)d->ucomp, (void *)d->z0, (void *)d->z, (void *)d->kz,
-                    (void *)d->einv, (void *)d->s, (void *)d->a, (void *)d->d})
+                    (void *)d->einv, (void *)d->part, (void *)d->a, (void *)d->d, (void *)d->keep})
         if (p) cudaFree(p);
     delete d;
 }
@@ -363,26 +410,26 @@ cudaError_t defl_setup(Defl *d, const KuLaunch &plan64, const Modal<double> &M64
     return e;
 }
 
-cudaError_t defl_apply(Defl *d, Mg *mg, const double *r, double *z, double *rt, cudaStream_t st) {
+cudaError_t defl_apply(Defl *d, Mg *mg, double *r, double *z, cudaStream_t st) {
     const Layout &L = d->L;
     const long long nU = d->nU;
-    const int nm = 6 * d->ncomp;
-    // a = E^-1 Z^T r ; rt = P r = r - (K Z) a
-    defl_dots_kernel<<<nm, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->z, r, d->s);
-    defl_solve_kernel<<<1, 384, 0, st>>>(nm, d->einv, d->s, nullptr, d->a);
-    count_launches(2);
+    const dim3 gdot(d->nchunk, d->ncomp);
+    // a = E^-1 Z^T r ; r <- P r = r - (K Z) a on the supports (old entries kept)
+    defl_dots_kernel<<<gdot, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->z, r, d->nchunk, d->part);
+    defl_solve_kernel<<<1, 128, 0, st>>>(d->ncomp, d->nchunk, d->einv, d->part, nullptr, d->a);
+    defl_project_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->ucomp, d->kz, d->a, d->keep,
+                                                                  r);
+    count_launches(3);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rt, r, sizeof(double) * 3 * L.cs, cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return e;
-    defl_scatter_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->ucomp, d->kz, d->a, -1.0, rt);
+    // y = M P r, then r restored exactly
+    if (e == cudaSuccess) e = mg_apply(mg, r, z, st);
+    defl_restore_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->keep, r);
     count_launches(1);
-    e = cudaGetLastError();
-    // y = M P r
-    if (e == cudaSuccess) e = mg_apply(mg, rt, z, st);
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // z = P^T y + Q r = y + Z (a - E^-1 (K Z)^T y)
-    defl_dots_kernel<<<nm, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->kz, z, d->s);
-    defl_solve_kernel<<<1, 384, 0, st>>>(nm, d->einv, d->s, d->a, d->d);
+    defl_dots_kernel<<<gdot, DEFL_THREADS, 0, st>>>(nU, L.cs, d->off, d->unode, d->kz, z, d->nchunk, d->part);
+    defl_solve_kernel<<<1, 128, 0, st>>>(d->ncomp, d->nchunk, d->einv, d->part, d->a, d->d);
     defl_scatter_kernel<<<blocks_for(nU), DEFL_THREADS, 0, st>>>(nU, L.cs, d->unode, d->ucomp, d->z, d->d, 1.0, z);
     count_launches(3);
     return cudaGetLastError();

@@ -16,9 +16,8 @@
 // them lie within 3 elements of each other, so that the node supports of K Z
 // (the component's nodes and one ring around them) of different components are
 // disjoint and E is block diagonal (6 x 6 per component).  Z, K Z and E live on
-// those supports only; one application costs two small dot-product launches, two
-// small 6 x 6 solves, two scatters on the supports, one vector copy and the
-// V-cycle.
+// those supports only; one application costs two dot-product launches, two 6 x 6
+// block solves and three passes over the supports besides the V-cycle.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -49,7 +48,8 @@ int defl_components(const Defl *d);
 cudaError_t defl_setup(Defl *d, const KuLaunch &plan64, const Modal<double> &M64, const double *s64,
                        const uint8_t *mask, double *v, double *w, cudaStream_t st);
 
-// z = P^T M P r + Q r with M = mg_apply(mg, .); rt: scratch vector (3 L.cs doubles).
-cudaError_t defl_apply(Defl *d, Mg *mg, const double *r, double *z, double *rt, cudaStream_t st);
+// z = P^T M P r + Q r with M = mg_apply(mg, .).  P r is formed in r itself on the
+// supports (the V-cycle reads it there) and r is restored exactly afterwards.
+cudaError_t defl_apply(Defl *d, Mg *mg, double *r, double *z, cudaStream_t st);
 
 }  // namespace amk

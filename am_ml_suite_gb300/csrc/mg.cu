@@ -139,7 +139,8 @@ __global__ void mg_prolong_kernel(Layout Lc, Layout Lf, const float *__restrict_
 }
 
 // x = A^-1 b on the coarsest grid; A^-1 symmetric, n x n, dense DOF order
-// 3 * ((iz (ny+1) + iy)(nx+1) + ix) + c
+// 3 * ((iz (ny+1) + iy)(nx+1) + ix) + c.  One warp per row of A^-1 (coalesced
+// reads of the row, a shuffle reduction), every block holding b in shared memory.
 __global__ void mg_dense_kernel(Layout L, int n, const float *__restrict__ ainv, const float *__restrict__ b,
                                 float *__restrict__ x) {
     extern __shared__ float bd[];
@@ -150,12 +151,18 @@ __global__ void mg_dense_kernel(Layout L, int n, const float *__restrict__ ainv,
         bd[i] = b[node_index(L, ix, iy, iz) + c * L.cs];
     }
     __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < n; i += gridDim.x * nw) {
+        const float *row = ainv + (long long)i * n;
         float acc = 0.f;
-        for (int j = 0; j < n; ++j) acc = fmaf(ainv[(long long)j * n + i], bd[j], acc);
-        const int c = i % 3, nd = i / 3;
-        const int ix = nd % nx1, iy = (nd / nx1) % ny1, iz = nd / (nx1 * ny1);
-        x[node_index(L, ix, iy, iz) + c * L.cs] = acc;
+        for (int j = lane; j < n; j += 32) acc = fmaf(row[j], bd[j], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const int c = i % 3, nd = i / 3;
+            const int ix = nd % nx1, iy = (nd / nx1) % ny1, iz = nd / (nx1 * ny1);
+            x[node_index(L, ix, iy, iz) + c * L.cs] = acc;
+        }
     }
 }
 
@@ -374,7 +381,7 @@ cudaError_t vcycle(Mg *m, size_t l, cudaStream_t st) {
     cudaError_t e;
     if (l + 1 == m->lv.size()) {
         const int n = m->n_dense;
-        mg_dense_kernel<<<(n + 255) / 256, 256, sizeof(float) * n, st>>>(v.L, n, m->ainv, v.b, v.x);
+        mg_dense_kernel<<<(n + 7) / 8, 256, sizeof(float) * n, st>>>(v.L, n, m->ainv, v.b, v.x);
         count_launches(1);
         return cudaGetLastError();
     }

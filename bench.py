@@ -391,7 +391,8 @@ def main():
     ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS) + ["batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd", "filter", "oc"],
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd", "filter", "oc",
+                                        "vcycle", "vcycle_defl"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--compare-mg", action="store_true",
@@ -550,8 +551,8 @@ def main():
         # ku: the staged PCG K*u the solver runs; ku2: the register-direct kernel it
         # replaced; ku3s3: the staged kernel with 3 stages instead of 4
         which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7,
-                 "filter": 8, "oc": 9}[args.probe]
-        if which >= 8:
+                 "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11}[args.probe]
+        if which in (8, 9):
             p.simp_step()  # the filter and OC probes time the state a SIMP step leaves
         avg, mn = p.bench_kernel(which, reps=args.reps, flush_l2=True)
         lay = p.layout_info()

@@ -268,7 +268,9 @@ long long am_launch_count(void);
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
  * and folded iterate) iteration, 8 the C++ cone sensitivity filter
  * (shared-memory stencil), 9 one OC bisection pass (double-float) -- these two
- * on the state of the last am_simp_step.  flush_l2 != 0 overwrites a 512 MB buffer before each
+ * on the state of the last am_simp_step --, 10 one multigrid V-cycle and 11 the
+ * V-cycle balanced by the rigid-body modes of the passive solid inclusions (both
+ * a sequence of launches, timed as a whole).  flush_l2 != 0 overwrites a 512 MB buffer before each
  * launch so the kernel reads from HBM, then reads that buffer back so the write's
  * dirty L2 lines are written back before the timed launch.  Solver state is restored afterwards. */
 am_status am_bench_kernel(am_problem *p, int which, int reps, int flush_l2, double *avg_ms, double *min_ms);
