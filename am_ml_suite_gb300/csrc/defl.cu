@@ -8,17 +8,16 @@
 // methods", J. Sci. Comput. 39 (2009).
 #include <algorithm>
 #include <cmath>
-#include <numeric>
 #include <vector>
 
 #include "defl.h"
+#include "defl_space.h"
 
 namespace amk {
 
 namespace {
 
 constexpr int DEFL_THREADS = 256;
-constexpr int DEFL_MERGE = 3;  // components closer than this many elements are merged
 constexpr int DEFL_CHUNK = 256;  // support entries per block of the dot products
 
 inline int blocks_for(long long n) {
@@ -219,114 +218,18 @@ struct Defl {
 
 Defl *defl_create(const Layout &L, const uint8_t *solid, cudaError_t *err) {
     *err = cudaSuccess;
-    const int nx = L.nx, ny = L.ny, nz = L.nz;
-    std::vector<long long> elems;
-    for (long long e = 0; e < L.nel; ++e)
-        if (solid[e]) elems.push_back(e);
-    // none, or so many that the coarse grids represent them (and the mode arrays
-    // would span most of the grid): no deflation
-    if (elems.empty() || (long long)elems.size() > L.nel / 4) return nullptr;
-    // union-find over the solid elements, merging those within DEFL_MERGE elements
-    std::vector<int> pos((size_t)L.nel, -1);
-    for (size_t i = 0; i < elems.size(); ++i) pos[(size_t)elems[i]] = (int)i;
-    std::vector<int> parent(elems.size());
-    std::iota(parent.begin(), parent.end(), 0);
-    auto find = [&](int i) {
-        while (parent[i] != i) i = parent[i] = parent[parent[i]];
-        return i;
-    };
-    for (size_t i = 0; i < elems.size(); ++i) {
-        const long long e = elems[i];
-        const int ex = (int)(e % nx), ey = (int)((e / nx) % ny), ez = (int)(e / ((long long)nx * ny));
-        for (int dz = -DEFL_MERGE; dz <= DEFL_MERGE; ++dz)
-            for (int dy = -DEFL_MERGE; dy <= DEFL_MERGE; ++dy)
-                for (int dx = -DEFL_MERGE; dx <= DEFL_MERGE; ++dx) {
-                    const int x = ex + dx, y = ey + dy, z = ez + dz;
-                    if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
-                    const int j = pos[(size_t)elem_index(L, x, y, z)];
-                    if (j > (int)i) {
-                        const int a = find((int)i), b = find(j);
-                        if (a != b) parent[std::max(a, b)] = std::min(a, b);
-                    }
-                }
-    }
-    std::vector<int> label(elems.size()), root_id(elems.size(), -1);
-    int ncomp = 0;
-    for (size_t i = 0; i < elems.size(); ++i) {
-        const int r = find((int)i);
-        if (root_id[r] < 0) root_id[r] = ncomp++;
-        label[i] = root_id[r];
-    }
-    if (ncomp > DEFL_MAX_COMPONENTS) return nullptr;
-    // core nodes (nodes of the component's elements) and support (core + one ring)
-    const long long nnx = nx + 1, nny = ny + 1, nnz = nz + 1, nn = nnx * nny * nnz;
-    auto nid = [&](long long x, long long y, long long z) { return (z * nny + y) * nnx + x; };
-    std::vector<int> core((size_t)nn, -1), supp((size_t)nn, -1);
-    for (size_t i = 0; i < elems.size(); ++i) {
-        const long long e = elems[i];
-        const int ex = (int)(e % nx), ey = (int)((e / nx) % ny), ez = (int)(e / ((long long)nx * ny));
-        for (int c = 0; c < 8; ++c) core[(size_t)nid(ex + (c & 1), ey + ((c >> 1) & 1), ez + (c >> 2))] = label[i];
-    }
-    std::vector<double> cen((size_t)ncomp * 3, 0.0), cnt((size_t)ncomp, 0.0);
-    std::vector<double> lo((size_t)ncomp * 3, 1e300), hi((size_t)ncomp * 3, -1e300);
-    for (long long n = 0; n < nn; ++n) {
-        const int c = core[(size_t)n];
-        if (c < 0) continue;
-        const long long x = n % nnx, y = (n / nnx) % nny, z = n / (nnx * nny);
-        const double p[3] = {(double)x, (double)y, (double)z};
-        for (int k = 0; k < 3; ++k) {
-            cen[(size_t)c * 3 + k] += p[k];
-            lo[(size_t)c * 3 + k] = std::min(lo[(size_t)c * 3 + k], p[k]);
-            hi[(size_t)c * 3 + k] = std::max(hi[(size_t)c * 3 + k], p[k]);
-        }
-        cnt[(size_t)c] += 1.0;
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const long long X = x + dx, Y = y + dy, Z = z + dz;
-                    if (X < 0 || Y < 0 || Z < 0 || X >= nnx || Y >= nny || Z >= nnz) continue;
-                    supp[(size_t)nid(X, Y, Z)] = c;  // supports of merged-apart components are disjoint
-                }
-    }
-    std::vector<double> scale((size_t)ncomp);
-    for (int c = 0; c < ncomp; ++c) {
-        double ext = 1.0;
-        for (int k = 0; k < 3; ++k) {
-            cen[(size_t)c * 3 + k] /= cnt[(size_t)c];
-            ext = std::max(ext, 0.5 * (hi[(size_t)c * 3 + k] - lo[(size_t)c * 3 + k]));
-        }
-        scale[(size_t)c] = 1.0 / ext;  // rotations of unit size at the component's edge
-    }
-    // entries grouped by component
-    std::vector<std::vector<long long>> members((size_t)ncomp);
-    for (long long n = 0; n < nn; ++n)
-        if (supp[(size_t)n] >= 0) members[(size_t)supp[(size_t)n]].push_back(n);
+    DeflSpace sp;
+    if (!defl_space(L.nx, L.ny, L.nz, L.sx, L.sxy, solid, sp)) return nullptr;
+    const int ncomp = sp.ncomp;
     Defl *d = new Defl;
     d->L = L;
     d->ncomp = ncomp;
-    d->off_h.assign((size_t)ncomp + 1, 0);
-    for (int c = 0; c < ncomp; ++c) d->off_h[(size_t)c + 1] = d->off_h[(size_t)c] + (long long)members[(size_t)c].size();
+    d->off_h = sp.off;
     const long long nU = d->off_h.back();
     d->nU = nU;
-    std::vector<long long> un((size_t)nU);
-    std::vector<int> uc((size_t)nU);
-    std::vector<double> z0((size_t)18 * nU, 0.0);
-    for (int c = 0; c < ncomp; ++c)
-        for (size_t q = 0; q < members[(size_t)c].size(); ++q) {
-            const long long u = d->off_h[(size_t)c] + (long long)q, n = members[(size_t)c][q];
-            const long long x = n % nnx, y = (n / nnx) % nny, z = n / (nnx * nny);
-            un[(size_t)u] = node_index(L, (int)x, (int)y, (int)z);
-            uc[(size_t)u] = c;
-            if (core[(size_t)n] != c) continue;  // ring nodes: Z = 0, K Z may not be
-            // coordinates in node steps, scaled so the rotations are of unit size at the edge
-            const double s = scale[(size_t)c];
-            const double dx = s * (x - cen[(size_t)c * 3]), dy = s * (y - cen[(size_t)c * 3 + 1]),
-                         dz = s * (z - cen[(size_t)c * 3 + 2]);
-            // translations, then rotations e_k x d
-            const double modes[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, -dz, dy}, {dz, 0, -dx}, {-dy, dx, 0}};
-            for (int t = 0; t < 6; ++t)
-                for (int k = 0; k < 3; ++k) z0[(size_t)(t * 3 + k) * nU + u] = modes[t][k];
-        }
+    const std::vector<long long> &un = sp.unode;
+    const std::vector<int> &uc = sp.ucomp;
+    const std::vector<double> &z0 = sp.z0;
     const int nm = 6 * ncomp;
     long long longest = 1;
     for (int c = 0; c < ncomp; ++c) longest = std::max(longest, d->off_h[(size_t)c + 1] - d->off_h[(size_t)c]);

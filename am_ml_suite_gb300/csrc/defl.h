@@ -24,11 +24,10 @@
 
 #include "am_common.cuh"
 #include "kernels.cuh"
+#include "defl_space.h"
 #include "mg.h"
 
 namespace amk {
-
-constexpr int DEFL_MAX_COMPONENTS = 64;
 
 struct Defl;
 
