@@ -164,6 +164,7 @@ SIGNATURES = {
     "am_simp_get_density": (ctypes.c_int, [_vp, _dp]),
     "am_launch_count": (ctypes.c_longlong, []),
     "am_selftest_copy_wait": (ctypes.c_int, [ctypes.c_double, _ip, _dp]),
+    "am_selftest_solve_timeout": (ctypes.c_int, [_vp, ctypes.POINTER(SimpConfig), _dp, ctypes.c_int, _ip]),
     "am_bench_kernel": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "am_problem_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "am_precond_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_longlong, ctypes.POINTER(_vp)]),
@@ -331,6 +332,14 @@ class Problem:
                                     ptr(pp), float(beta), int(impl), ptr(p_out), ptr(q_out), ctypes.byref(pq)),
               "am_ku_pcg_step")
         return p_out, q_out, pq.value
+
+    def selftest_solve_timeout(self, cfg, rho, load_case=0):
+        """Status (an int) that am_solve returns when a kernel of its PCG reports a
+        copy wait that ran out; the flag is set on the host, no wait runs out."""
+        st = ctypes.c_int(-1)
+        check(load().am_selftest_solve_timeout(self.handle, ctypes.byref(cfg), ptr(self._rho(rho)), int(load_case),
+                                               ctypes.byref(st)), "am_selftest_solve_timeout")
+        return st.value
 
     def solve(self, cfg, rho, load_case=0):
         u = np.zeros(self.N)

@@ -172,6 +172,9 @@ struct am_problem {
     am_simp_config cfg{};
     double n_design = 0.0;
     int iter = 0;
+    // self-test only: the next PCG run starts with Scalars::kerr set, as if a
+    // kernel's bounded copy wait had run out (am_selftest_solve_timeout)
+    bool inject_kerr = false;
 };
 
 namespace {
@@ -360,6 +363,11 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
     cudaGraphExec_t *gx = std::is_same<T, float>::value ? &P->g32 : &P->g64;
     if constexpr (std::is_same<T, float>::value) CKS(ku3_ready(P));
     if (!*gx) CKS(build_pcg_graph<T>(P, gx));
+    if (P->inject_kerr) {
+        static const int kOne = 1;
+        P->inject_kerr = false;
+        CK(cudaMemcpyAsync(&P->S->kerr, &kOne, sizeof(int), cudaMemcpyHostToDevice, P->st));
+    }
     CKS(sync_scalars(P));
     // every chunk either advances the iteration count or ends the solve; the
     // host bound below only catches a solver state that stops advancing
@@ -379,7 +387,7 @@ am_status run_pcg(am_problem *P, int *its, int *status) {
     }
     *its = P->Sh->it;
     *status = P->Sh->status;
-    if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_CUDA, "a bulk-copy wait of the PCG timed out");
+    if (P->Sh->status == ST_TIMEOUT) return fail(AM_ERR_TIMEOUT, "a bulk-copy wait of the PCG timed out");
     return AM_OK;
 }
 
@@ -1055,7 +1063,7 @@ am_status am_ku_pcg_step(am_problem *P, const am_simp_config *cfg, const double 
         CK(ku2_pcg(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p, P->mask.p,
                    P->q32v.p, P->partial.p, P->S, P->st));
     CKS(sync_scalars(P));
-    if (P->Sh->kerr) return fail(AM_ERR_CUDA, "a copy wait of the PCG K*u timed out");
+    if (P->Sh->kerr) return fail(AM_ERR_TIMEOUT, "a copy wait of the PCG K*u timed out");
     if (pq) *pq = P->Sh->pq;
     if (p_out) {
         CK(dev_to_dof_t<float>(P->L, P->p32b.p, P->vstage.p, P->st));
@@ -1107,6 +1115,24 @@ am_status am_solve(am_problem *P, const am_simp_config *cfg, const double *rho, 
             stats->min_displacement = mn;
         }
     }
+    return AM_OK;
+}
+
+am_status am_selftest_solve_timeout(am_problem *P, const am_simp_config *cfg, const double *rho, int load_case,
+                                    int *solve_status) {
+    CKS(check_problem(P));
+    if (!solve_status) return fail(AM_ERR_INVALID_ARG, "null solve_status");
+    P->inject_kerr = true;
+    am_solve_stats st{};
+    const am_status s = am_solve(P, cfg, rho, load_case, nullptr, &st);
+    const std::string msg = g_last_error;
+    P->inject_kerr = false;
+    // clear the flag so the problem stays usable
+    static const int kZero = 0;
+    CK(cudaMemcpyAsync(&P->S->kerr, &kZero, sizeof(int), cudaMemcpyHostToDevice, P->st));
+    CK(cudaStreamSynchronize(P->st));
+    *solve_status = (int)s;
+    g_last_error = msg;
     return AM_OK;
 }
 

@@ -220,7 +220,7 @@ am_status batch_solve(am_batch *B, int max_chunks) {
             if (B->Sh[p].status == ST_NAN)
                 return bfail(AM_ERR_NAN_DETECTED, "NaN in the PCG of batch problem " + std::to_string(p));
             if (B->Sh[p].status == ST_TIMEOUT)
-                return bfail(AM_ERR_CUDA, "a bulk-copy wait of the batched PCG update timed out");
+                return bfail(AM_ERR_TIMEOUT, "a bulk-copy wait of the batched PCG update timed out");
             B->pcg_its[p] += B->Sh[p].it;
         }
     }

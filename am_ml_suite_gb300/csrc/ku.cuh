@@ -303,8 +303,8 @@ __device__ __forceinline__ void ku_tile_body(KuArgs<T> A, const Blk B) {
                             A.y[n + c * cs] = q;
                             d0.add_prod(pcur[c], q);
                         }
-                    } else {  // RESID
-                        const T dv = A.dinv[n];
+                    } else {  // RESID (dinv nullable: r.(D^-1 r) is then 0)
+                        const T dv = A.dinv ? A.dinv[n] : T(0);
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             const T rr = ((m >> c) & 1u) ? T(0) : (T)(A.f[n + c * cs] - (double)val[c]);

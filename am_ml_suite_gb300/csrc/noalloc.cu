@@ -11,11 +11,13 @@
 // fixed size, present on every device that loads the library until exit.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <mutex>
 #include <string>
 
 #include "../../include/am_gpu.h"
 #include "kernels.cuh"
+#include "ku.cuh"
 
 using namespace amk;
 
@@ -24,6 +26,11 @@ namespace {
 // Largest number of K*u tiles one call may use: a tile covers 32 x 4 node columns
 // of the full z extent, so (nx+1)/32 * (ny+1)/4 (rounded up) must not exceed it.
 constexpr int kNoAllocMaxTiles = 32768;
+// The FP64 residual tile (32 x 4 node columns) must run without the opt-in to
+// more than 48 KB of dynamic shared memory: that opt-in is made when a problem
+// is created, and this entry point may be the first call into the library.
+static_assert(KuShape<32, 4>::smem_bytes<double>() <= 48 * 1024,
+              "the allocation-free residual relies on the default dynamic shared-memory limit");
 static __device__ __align__(256) double g_noalloc_partial[2 * kNoAllocMaxTiles];  // 512 KB
 static __device__ __align__(256) Scalars g_noalloc_scalars;
 
@@ -73,6 +80,14 @@ extern "C" am_status am_residual_noalloc(int nx, int ny, int nz, double h, doubl
                                          const double *scale, const double *u, const double *f,
                                          const uint8_t *mask, double *r, double *rr, void *stream) {
     if (nx < 1 || ny < 1 || nz < 1) return noalloc_fail(AM_ERR_INVALID_ARG, "grid dimensions must be >= 1");
+    if (nx >= INT_MAX || ny >= INT_MAX || nz >= INT_MAX)
+        return noalloc_fail(AM_ERR_INVALID_ARG, "grid dimensions must be < INT_MAX");
+    // tile count in 64-bit arithmetic, before any int-sized layout field is formed
+    const long long tiles = ((long long)nx + 1 + 31) / 32 * (((long long)ny + 1 + 3) / 4);
+    if (tiles > kNoAllocMaxTiles)
+        return noalloc_fail(AM_ERR_SIZE_MISMATCH,
+                            "grid too large for the fixed scratch: ceil((nx+1)/32)*ceil((ny+1)/4) = " +
+                                std::to_string(tiles) + " > " + std::to_string(kNoAllocMaxTiles));
     if (!(h > 0.0) || !(E0 > 0.0) || !(nu > -1.0 && nu < 0.5))
         return noalloc_fail(AM_ERR_INVALID_ARG, "need h > 0, E0 > 0, -1 < nu < 0.5");
     if (!scale || !u || !f || !mask || !r || !rr) return noalloc_fail(AM_ERR_INVALID_ARG, "null device pointer");
@@ -102,10 +117,8 @@ extern "C" am_status am_residual_noalloc(int nx, int ny, int nz, double h, doubl
     // must start at zero
     cudaError_t e = cudaMemsetAsync(d->scalars, 0, sizeof(Scalars), st);
     if (e != cudaSuccess) return noalloc_fail(AM_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
-    // The residual kernel also accumulates r.(w r) for a per-node weight w (the
-    // Jacobi start of a PCG); this entry point gives it u's first plane as w and
-    // discards that sum.
-    e = ku_resid(K, L, M, scale, u, f, u, mask, r, nullptr, d->partial, d->scalars, st);
+    // no Jacobi weight: the kernel's r.(D^-1 r) sum is not formed
+    e = ku_resid(K, L, M, scale, u, f, nullptr, mask, r, nullptr, d->partial, d->scalars, st);
     if (e != cudaSuccess) return noalloc_fail(AM_ERR_CUDA, std::string("residual kernel: ") + cudaGetErrorString(e));
     e = cudaMemcpyAsync(rr, &d->scalars->res_rr, sizeof(double), cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return noalloc_fail(AM_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));

@@ -255,6 +255,16 @@ am_status am_simp_get_density(am_problem *p, double *rho_out);
  * limit_ms when the wait gave up as it should. */
 am_status am_selftest_copy_wait(double limit_ms, int *timed_out, double *waited_ms);
 
+/* Self-test of the status a solve returns when one of its kernels reports that a
+ * bounded copy wait ran out (no reference counterpart).  No wait is made to run
+ * out: the flag such a kernel sets is set on the host before the first PCG
+ * chunk of am_solve(p, cfg, rho, load_case); every kernel then completes
+ * normally and the PCG ends at its first update with the timeout status.
+ * *solve_status receives what am_solve returned (AM_ERR_TIMEOUT), and the flag
+ * is cleared again so the problem stays usable. */
+am_status am_selftest_solve_timeout(am_problem *p, const am_simp_config *cfg, const double *rho, int load_case,
+                                    int *solve_status);
+
 /* Kernel launches this library has issued so far (CUDA-graph replays add the
  * kernel nodes they contain). */
 long long am_launch_count(void);
