@@ -59,6 +59,7 @@ class SimpConfig(ctypes.Structure):
         ("verbose", ctypes.c_int),
         ("mixed_solver", ctypes.c_int),
         ("mg_deflation", ctypes.c_int),
+        ("cpp_assembly_index", ctypes.c_int),
     ]
 
 
@@ -130,6 +131,23 @@ class RunMetadata(ctypes.Structure):
     ]
 
 
+class BracketParams(ctypes.Structure):
+    """Mirror of ``am_bracket_params``."""
+
+    _fields_ = [
+        ("size_mm", ctypes.c_double * 3),
+        ("resolution_mm", ctypes.c_double),
+        ("base_thickness_mm", ctypes.c_double),
+        ("hole_diameter_mm", ctypes.c_double),
+        ("hole_offset_mm", ctypes.c_double),
+        ("eyelet_diameter_mm", ctypes.c_double),
+        ("eyelet_offset_mm", ctypes.c_double),
+        ("eyelet_z_offset_mm", ctypes.c_double),
+        ("eyelet_height_mm", ctypes.c_double),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+    ]
+
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _i8p = ctypes.POINTER(ctypes.c_int8)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
@@ -185,6 +203,10 @@ SIGNATURES = {
     "am_precond_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
+    "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
+    "am_bracket_params_default": (None, [ctypes.POINTER(BracketParams), ctypes.c_double]),
+    "am_bracket_build": (ctypes.c_int, [ctypes.POINTER(BracketParams), _dp, ctypes.c_int, _i8p, _dp, _i64p, _i64p,
+                                        _i64p, _i64p, ctypes.c_int64]),
     "am_write_density_npy": (ctypes.c_int, [ctypes.c_char_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int]),
     "am_write_history_csv": (ctypes.c_int, [ctypes.c_char_p, _dp, _dp, ctypes.c_int]),
@@ -511,6 +533,15 @@ class Preconditioner:
         check(load().am_precond_eval(self.handle, int(first), int(count), int(loss), ctypes.byref(v)),
               "am_precond_eval")
         return v.value
+
+
+CONV_MMA_SYNC, CONV_TCGEN05 = 0, 1
+
+
+def set_conv_kernels(impl: int):
+    """Kernels of the network's convolutions: CONV_TCGEN05 (default) or the legacy
+    CONV_MMA_SYNC baseline."""
+    check(load().am_precond_set_kernels(int(impl)), "am_precond_set_kernels")
 
 
 class Batch:

@@ -49,6 +49,10 @@ class SIMPConfig:
     cg_max_iterations: int = 100000
     precision: int = nat.PREC_MIXED
     warm_start: bool = True
+    # True: element stiffness scales read the density list with the reference
+    # assembler's z-fastest index (global_assembler.hpp:162-164) like the reference
+    # engine, to replay its runs; False: every density at its own element
+    reference_assembly_index: bool = False
 
 
 @dataclass
@@ -109,7 +113,8 @@ class CPPTopologyOptimizer:
             filter_radius=float(c.filter_radius), move_limit=float(c.move_limit), rho_min=float(c.rho_min),
             E_min=float(c.E_min), convergence_tol=float(c.convergence_tol), max_iterations=int(c.max_iterations),
             precision=int(c.precision), cg_tol=float(c.cg_tol), cg_max_iterations=int(c.cg_max_iterations),
-            warm_start=int(bool(c.warm_start)), layout=nat.LAYOUT_XFASTEST)
+            warm_start=int(bool(c.warm_start)), layout=nat.LAYOUT_XFASTEST,
+            cpp_assembly_index=int(bool(c.reference_assembly_index)))
 
     def _set_loads(self, forces, fixed_dofs):
         F = np.ascontiguousarray(forces, dtype=np.float64).ravel()

@@ -270,7 +270,8 @@ am_status setup_operator(am_problem *P, const am_simp_config &c, const double *r
     P->rho_op = rho_dev;
     const int variant = c.variant;
     const int8_t *g = (variant == AM_VARIANT_PY && !P->grid_host.empty()) ? P->grid.p : nullptr;
-    CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st));
+    const int d1 = (variant == AM_VARIANT_CPP && c.cpp_assembly_index) ? 1 : 0;
+    CK(scales(P->L, rho_dev, g, variant, c.penalty, c.E_min, c.rho_min, P->E0, P->s64.p, P->s32.p, P->st, d1));
     P->pad_dirty = true;
     P->mg_dirty = true;
     return AM_OK;

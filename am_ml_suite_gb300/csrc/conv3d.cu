@@ -459,8 +459,13 @@ bool aligned8(const TensorView &t) { return t.cstride % 8 == 0 && t.coff % 8 == 
 
 }  // namespace
 
+static int g_conv_impl = 1;
+void conv3d_set_impl(int impl) { g_conv_impl = impl ? 1 : 0; }
+int conv3d_impl() { return g_conv_impl; }
+
 cudaError_t conv3d_fwd(const Grid5 &g, TensorView x, int cin, const __nv_bfloat16 *w, int cout, TensorView y,
                        TensorView yf, int relu, cudaStream_t st) {
+    if (g_conv_impl == 1) return conv3d_fwd_tc(g, x, cin, w, cout, y, yf, relu, st);
     if (cin % 16 || cout % 16 || !aligned8(x) || (y.p && (y.cstride % 2 || y.coff % 2)) ||
         (yf.p && (yf.cstride % 2 || yf.coff % 2)))
         return cudaErrorInvalidValue;
@@ -495,6 +500,7 @@ cudaError_t conv3d_fwd(const Grid5 &g, TensorView x, int cin, const __nv_bfloat1
 }
 
 cudaError_t conv3d_wgrad(const Grid5 &g, TensorView x, int cin, TensorView dy, int cout, float *dw, cudaStream_t st) {
+    if (g_conv_impl == 1) return conv3d_wgrad_tc(g, x, cin, dy, cout, dw, st);
     if (cin % 16 || cout % 16 || !aligned8(x) || !aligned8(dy)) return cudaErrorInvalidValue;
     WgArgs a{};
     a.x = static_cast<const __nv_bfloat16 *>(x.p);

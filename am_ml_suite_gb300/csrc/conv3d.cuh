@@ -24,8 +24,22 @@ struct Grid5 {
     long long voxels() const { return (long long)n * dz * dy * dx; }
 };
 
-// y = conv(x, w) [+ y if accumulate]; relu; output BF16 (y) and/or FP32 (yf).
-// Cin, Cout multiples of 16.
+// Which kernels the convolutions run on: 1 (the default) tcgen05.mma with TMEM
+// accumulators and tensor-copy staging (conv3d_tc.cu); 0 the legacy
+// mma.sync/ldmatrix/cp.async kernels (conv3d.cu), kept as the baseline the
+// tensor-core kernels are measured and checked against.
+void conv3d_set_impl(int impl);
+int conv3d_impl();
+// Error flag of the tensor-core kernels' bounded waits (1 = a wait ran out), read
+// after the work queued on `st`; clear resets it.
+cudaError_t conv3d_tc_error(int *flag, bool clear, cudaStream_t st);
+cudaError_t conv3d_fwd_tc(const Grid5 &g, TensorView x, int cin, const __nv_bfloat16 *w, int cout, TensorView y,
+                          TensorView yf, int relu, cudaStream_t st);
+cudaError_t conv3d_wgrad_tc(const Grid5 &g, TensorView x, int cin, TensorView dy, int cout, float *dw,
+                            cudaStream_t st);
+
+// y = conv(x, w); relu; output BF16 (y) and/or FP32 (yf).  Cin, Cout multiples
+// of 16.
 cudaError_t conv3d_fwd(const Grid5 &g, TensorView x, int cin, const __nv_bfloat16 *w, int cout, TensorView y,
                        TensorView yf, int relu, cudaStream_t st);
 // dw[tap][cout][cin] += sum_v dy[v][cout] x[v + tap][cin]   (FP32 atomics)

@@ -944,11 +944,18 @@ __device__ __forceinline__ double pow_fast(double x, double p) {
 
 __device__ __forceinline__ void scales_body(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
                               int variant, double p, double emin, double rho_min, double E,
-                              double *__restrict__ s64, float *__restrict__ s32, const Blk B) {
+                              double *__restrict__ s64, float *__restrict__ s32, int d1, const Blk B) {
     for (long long e = B.b * (long long)blockDim.x + threadIdx.x; e < L.nel;
          e += (long long)B.n * blockDim.x) {
         const int g = grid ? grid[e] : 0;
-        const double r = rho[e];
+        long long src = e;
+        if (d1) {
+            // the reference C++ assembler's density index i*ny*nz + j*nz + k
+            // applied to the optimizer's x-fastest vector (global_assembler.hpp:162-164)
+            const long long ex = e % L.nx, ey = (e / L.nx) % L.ny, ez = e / ((long long)L.nx * L.ny);
+            src = (ex * L.ny + ey) * L.nz + ez;
+        }
+        const double r = rho[src];
         double v;
         if (variant == 0) {
             if (g == -1 || r < rho_min) v = 0.0;
@@ -965,13 +972,13 @@ __device__ __forceinline__ void scales_body(Layout L, const double *__restrict__
 }
 __global__ void scales_kernel(Layout L, const double *__restrict__ rho, const int8_t *__restrict__ grid,
                               int variant, double p, double emin, double rho_min, double E,
-                              double *__restrict__ s64, float *__restrict__ s32) {
-    scales_body(L, rho, grid, variant, p, emin, rho_min, E, s64, s32, grid_blk());
+                              double *__restrict__ s64, float *__restrict__ s32, int d1) {
+    scales_body(L, rho, grid, variant, p, emin, rho_min, E, s64, s32, d1, grid_blk());
 }
 cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int variant, double p,
-                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st) {
+                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st, int d1) {
     const int nb = std::max(1, std::min(div_up(L.nel, 256), 152 * 16));
-    scales_kernel<<<nb, 256, 0, st>>>(L, rho, grid, variant, p, emin, rho_min, E, s64, s32);
+    scales_kernel<<<nb, 256, 0, st>>>(L, rho, grid, variant, p, emin, rho_min, E, s64, s32, d1);
     return counted(cudaGetLastError());
 }
 
@@ -1667,7 +1674,7 @@ __global__ void __launch_bounds__(256) b_scales_kernel(const BatchItem *items, W
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
-        scales_body(it.L, it.rho, nullptr, 0, it.penalty, it.emin, it.rho_min, 1.0, it.s64, it.s32,
+        scales_body(it.L, it.rho, nullptr, 0, it.penalty, it.emin, it.rho_min, 1.0, it.s64, it.s32, 0,
                     Blk{_k.y, it.n_elem});
     }
 }

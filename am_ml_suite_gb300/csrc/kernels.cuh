@@ -142,7 +142,7 @@ cudaError_t fcg_update(const Layout &L, double *x, double *r, const double *p, c
 // grid -1 or rho < rho_min -> 0, grid 1 -> 1, else emin + rho^p (1 - emin);
 // variant 1 (PY): grid -1 -> 0, grid 1 -> 1, else (emin + rho^p (E - emin))/E.
 cudaError_t scales(const Layout &L, const double *rho, const int8_t *grid, int variant, double p,
-                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st);
+                   double emin, double rho_min, double E, double *s64, float *s32, cudaStream_t st, int d1 = 0);
 // per-node inverse diagonal (KE[0][0] * sum of the adjacent scales), orphan DOFs
 // (|diag| < 1e-15) joined to the constrained bits of `fixed_bits`.
 cudaError_t diag_mask(const Layout &L, const double *s64, double d0, const uint8_t *fixed_bits,

@@ -62,6 +62,15 @@ am_status pfail(am_status s, const std::string &msg) {
 
 typedef __nv_bfloat16 bf16;
 
+// AM_ERR_TIMEOUT if a tensor-core convolution on `st` gave up a bounded wait
+am_status conv_status(cudaStream_t st) {
+    int f = 0;
+    PCK(conv3d_tc_error(&f, true, st));
+    if (f) return pfail(AM_ERR_TIMEOUT, "a bounded copy / MMA wait of a tensor-core convolution ran out");
+    return AM_OK;
+}
+
+
 struct LayerSpec {
     int cin, cout, cin_used, cout_used;
 };
@@ -636,7 +645,7 @@ am_status precond_apply(am_precond *M, const PrecondView &v, const double *r, do
     apply_out_kernel<<<eb(L.cs), 256, 0, v.st>>>(L, gz, gy, gx, r, dsq, v.mask, M->infer.out.p, M->acc.p, h[1], z);
     PCK(cudaGetLastError());
     count_launches(21 + 5);
-    return AM_OK;
+    return conv_status(v.st);
 }
 
 am_status precond_add_density(am_precond *M, const PrecondView &v, const Modal<float> &M32, const float *s32,
@@ -912,7 +921,7 @@ am_status am_precond_forward(am_precond *M, int n, int gz, int gy, int gx, const
     PCK(cudaGetLastError());
     PCK(cudaMemcpyAsync(out, M->hout.p, V * 3 * sizeof(float), cudaMemcpyDeviceToHost, M->st));
     PCK(cudaStreamSynchronize(M->st));
-    return AM_OK;
+    return conv_status(M->st);
 }
 
 am_status am_precond_param_grad(am_precond *M, int n, int gz, int gy, int gx, const float *in, const float *dout,
@@ -937,7 +946,7 @@ am_status am_precond_param_grad(am_precond *M, int n, int gz, int gy, int gx, co
     PCK(backward(M, A, M->st));
     PCK(cudaMemcpyAsync(grad, M->g.p, M->off[kLayers] * sizeof(float), cudaMemcpyDeviceToHost, M->st));
     PCK(cudaStreamSynchronize(M->st));
-    return AM_OK;
+    return conv_status(M->st);
 }
 
 am_status am_precond_bench_forward(am_precond *M, int n, int gz, int gy, int gx, int reps, double *avg_ms,
@@ -961,6 +970,7 @@ am_status am_precond_bench_forward(am_precond *M, int n, int gz, int gy, int gx,
     PCK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    PCKS(conv_status(M->st));
     if (avg_ms) *avg_ms = ms / reps;
     if (flops) {
         // 2 * 27 * cin * cout per voxel of each layer's grid (channels as computed)
@@ -1001,6 +1011,7 @@ am_status am_precond_train(am_precond *M, const am_train_config *cfg, float *epo
             tot += l;
             cnt += nb;
         }
+        PCKS(conv_status(M->st));
         if (epoch_loss) epoch_loss[ep] = cnt ? (float)(tot / cnt) : 0.f;
         if (cfg->verbose) std::printf("epoch %d: loss %.4e (%lld samples)\n", ep, cnt ? tot / cnt : 0.0, cnt);
     }
@@ -1022,7 +1033,13 @@ am_status am_precond_eval(am_precond *M, long long first, long long count, int l
         tot += l;
     }
     *mean_loss = tot / count;
-    return AM_OK;
+    return conv_status(M->st);
 }
 
 }  // extern "C"
+
+extern "C" am_status am_precond_set_kernels(int impl) {
+    if (impl != 0 && impl != 1) return pfail(AM_ERR_INVALID_ARG, "impl must be 0 (mma.sync) or 1 (tcgen05)");
+    conv3d_set_impl(impl);
+    return AM_OK;
+}

@@ -1,23 +1,26 @@
 #!/usr/bin/env python
-"""SIMP iterations/s and PCG solve ms at relative residual 1e-6 on GB300.
+"""SIMP iterations/s and PCG solve ms at relative residual 1e-6 on GB300:
+learned vs Jacobi PCG.
 
-Workload (default ``bracket192``): the 192x96x96 bracket -- 1,769,472 hex8
-elements, 5,447,811 DOF, E0 = 1, nu = 0.3, E_min = 1e-9, p = 3, vf = 0.3,
-rmin = 2.0 cone sensitivity filter, move 0.2, clamped x = 0 face, a passive void
-cylinder (radius 16 voxels through y, axis at the x-z centre, rho = 0) and four
-passive solid 6x6 bolt-pad columns (full height, inset 6 voxels from the x-y
-corners, rho = 1), 3 point loads on the top face at seeded random nodes
-(numpy default_rng(2)), magnitude U(0.5, 1.5), direction uniform on the sphere.
-FP64 flexible CG to rel-res 1e-6 preconditioned by FP32 Jacobi-PCG inner solves.
+Workload (default ``cantilever256``): the 256x128x128 cantilever -- 4,194,304
+hex8 elements, 12,830,211 DOF, E0 = 1, nu = 0.3, E_min = 1e-9, p = 3, vf = 0.25,
+rmin = 2.5 cone sensitivity filter, move 0.2, clamped x = 0 face, a -z load of
+total magnitude 1 spread over the 33x33 nodes of the central 32x32 element patch
+of the x = 256 face.  ``bracket192`` is the 192x96x96 bracket (void cylinder,
+four passive bolt-pad columns, 3 seeded point loads); ``batch256`` the 256
+seeded cantilevers of uneven sizes solved together.
 
-One step = one SIMP iteration (solve, sensitivities, filter, OC update).
-``value``: iterations/s over the timed steps with the state resident in HBM,
-timed with CUDA events on the library's stream.
-``e2e``: the same metric through the public C ABI from host buffers
-(``am_problem_set_loads`` + ``am_simp_run`` for W+K iterations, density
-downloaded).  The working set of a step (solver vectors + element arrays,
-~300 MB) exceeds the 129 MB L2, so no explicit flush is needed between steps;
-the roofline probe of the dominant kernel flushes L2 before each launch.
+One step = one SIMP iteration (solve, sensitivities, filter, OC update).  The
+solver arms (``--arms``; jacobi, learned, mg) each time SIMP steps 1..K of a
+fresh problem from the same initial density after W warm-up steps on a
+throwaway problem; every solve is accepted on its FP64 residual at 1e-6.
+``value``: iterations/s of the primary arm (Jacobi PCG, the method the reference
+arm runs on the CPU), timed with CUDA events on the library's stream;
+``arms`` holds every arm's rate, PCG solve ms, iterations and agreement with the
+Jacobi arm.  ``e2e``: the primary arm through the public C ABI from pinned host
+buffers (loads, network weights, am_simp_run for K iterations, density read
+back).  The working set of a step (solver vectors + element arrays, > 1 GB)
+exceeds the 129 MB L2; the roofline probes flush L2 before each launch.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -235,22 +238,6 @@ def run_batch(args, nat, world, rank):
         print(json.dumps(line))
 
 
-MIXED_SOLVER = {"reliable": 0, "flexible": 1}
-PRECOND = {"jacobi": 0, "mg": 2}
-_mixed_solver = "reliable"
-_inner_tol = 0.0
-_precond = "jacobi"
-_mg_deflation = 1
-
-
-def simp_config(nat, W, max_iterations=100):
-    return nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
-                              rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
-                              precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=_inner_tol,
-                              cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver],
-                              preconditioner=PRECOND[_precond], mg_deflation=_mg_deflation)
-
-
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -304,6 +291,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f).get("bf16_tflops", 1900.0))
+    return 1900.0
+
+
 def ku_traffic_per_launch(W, nodes, elements):
     """DRAM bytes per launch of the fused FP32 PCG K*u from the committed ncu
     summary (measured on a smaller case, scaled by nodes), or None."""
@@ -338,87 +333,236 @@ def cpu_baseline(W, steps_gpu_its, pcg_iters_sample=20):
             "phases_s": times}
 
 
-def measured_pcg_iterations(workload):
-    """PCG iterations per SIMP iteration measured by this GB300 arm on the same
-    workload and steps (committed with the profiles), or None."""
-    p = os.path.join(ROOT, "profiles", "pcg_iterations.json")
-    if not os.path.exists(p):
-        return None
-    with open(p) as f:
-        d = json.load(f)
-    e = d.get(workload)
-    return None if e is None else float(e["pcg_iterations_per_solve"])
+
+
+METRIC = "SIMP iters/s and PCG solve ms @ rel-res 1e-6: learned vs Jacobi PCG, 1×GB300"
+
+# Solver arms of one bench line.  jacobi: one FP32 Jacobi-PCG sequence with FP64
+# residual replacement; learned: the FP64 flexible CG preconditioned by the trained
+# conv3d network (Jacobi PCG its fallback on stagnation); mg: the multigrid V-cycle
+# in the FP64 flexible CG.  Every solve of every arm is accepted on its FP64
+# residual at rel-res 1e-6.
+ARM_DESC = {
+    "jacobi": "FP32 Jacobi PCG with FP64 residual replacement (mixed precision)",
+    "learned": "FP64 flexible CG preconditioned by the trained conv3d encoder-decoder, FP32 Jacobi-PCG refinement",
+    "mg": "FP64 flexible CG preconditioned by the FP32 multigrid V-cycle",
+}
+_inner_tol = 0.0
+_mg_deflation = 1
+_mixed_solver = "reliable"
+MIXED_SOLVER = {"reliable": 0, "flexible": 1}
+
+
+def simp_config(nat, W, max_iterations=100, arm="jacobi"):
+    c = nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
+                           rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=max_iterations,
+                           precision=nat.PREC_MIXED, cg_tol=1e-6, warm_start=1, inner_tol=_inner_tol,
+                           cg_max_iterations=200000, mixed_solver=MIXED_SOLVER[_mixed_solver],
+                           mg_deflation=_mg_deflation)
+    if arm == "learned":
+        c.preconditioner = nat.PRECOND_LEARNED
+        c.mixed_solver = nat.MIXED_FLEXIBLE
+    elif arm == "mg":
+        c.preconditioner = nat.PRECOND_MG
+    return c
+
+
+def reference_sample(W, n_pcg, pcg_iters_sample=10):
+    """Projected seconds of one SIMP iteration of the CPU restatement: one bounded
+    sample (CSR assembly, `pcg_iters_sample` Jacobi-PCG iterations, sensitivities,
+    filter, OC on the full workload) with the PCG phase scaled to n_pcg iterations."""
+    import oracle as O
+
+    prm = O.make_params(volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2, rho_min=0.01,
+                        E_min=1e-9)
+    times, threads = O.baseline_sample(W["shape"], prm, W["rho0"].ravel(), W["F"], W["fixed"], pcg_iters_sample)
+    s = (times["assembly"] + times["pcg_setup"] + n_pcg * times["pcg_iteration"] + times["sensitivities"] +
+         times["filter"] + times["oc"])
+    return s, times, threads
+
+
+def reference_whole_iteration(W):
+    """One whole C++-variant SIMP iteration (the first, from the workload's initial
+    density) of the CPU restatement: CSR assembly, FP64 Jacobi PCG from zero to
+    rel-res 1e-6, sensitivities, filter, OC.  Returns (seconds, PCG iterations)."""
+    import oracle as O
+
+    prm = O.make_params(volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2, rho_min=0.01,
+                        E_min=1e-9, convergence_tol=0.0, max_iterations=1, cg_tol=1e-6, cg_maxit=200000,
+                        warm_start=0, use_csr=1)
+    t0 = time.perf_counter()
+    r = O.simp_cpp(W["shape"], 1.0, 1.0, 0.3, prm, W["rho0"], W["F"], W["fixed"])
+    return time.perf_counter() - t0, int(r["cg_iters"][0])
 
 
 def run_reference(args, W):
-    import oracle as O  # noqa: F401
-
-    # bounded sample per step: one timed sample of the CPU restatement per step,
-    # extrapolated with the PCG iteration count the GB300 arm measured (same
-    # method and tolerance), so both arms do the same number of PCG iterations
+    """The reference arm: the CPU restatement of the reference's C++ SIMP loop
+    (topology_optimizer.cpp:294-520 with Jacobi PCG, the preconditioner the metric
+    names) on all host cores.  SIMP iteration 1 is run whole, which gives the PCG
+    iteration count of a solve from zero to rel-res 1e-6; each step is then one
+    bounded sample projected with that count (the reference solves every
+    iteration from zero, linear_solver.cpp:136-155)."""
+    t_whole, n_pcg = reference_whole_iteration(W)
     vals = []
     sample = None
-    its = measured_pcg_iterations(args.workload)
-    if its is None:
-        its = float(os.environ.get("AM_BENCH_PCG_ITS", "2000"))
-    for _ in range(max(1, args.warmup)):
-        cpu_baseline(W, its, 5)
+    for _ in range(args.warmup):
+        reference_sample(W, n_pcg, 2)
     t0 = time.time()
     for _ in range(args.steps):
-        cb = cpu_baseline(W, its, 10)
-        vals.append(cb["value"])
-        sample = cb
+        s, times, threads = reference_sample(W, n_pcg)
+        vals.append(1.0 / s)
+        sample = (times, threads)
     wall = time.time() - t0
     value = statistics.median(vals)
-    line = {"metric": "SIMP iters/s @ rel-res 1e-6 (Jacobi PCG)", "value": value, "unit": "SIMP iters/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "shape": list(W["shape"]), "description": W["desc"]},
-            "cpu_baseline": {"value": value, "unit": "SIMP iters/s", "cores": sample["cores"], "kind": "port",
-                             "sample": sample["sample"]},
+    times, threads = sample
+    desc = (f"SIMP iteration 1 run whole on the FP64 CPU restatement ({n_pcg} Jacobi-PCG iterations to rel-res "
+            f"1e-6, {t_whole:.1f} s); each step a bounded sample (CSR assembly, 10 PCG iterations, sensitivities, "
+            f"filter, OC on the full workload) with the PCG phase projected to {n_pcg} iterations")
+    line = {"metric": METRIC, "value": value, "unit": "SIMP iters/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "shape": list(W["shape"]), "description": W["desc"],
+                       "preconditioner": "jacobi", "cg_tol": 1e-6},
+            "projected": True, "pcg_iterations_per_solve": n_pcg, "pcg_solve_ms": 1000.0 * n_pcg *
+            times["pcg_iteration"], "whole_iteration_1": {"s": t_whole, "pcg_iterations": n_pcg},
+            "cpu_baseline": {"value": value, "unit": "SIMP iters/s", "cores": threads, "kind": "port",
+                             "sample": desc, "phases_s": times},
             "e2e": {"value": value, "unit": "SIMP iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
     print(json.dumps(line))
 
 
+def time_arm(nat, torch, W, arm, steps, pre=None, keep=False):
+    """SIMP steps 1..`steps` of a fresh problem with the arm's solver, timed with
+    CUDA events on the library's stream (allocation and set-up of the fresh state
+    included).  Returns the per-step results and, if keep, the open problem."""
+    p = nat.Problem(W["shape"], 1.0, 1.0, 0.3)
+    p.set_loads([W["F"]], [W["fixed"]])
+    if pre is not None:
+        p.set_preconditioner(pre)
+    cfg = simp_config(nat, W, max_iterations=max(steps, 1), arm=arm)
+    stream = torch.cuda.ExternalStream(p.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = nat.launch_count()
+    ev0.record(stream)
+    p.simp_begin(cfg, W["rho0"])
+    res = [p.simp_step() for _ in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = nat.launch_count() - l0
+    s = ev0.elapsed_time(ev1) * 1e-3
+    rho = p.simp_density()
+    out = {"s": s, "value": steps / s, "ms_per_step": 1000.0 * s / steps,
+           "pcg_solve_ms": 1000.0 * statistics.mean(r.solve_time_s for r in res),
+           "pcg_iterations_per_solve": statistics.mean(r.solver_iterations for r in res),
+           "outer_iterations_per_solve": statistics.mean(r.solver_outer_iterations for r in res),
+           "learned_applications_per_solve": statistics.mean(r.solver_learned_applications for r in res),
+           "solver_residual_max": max(r.solver_residual for r in res),
+           "compliance": [r.compliance for r in res], "gpu_launches": int(launches), "density": rho}
+    if keep:
+        return out, p
+    p.close()
+    return out, None
+
+
+def arm_summary(a, ref=None):
+    keys = ["value", "ms_per_step", "pcg_solve_ms", "pcg_iterations_per_solve", "outer_iterations_per_solve",
+            "learned_applications_per_solve", "solver_residual_max", "gpu_launches"]
+    d = {k: a[k] for k in keys}
+    d["compliance_last"] = a["compliance"][-1]
+    if ref is not None and ref is not a:
+        c, cr = np.array(a["compliance"]), np.array(ref["compliance"])
+        d["compliance_rel_diff_vs_jacobi_max"] = float(np.max(np.abs(c - cr) / np.abs(cr)))
+        d["density_max_abs_diff_vs_jacobi"] = float(np.max(np.abs(a["density"] - ref["density"])))
+    return d
+
+
+def e2e_run(nat, torch, W, arm, iterations, pre_weights=None):
+    """The same metric through the C ABI from pinned host buffers: problem loads,
+    (the network's weights,) am_simp_run for `iterations` SIMP iterations and the
+    density read back, all inside the timed region."""
+    def pinned(a, dtype):
+        t = torch.empty(a.size, dtype=dtype, pin_memory=True)
+        arr = t.numpy()
+        arr[:] = a.ravel()
+        return arr, t
+
+    nel = int(np.prod(W["shape"]))
+    F_h, _tF = pinned(W["F"], torch.float64)
+    fx_h, _tx = pinned(W["fixed"].astype(np.int64), torch.int64)
+    r0_h, _tr = pinned(W["rho0"], torch.float64)
+    out_h, _to = pinned(np.zeros(nel), torch.float64)
+    w_h = None
+    if pre_weights is not None:
+        w_h, _tw = pinned(pre_weights, torch.float32)
+    cfg = simp_config(nat, W, max_iterations=iterations, arm=arm)
+    q = nat.Problem(W["shape"], 1.0, 1.0, 0.3)
+    pre = nat.Preconditioner(seed=0, capacity=0) if w_h is not None else None
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    q.set_loads([F_h], [fx_h])
+    if pre is not None:
+        pre.set_params(w_h)
+        q.set_preconditioner(pre)
+    r = q.simp_run(cfg, r0_h)
+    out_h[:] = r["density"]
+    te1 = time.perf_counter()
+    q.close()
+    if pre is not None:
+        pre.close()
+    h2d = F_h.nbytes + fx_h.nbytes + r0_h.nbytes + (0 if w_h is None else w_h.nbytes)
+    d2h = out_h.nbytes + 3 * 8 * iterations
+    return {"value": iterations / (te1 - te0), "unit": "SIMP iters/s",
+            "h2d_bytes_per_step": int(h2d / iterations), "d2h_bytes_per_step": int(d2h / iterations),
+            "iterations": iterations, "wall_s": te1 - te0, "arm": arm,
+            "note": "am_problem_set_loads" + (" + am_precond_set_params" if w_h is not None else "") +
+                    " + am_simp_run from pinned host buffers, density read back; a fresh problem (SIMP steps 1..K)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="bracket192", choices=sorted(WORKLOADS) + ["batch256"])
+    ap.add_argument("--workload", default="cantilever256", choices=sorted(WORKLOADS) + ["batch256"])
+    ap.add_argument("--arms", default="jacobi,learned,mg",
+                    help="comma-separated solver arms timed from the same start: jacobi, learned, mg")
+    ap.add_argument("--primary", default="jacobi",
+                    help="the arm whose rate is `value` (default jacobi: the method the reference arm runs on the "
+                         "CPU, so the two lines compare like for like; the other arms are in `arms`)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd", "filter", "oc",
-                                        "vcycle", "vcycle_defl"],
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd",
+                                        "filter", "oc", "vcycle", "vcycle_defl"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--compare-mg", action="store_true",
                     help="time --steps SIMP iterations with the Jacobi and the multigrid mixed-precision solvers "
                          "from the same start and report the ratio and the compliance / density agreement")
     ap.add_argument("--compare-fp64", action="store_true",
-                    help="time --steps SIMP iterations in mixed precision and in FP64 plain Jacobi from the same "
-                         "start and report the ratio and the compliance / density agreement")
+                    help="time --steps SIMP iterations of --arms' first arm in mixed precision and of FP64 plain "
+                         "Jacobi PCG from the same start and report the ratio and the agreement")
     ap.add_argument("--inner-tol", type=float, default=0.0,
                     help="mixed precision: residual reduction between FP64 replacements / per inner solve "
                          "(0: the solver's default, 0.1 reliable / 0.01 flexible)")
-    ap.add_argument("--precond", default="jacobi", choices=sorted(PRECOND),
-                    help="jacobi: Jacobi PCG (the headline); mg: multigrid V-cycle in the FP64 flexible CG")
     ap.add_argument("--mg-deflation", type=int, default=1, choices=[0, 1],
                     help="multigrid: balance the V-cycle with the rigid-body modes of the passive solid "
                          "inclusions (1, the default) or not (0)")
     ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
-                    help="mixed precision: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
+                    help="jacobi arm: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
                          "flexible CG over FP32 inner solves (flexible)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global _mixed_solver, _inner_tol, _precond, _mg_deflation
+    global _mixed_solver, _inner_tol, _mg_deflation
     _mixed_solver = args.mixed_solver
     _mg_deflation = args.mg_deflation
     _inner_tol = args.inner_tol
-    _precond = args.precond
+    arms = [a for a in args.arms.split(",") if a]
+    for a in arms:
+        if a not in ARM_DESC:
+            raise SystemExit(f"unknown arm {a}")
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -448,6 +592,7 @@ def main():
         return
 
     from am_ml_suite_gb300 import _build, _native as nat
+    from am_ml_suite_gb300 import learned
 
     _build.build()
     nat.load()
@@ -456,55 +601,32 @@ def main():
     if args.workload == "batch256":
         run_batch(args, nat, world, rank)
         return
+    import torch
+
+    torch.cuda.init()
     shape = W["shape"]
-    cfg = simp_config(nat, W)
 
-    if args.compare_mg:
-        import torch
+    weights = learned.load_weights() if "learned" in arms else None
+    pre = None
+    if weights is not None:
+        pre = nat.Preconditioner(seed=0, capacity=0)
+        pre.set_params(weights)
+    elif "learned" in arms:
+        arms.remove("learned")
 
+    if args.compare_mg or args.compare_fp64:
+        if args.compare_mg:
+            pairs = [("jacobi", "jacobi", nat.PREC_MIXED), ("mg", "mg", nat.PREC_MIXED)]
+        else:
+            pairs = [(arms[0], arms[0], nat.PREC_MIXED), ("fp64", "jacobi", nat.PREC_FP64)]
         out = {}
-        for name, pc in (("jacobi", nat.PRECOND_JACOBI), ("mg", nat.PRECOND_MG)):
+        for name, arm, prec in pairs:
             p = nat.Problem(shape, 1.0, 1.0, 0.3)
             p.set_loads([W["F"]], [W["fixed"]])
-            c = simp_config(nat, W, max_iterations=args.steps)
-            c.preconditioner = pc
-            p.simp_begin(c, W["rho0"])
-            st = torch.cuda.ExternalStream(p.stream())
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record(st)
-            res = [p.simp_step() for _ in range(args.steps)]
-            e1.record(st)
-            torch.cuda.synchronize()
-            out[name] = dict(s=e0.elapsed_time(e1) * 1e-3, comp=np.array([r.compliance for r in res]),
-                             its=[r.solver_iterations for r in res], res=max(r.solver_residual for r in res),
-                             outer=[r.solver_outer_iterations for r in res], rho=p.simp_density())
-            p.close()
-        j, m = out["jacobi"], out["mg"]
-        rel = np.abs(m["comp"] - j["comp"]) / np.abs(j["comp"])
-        print(json.dumps({
-            "metric": "SIMP s/iteration: mixed precision, multigrid vs Jacobi preconditioner, same GPU",
-            "workload": args.workload, "steps": args.steps, "jacobi_s_per_step": j["s"] / args.steps,
-            "mg_s_per_step": m["s"] / args.steps, "speedup": j["s"] / m["s"],
-            "compliance_rel_diff_max": float(rel.max()), "compliance_rel_diff_final": float(rel[-1]),
-            "compliance_final": float(j["comp"][-1]),
-            "density_max_abs_diff": float(np.max(np.abs(m["rho"] - j["rho"]))),
-            "pcg_iterations_jacobi_mean": float(np.mean(j["its"])), "pcg_iterations_mg_mean": float(np.mean(m["its"])),
-            "mg_deflation": _mg_deflation, "mg_iterations": m["its"], "mg_outer_iterations": m["outer"],
-            "residual_max": max(j["res"], m["res"])}))
-        return
-
-    if args.compare_fp64:
-        import torch
-
-        out = {}
-        for name, prec in (("mixed", nat.PREC_MIXED), ("fp64", nat.PREC_FP64)):
-            p = nat.Problem(shape, 1.0, 1.0, 0.3)
-            p.set_loads([W["F"]], [W["fixed"]])
-            c = simp_config(nat, W)
+            if arm == "learned":
+                p.set_preconditioner(pre)
+            c = simp_config(nat, W, max_iterations=args.steps, arm=arm)
             c.precision = prec
-            if prec == nat.PREC_FP64:
-                c.preconditioner = nat.PRECOND_JACOBI  # the plain FP64 Jacobi-PCG GPU path
             p.simp_begin(c, W["rho0"])
             st = torch.cuda.ExternalStream(p.stream())
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -517,27 +639,27 @@ def main():
                              its=[r.solver_iterations for r in res], res=max(r.solver_residual for r in res),
                              rho=p.simp_density())
             p.close()
-        m, f = out["mixed"], out["fp64"]
+        (na, a), (nb, b) = list(out.items())
+        rel = np.abs(a["comp"] - b["comp"]) / np.abs(b["comp"])
         print(json.dumps({
-            "metric": "SIMP s/iteration: mixed precision (FP32 PCG with FP64 residual replacement, or the FP64 flexible CG "
-                      "over FP32 inner solves: mixed_solver) vs FP64 plain Jacobi PCG, same GPU",
-            "mixed_solver": _mixed_solver, "inner_tol": _inner_tol, "preconditioner": _precond,
-            "workload": args.workload, "steps": args.steps, "mixed_s_per_step": m["s"] / args.steps,
-            "fp64_s_per_step": f["s"] / args.steps, "speedup": f["s"] / m["s"],
-            "compliance_rel_diff_max": float(np.max(np.abs(m["comp"] - f["comp"]) / np.abs(f["comp"]))),
-            "density_max_abs_diff": float(np.max(np.abs(m["rho"] - f["rho"]))),
-            "pcg_iterations_mixed": m["its"], "pcg_iterations_fp64": f["its"],
-            "residual_max": max(m["res"], f["res"])}))
+            "compare": f"{na} vs {nb}", "workload": args.workload, "steps": args.steps,
+            f"{na}_s_per_step": a["s"] / args.steps, f"{nb}_s_per_step": b["s"] / args.steps,
+            "speedup": b["s"] / a["s"] if na != "jacobi" or nb == "fp64" else a["s"] / b["s"],
+            "compliance_rel_diff_max": float(rel.max()), "compliance_rel_diff_final": float(rel[-1]),
+            "compliance_final": float(b["comp"][-1]),
+            "density_max_abs_diff": float(np.max(np.abs(a["rho"] - b["rho"]))),
+            f"pcg_iterations_{na}": a["its"], f"pcg_iterations_{nb}": b["its"],
+            f"compliance_{na}": a["comp"].tolist(), f"compliance_{nb}": b["comp"].tolist(),
+            "mg_deflation": _mg_deflation, "residual_max": max(a["res"], b["res"])}))
         return
 
     if args.probe == "conv":
         # forward passes of the learned preconditioner on this workload's node grid
-        pre = nat.Preconditioner(seed=0, capacity=0)
+        pc = nat.Preconditioner(seed=0, capacity=0)
         nx, ny, nz = shape
         g = [(v + 1 + 7) // 8 * 8 for v in (nz, ny, nx)]
-        ms, flops = pre.bench_forward(1, g[0], g[1], g[2], reps=args.reps)
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peak = float(json.load(f).get("bf16_tflops", 1900.0))
+        ms, flops = pc.bench_forward(1, g[0], g[1], g[2], reps=args.reps)
+        peak = measured_bf16_peak()
         tf = flops / (ms * 1e-3) / 1e12
         print(json.dumps({"probe": "conv", "workload": args.workload, "grid_zyx": g, "reps": args.reps,
                           "ms_per_forward": ms, "tflops": tf, "bf16_peak_tflops": peak, "frac": tf / peak}))
@@ -547,9 +669,7 @@ def main():
         # set-up only, then `reps` launches of one kernel (L2 flushed before each)
         p = nat.Problem(shape, 1.0, 1.0, 0.3)
         p.set_loads([W["F"]], [W["fixed"]])
-        p.simp_begin(cfg, W["rho0"])
-        # ku: the staged PCG K*u the solver runs; ku2: the register-direct kernel it
-        # replaced; ku3s3: the staged kernel with 3 stages instead of 4
+        p.simp_begin(simp_config(nat, W), W["rho0"])
         which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7,
                  "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11}[args.probe]
         if which in (8, 9):
@@ -561,125 +681,108 @@ def main():
                           "min_ms": mn, "nodes": lay["nodes"], "elements": lay["elements"]}))
         return
 
-    import torch
+    primary = args.primary if args.primary in arms else arms[0]
+    if primary not in arms:
+        raise SystemExit(f"primary arm {primary} is not timed")
 
-    torch.cuda.init()
+    # ---- warm-up: W SIMP steps of every arm on throwaway problems -----------
+    for arm in arms:
+        time_arm(nat, torch, W, arm, args.warmup, pre=pre if arm == "learned" else None)
 
-    # ---- device-resident timed region --------------------------------------
-    p = nat.Problem(shape, 1.0, 1.0, 0.3)
-    p.set_loads([W["F"]], [W["fixed"]])
-    p.simp_begin(cfg, W["rho0"])
-    warm = [p.simp_step() for _ in range(args.warmup)]
-    lay = p.layout_info()
-    # CUDA events on the stream the library launches on
-    lib_stream = torch.cuda.ExternalStream(p.stream())
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # ---- timed: SIMP steps 1..K of a fresh problem per arm ------------------
     if world > 1:
         import torch.distributed as dist
 
         dist.barrier()
     torch.cuda.synchronize()
-    l0 = nat.launch_count()
+    results, keep_p = {}, None
     with ClockSampler(0) as clk:
-        ev0.record(lib_stream)
-        res = [p.simp_step() for _ in range(args.steps)]
-        ev1.record(lib_stream)
-        torch.cuda.synchronize()
-    l1 = nat.launch_count()
+        for arm in arms:
+            r, p = time_arm(nat, torch, W, arm, args.steps, pre=pre if arm == "learned" else None,
+                            keep=arm == primary)
+            results[arm] = r
+            if p is not None:
+                keep_p = p
     if world > 1:
         dist.barrier()
-    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    elapsed = results[primary]["s"]
     if world > 1:
         t = torch.tensor([elapsed], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
     value = world * args.steps / elapsed
-    pcg_ms = 1000.0 * statistics.mean(r.solve_time_s for r in res)
-    pcg_its = statistics.mean(r.solver_iterations for r in res)
 
-    # ---- roofline of the dominant kernel (fused FP32 PCG K*u) ---------------
+    # ---- rooflines: the inner PCG's K*u and vector update, the network ------
+    lay = keep_p.layout_info()
     nodes, nel = lay["nodes"], lay["elements"]
-    ku_ms, ku_min = p.bench_kernel(0, reps=20, flush_l2=True)
-    # reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B), scale
-    # (4 B per element); writes p, q (3 x 4 B each per node)
-    alg_bytes = 53 * nodes + 4 * nel
+    ku_ms, ku_min = keep_p.bench_kernel(0, reps=20, flush_l2=True)
+    res_ms, _ = keep_p.bench_kernel(1, reps=5, flush_l2=True)
+    upd_ms, upd_min = keep_p.bench_kernel(2, reps=20, flush_l2=True)
+    keep_p.close()
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (ku_ms * 1e-3) / 1e9
-    traffic = ku_traffic_per_launch(W, nodes, nel)
-    res_ms, _ = p.bench_kernel(1, reps=5, flush_l2=True)
-    upd_ms, upd_min = p.bench_kernel(2, reps=20, flush_l2=True)
-    # the other half of a PCG iteration, averaged over the even / odd pair the
-    # timed launches alternate between: an even iteration reads r, q (3 x 4 B each
-    # per node) and dinv (4 B) and writes r (40 B per node); an odd one also reads
-    # the double-float iterate (3 x 8 B), p_prev and p (3 x 4 B each) and writes
-    # the iterate (112 B per node)
+    # ku3: reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B),
+    # scale (4 B per element); writes p, q (3 x 4 B each per node)
+    alg_bytes = 53 * nodes + 4 * nel
+    ku_roof = {"bound": "hbm", "kernel": "ku3_kernel<8,4> (tensor-copy staged p-update + FP32 K*p + p.q)",
+               "achieved": alg_bytes / (ku_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+               "frac": alg_bytes / (ku_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+               "traffic": ku_traffic_per_launch(W, nodes, nel), "algorithmic_bytes": alg_bytes,
+               "avg_ms": ku_ms, "min_ms": ku_min}
+    # the update averaged over its even / odd pair: 40 / 112 B per node
     upd_bytes = 76 * nodes
-    p.close()
+    upd_roof = {"bound": "hbm",
+                "kernel": "pcg_update_df_kernel (double-float iterate folded every 2nd iteration, bulk-copy staged)",
+                "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": upd_bytes / (upd_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": upd_bytes,
+                "avg_ms": upd_ms, "min_ms": upd_min}
+    roof = ku_roof
+    conv_roof = None
+    if "learned" in arms:
+        nx, ny, nz = shape
+        g = [(v + 1 + 7) // 8 * 8 for v in (nz, ny, nx)]
+        fwd_ms, flops = pre.bench_forward(1, g[0], g[1], g[2], reps=5)
+        bf16 = measured_bf16_peak()
+        tf = flops / (fwd_ms * 1e-3) / 1e12
+        conv_roof = {"bound": "tensor", "kernel": "conv3d forward (15 BF16 3x3x3 convolutions of the network)",
+                     "achieved": tf, "peak": bf16, "unit": "TFLOP/s", "frac": tf / bf16, "peak_kind": "measured",
+                     "traffic": None, "algorithmic_flops": flops, "avg_ms": fwd_ms}
+        if primary == "learned":
+            la = results["learned"]
+            net_s = la["learned_applications_per_solve"] * fwd_ms
+            pcg_s = la["pcg_iterations_per_solve"] * (ku_ms + upd_ms)
+            if net_s > pcg_s:
+                roof = conv_roof
 
     # ---- end to end through the C ABI from host buffers ---------------------
     e2e = None
     if not args.no_e2e:
-        total = args.warmup + args.steps
-        ecfg = simp_config(nat, W, max_iterations=total)
-        try:
-            def pinned(a, dtype):
-                t = torch.empty(a.size, dtype=dtype, pin_memory=True)
-                arr = t.numpy()
-                arr[:] = a.ravel()
-                return arr, t
-
-            F_h, _tF = pinned(W["F"], torch.float64)
-            fx_h, _tx = pinned(W["fixed"].astype(np.int64), torch.int64)
-            r0_h, _tr = pinned(W["rho0"], torch.float64)
-            out_h, _to = pinned(np.zeros(nel), torch.float64)
-        except Exception:
-            F_h, fx_h, r0_h, out_h = W["F"], W["fixed"].astype(np.int64), W["rho0"].ravel(), np.zeros(nel)
-        q = nat.Problem(shape, 1.0, 1.0, 0.3)
-        te0 = time.perf_counter()
-        q.set_loads([F_h], [fx_h])
-        r = q.simp_run(ecfg, r0_h)
-        out_h[:] = r["density"]
-        te1 = time.perf_counter()
-        q.close()
-        h2d = F_h.nbytes + fx_h.nbytes + r0_h.nbytes
-        d2h = out_h.nbytes + 3 * 8 * total
-        e2e = {"value": world * total / (te1 - te0), "unit": "SIMP iters/s",
-               "h2d_bytes_per_step": int(h2d / total), "d2h_bytes_per_step": int(d2h / total),
-               "iterations": total, "wall_s": te1 - te0,
-               "note": "am_problem_set_loads + am_simp_run from host buffers, cold start included"}
+        e2e = e2e_run(nat, torch, W, primary, args.steps, pre_weights=weights if primary == "learned" else None)
+        e2e["value"] *= world
 
     cpu = None
-    # the CPU restatement runs Jacobi PCG: its extrapolation needs Jacobi iteration counts
-    if not args.no_cpu_baseline and rank == 0 and _precond == "jacobi":
-        cpu = cpu_baseline(W, pcg_its)
+    if not args.no_cpu_baseline and rank == 0 and "jacobi" in results:
+        cpu = cpu_baseline(W, results["jacobi"]["pcg_iterations_per_solve"])
 
     if rank == 0:
+        ref = results.get("jacobi")
         line = {
-            "metric": ("SIMP iters/s @ rel-res 1e-6 (Jacobi PCG); PCG solve ms in pcg_solve_ms" if _precond == "jacobi"
-                       else "SIMP iters/s @ rel-res 1e-6 (multigrid-preconditioned flexible CG); solve ms in "
-                            "pcg_solve_ms"),
-            "value": value, "unit": "SIMP iters/s", "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": value, "unit": "SIMP iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": args.workload, "shape": list(shape), "dof": 3 * nodes, "elements": nel,
-                       "description": W["desc"], "precision": "mixed", "mixed_solver": _mixed_solver, "preconditioner": _precond,
-                       **({"mg_deflation": _mg_deflation} if _precond == "mg" else {}),
-                       "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probe flushes L2",
+                       "description": W["desc"], "precision": "mixed", "primary_arm": primary,
+                       "arms": {a: ARM_DESC[a] for a in arms}, "window": "SIMP steps 1..K of a fresh problem",
+                       "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probes flush L2",
                        "parallelism": f"replicas x{world}"},
-            "pcg_solve_ms": pcg_ms, "pcg_iterations_per_solve": pcg_its,
-            "solver_residual_max": max(r.solver_residual for r in res),
-            "compliance_last": res[-1].compliance,
-            "roofline": {"bound": "hbm", "kernel": "ku3_kernel<8,4> (tensor-copy staged p-update + FP32 K*p + p.q)",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
-                         "avg_ms": ku_ms, "min_ms": ku_min},
+            "pcg_solve_ms": results[primary]["pcg_solve_ms"],
+            "pcg_iterations_per_solve": results[primary]["pcg_iterations_per_solve"],
+            "solver_residual_max": max(r["solver_residual_max"] for r in results.values()),
+            "compliance_last": results[primary]["compliance"][-1],
+            "arms": {a: arm_summary(r, ref) for a, r in results.items()},
+            "roofline": roof,
             "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_fp64": res_ms, "pcg_update_fp32": upd_ms},
-            "roofline_update": {"bound": "hbm", "kernel": "pcg_update_df_kernel (double-float iterate folded every 2nd iteration, bulk-copy staged)",
-                                "achieved": upd_bytes / (upd_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                                "frac": upd_bytes / (upd_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": upd_bytes,
-                                "avg_ms": upd_ms, "min_ms": upd_min},
-            "gpu_launches": int(l1 - l0),
+            "roofline_ku": ku_roof, "roofline_update": upd_roof, "roofline_conv": conv_roof,
+            "gpu_launches": results[primary]["gpu_launches"],
             "clocks": clk.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,

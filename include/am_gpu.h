@@ -115,6 +115,12 @@ typedef struct am_simp_config {
                                  held at density 1), whose near-free motion once their
                                  surroundings turn void no coarse grid represents; 0: the
                                  V-cycle alone */
+    int cpp_assembly_index;   /* AM_VARIANT_CPP: 1 builds the element stiffness scales the way the
+                                 reference C++ engine does, reading the density vector with the
+                                 assembler's z-fastest element index (global_assembler.hpp:162-164)
+                                 although the optimizer stores it x-fastest
+                                 (topology_optimizer.hpp:218-232) -- for replaying runs of
+                                 am_topopt; 0 (the default) reads every density at its own element */
 } am_simp_config;
 
 /* Per-solve statistics (SolveStats, linear_solver.hpp:48-56). */
@@ -338,6 +344,13 @@ am_status am_precond_param_grad(am_precond *m, int n, int gz, int gy, int gx, co
  * voxel summed over the layers (measurement; no reference counterpart). */
 am_status am_precond_bench_forward(am_precond *m, int n, int gz, int gy, int gx, int reps, double *avg_ms,
                                    double *flops);
+/* Selects the kernels of every convolution of the network, process-wide:
+ * impl 1 (the default) tcgen05.mma with tensor-memory accumulators and tiled
+ * tensor-copy staging; impl 0 the legacy mma.sync/ldmatrix/cp.async kernels,
+ * kept as the baseline the tensor-core kernels are checked and timed against.
+ * A tensor-core convolution whose bounded wait runs out makes the call that ran
+ * it return AM_ERR_TIMEOUT. */
+am_status am_precond_set_kernels(int impl);
 /* Adds training samples: at density rho (host, cfg->layout) the problem's FP32
  * Jacobi PCG runs from u = 0 on load case `load_case`; the residual r_k and the
  * error e_k = u* - u_k after each iteration count k in iters[0..n_iters)
@@ -409,6 +422,42 @@ am_status am_batch_get_density(am_batch *b, double *rho_out);
 am_status am_batch_simp_run(am_batch *b, const am_simp_config *cfgs, const double *rho0, double *rho_out,
                             double *compliance_hist, double *volume_hist, int *iterations, int *converged,
                             long long *pcg_iterations);
+
+/* ---- problem set-up: the reference's BRK-A-01 bracket ------------------------------
+ * The voxel grid of create_bracket_domain (src/am/core/geometry.py:79-196; the C++
+ * driver's BracketDomain, cpp_engine/src/am_topopt.cpp:98-239) and the loads of
+ * create_brk_a_01_static_case_1/2 (src/am/core/loads.py:163-306; createForceVector /
+ * createFixedDofs, am_topopt.cpp:248-334), computed by device kernels and returned
+ * in caller-owned host buffers, identical cell for cell and DOF for DOF to the
+ * reference's. */
+typedef struct am_bracket_params {
+    double size_mm[3];          /* bounding box (x, y, z) */
+    double resolution_mm;       /* voxel edge */
+    double base_thickness_mm;   /* flange: fixed element layers int(t / res), at least 1 */
+    double hole_diameter_mm;    /* four void holes through the flange ... */
+    double hole_offset_mm;      /* ... int(offset / res) elements from the x and y edges */
+    double eyelet_diameter_mm;  /* void hole of the eyelet (axis along z at (nx/2, ny/2)) */
+    double eyelet_offset_mm;    /* fixed ring of material around it; also the pillar radius */
+    double eyelet_z_offset_mm;  /* eyelet centre below the top */
+    double eyelet_height_mm;    /* eyelet extent in z */
+    int nx, ny, nz;             /* grid (the reference: int(size_mm / resolution_mm) per axis;
+                                   the load builders take the caller's domain shape) */
+} am_bracket_params;
+
+/* The reference defaults (geometry.py:79-86, am_topopt.cpp:47-63) at the given
+ * resolution, with nx, ny, nz = int(size_mm / resolution_mm). */
+void am_bracket_params_default(am_bracket_params *p, double resolution_mm);
+
+/* Every output is nullable.  grid: nx*ny*nz cells -1 void / 0 design / 1 fixed in
+ * `layout`.  F: 3 (nx+1)(ny+1)(nz+1) forces in the reference DOF order,
+ * total_force[3] spread evenly over the load ring of the eyelet (static case 1:
+ * (0, 0, -15000); case 2: (10000 sin 30, 0, -10000 cos 30) computed by the caller).
+ * fixed / n_fixed: the 3 (nx+1)(ny+1) DOFs of the nodes at z = 0, ascending.
+ * load_nodes / n_load_nodes: the ring's node indices in the reference's loop order
+ * (load_nodes_capacity entries available; too few -> AM_ERR_SIZE_MISMATCH). */
+am_status am_bracket_build(const am_bracket_params *p, const double total_force[3], int layout, int8_t *grid,
+                           double *F, int64_t *fixed, int64_t *n_fixed, int64_t *load_nodes,
+                           int64_t *n_load_nodes, int64_t load_nodes_capacity);
 
 /* ---- result writers (host only) ----------------------------------------------------
  * The output files of the reference's C++ driver (cpp_engine/src/am_topopt.cpp), with

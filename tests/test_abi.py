@@ -56,7 +56,7 @@ def test_config_defaults(lib):
             c.max_iterations, c.convergence_tol) == (0.25, 3.0, 2.0, 0.2, 0.01, 1e-6, 100, 0.01)
     p = nat.default_config(nat.VARIANT_PY)
     assert p.E_min == 1e-9 and p.variant == nat.VARIANT_PY
-    assert ctypes.sizeof(nat.SimpConfig) == 120  # sizeof(am_simp_config) on LP64
+    assert ctypes.sizeof(nat.SimpConfig) == 120  # sizeof(am_simp_config) on LP64 (wrapper_check prints it)
 
 
 def test_status_strings(lib):

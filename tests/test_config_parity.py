@@ -1,0 +1,139 @@
+"""Parity at the benchmark configurations, on the GPU, against FP64 solves.
+
+The reference densities come from the benched path itself (mixed precision,
+Jacobi PCG with FP64 residual replacement, rel-res 1e-6, warm starts): 5 SIMP
+steps of the 192x96x96 bracket (config 2) and of a 64x32x32 cantilever with the
+256x128x128 cantilever's load pattern (config 5 downscaled).  At each step's
+density the displacement and the compliance u.F of a mixed solve are compared
+with an FP64-accepted solve to rel-res 1e-11 (flexible CG with the multigrid
+V-cycle, accepted on the FP64 residual; on the cantilever also the pure FP64
+Jacobi PCG path).
+
+What a relative residual bounds (measured on GB300 on these densities): the
+cantilever is well conditioned -- at rel-res 1e-6 both displacement and
+compliance agree with the tight solve to <= 5e-7.  The bracket is not: its
+passive solid pads end up floating in near-void material (stiffness contrast
+1e6), and their near-rigid motion is almost free of energy, so rel-res 1e-6
+leaves displacement errors of up to 3 % for every solver -- the FP64 plain
+Jacobi path included (29 %) -- while compliance, an energy, stays within 1.5e-6.
+The bracket test therefore checks the benchmark spec bounds (displacement and
+compliance <= 1e-6 against FP64) at rel-res 1e-10, where the mixed path meets
+them with margin, and checks at the benched rel-res 1e-6 that compliance stays
+within the 2e-6 that FP64 PCG itself reaches there."""
+import numpy as np
+import pytest
+
+from am_ml_suite_gb300 import _native as nat
+
+pytestmark = pytest.mark.gpu
+
+
+def _bracket192():
+    import bench
+
+    return bench.build_workload("bracket192")
+
+
+def _cantilever64():
+    """64x32x32 with config 5's loads: -z load of total 1 over the nodes of the
+    central 8x8 element patch of the x = 64 face; vf 0.25, rmin 2.5."""
+    nx, ny, nz = 64, 32, 32
+    node = lambda i, j, k: (i * (ny + 1) + j) * (nz + 1) + k  # noqa: E731
+    base = np.array([node(0, j, k) for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(3 * (nx + 1) * (ny + 1) * (nz + 1))
+    j0, k0 = ny // 2 - 4, nz // 2 - 4
+    nodes = [node(nx, j, k) for j in range(j0, j0 + 9) for k in range(k0, k0 + 9)]
+    F[3 * np.array(nodes) + 2] = -1.0 / len(nodes)
+    return dict(shape=(nx, ny, nz), rmin=2.5, vf=0.25, F=F, fixed=fixed, rho0=np.full((nx, ny, nz), 0.25))
+
+
+def _cfg(W, **kw):
+    c = nat.default_config(nat.VARIANT_CPP, volume_fraction=W["vf"], filter_radius=W["rmin"], move_limit=0.2,
+                           rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=100, cg_tol=1e-6,
+                           cg_max_iterations=400000)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def _trajectory(W, steps):
+    p = nat.Problem(W["shape"])
+    p.set_loads([W["F"]], [W["fixed"]])
+    p.simp_begin(_cfg(W), W["rho0"])
+    dens = [np.asarray(W["rho0"], dtype=np.float64).copy()]
+    for _ in range(steps - 1):
+        p.simp_step()
+        dens.append(p.simp_density().reshape(W["shape"]).copy())
+    p.close()
+    return dens
+
+
+def _errors(W, q, rho, uref, cref, **kw):
+    u, st = q.solve(_cfg(W, warm_start=0, **kw), rho)
+    assert st.converged and st.residual <= kw.get("cg_tol", 1e-6)
+    return (float(np.linalg.norm(u - uref) / np.linalg.norm(uref)), float(abs(W["F"] @ u - cref) / abs(cref)))
+
+
+def _reference(W, q, rho):
+    uref, sref = q.solve(_cfg(W, precision=nat.PREC_FP64, preconditioner=nat.PRECOND_MG, cg_tol=1e-11,
+                              warm_start=0), rho)
+    assert sref.converged and sref.residual <= 1e-11
+    return uref, float(W["F"] @ uref)
+
+
+def test_cantilever_config5_shape_mixed_solves_match_fp64():
+    W = _cantilever64()
+    q = nat.Problem(W["shape"])
+    q.set_loads([W["F"]], [W["fixed"]])
+    for k, rho in enumerate(_trajectory(W, 5)):
+        uref, cref = _reference(W, q, rho)
+        # the pure FP64 Jacobi-PCG path agrees with the multigrid FP64 reference
+        d64, c64 = _errors(W, q, rho, uref, cref, precision=nat.PREC_FP64, cg_tol=1e-10)
+        assert d64 <= 1e-7 and c64 <= 1e-9, (k, d64, c64)
+        d, c = _errors(W, q, rho, uref, cref, cg_tol=1e-6)
+        assert d <= 1e-6 and c <= 1e-6, (k, d, c)
+
+
+def test_bracket192_mixed_solves_match_fp64():
+    W = _bracket192()
+    q = nat.Problem(W["shape"])
+    q.set_loads([W["F"]], [W["fixed"]])
+    for k, rho in enumerate(_trajectory(W, 5)):
+        uref, cref = _reference(W, q, rho)
+        d, c = _errors(W, q, rho, uref, cref, cg_tol=1e-10)
+        assert d <= 1e-6 and c <= 1e-6, (k, d, c)
+        d6, c6 = _errors(W, q, rho, uref, cref, cg_tol=1e-6)
+        assert c6 <= 2e-6, (k, d6, c6)
+
+
+def test_cfg1_multigrid_and_jacobi_densities_after_50_iterations():
+    """Config 1 (48x24x12), 50 OC iterations at rel-res 1e-6 per solve: the
+    multigrid and Jacobi preconditioners change iteration counts and time, not
+    the design -- final densities within 1e-4 of each other and of the FP64
+    oracle (solved to 1e-12)."""
+    import oracle as O
+
+    shape = (48, 24, 12)
+    nx, ny, nz = shape
+    N = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(N)
+    line = np.array([nx * (ny + 1) * (nz + 1) + j * (nz + 1) + nz // 2 for j in range(ny + 1)])
+    F[3 * line + 2] = -1.0 / len(line)
+    prm = O.make_params(volume_fraction=0.3, filter_radius=1.5, move_limit=0.2, rho_min=0.01, E_min=1e-9,
+                        convergence_tol=0.0, max_iterations=50, cg_tol=1e-12, warm_start=1)
+    ref = O.simp_cpp(shape, 1.0, 1.0, 0.3, prm, np.full(shape, 0.3), F, fixed)
+    out = {}
+    for name, pc in (("jacobi", nat.PRECOND_JACOBI), ("mg", nat.PRECOND_MG)):
+        p = nat.Problem(shape)
+        p.set_loads([F], [fixed])
+        cfg = nat.default_config(nat.VARIANT_CPP, volume_fraction=0.3, filter_radius=1.5, move_limit=0.2,
+                                 rho_min=0.01, E_min=1e-9, convergence_tol=0.0, max_iterations=50, cg_tol=1e-6,
+                                 preconditioner=pc)
+        out[name] = p.simp_run(cfg, np.full(shape, 0.3))
+        p.close()
+    for name, r in out.items():
+        assert np.abs(r["density"] - ref["density"].ravel()).max() <= 1e-4, name
+    assert np.abs(out["mg"]["density"] - out["jacobi"]["density"]).max() <= 1e-4
