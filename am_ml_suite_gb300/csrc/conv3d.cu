@@ -389,18 +389,22 @@ __global__ void avgpool_bwd_kernel(int N, int dz, int dy, int dx, const __nv_bfl
     }
 }
 
+// one thread per (fine voxel, 8 channels): 16-byte copies (channel strides and
+// offsets are multiples of 8)
 __global__ void upsample_fwd_kernel(int N, int dz, int dy, int dx, const __nv_bfloat16 *in, int ics, int ico,
                                     __nv_bfloat16 *out, int ocs, int oco, int c) {
     const long long V = (long long)N * dz * dy * dx;
-    const long long total = V * c;
+    const int g = c / 8;
+    const long long total = V * g;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
-        const long long v = i / c;
-        const int ch = (int)(i % c);
+        const long long v = i / g;
+        const int ch = (int)(i - v * g) * 8;
         int n, z, y, x;
         unflatten(v, dx, dy, dz, n, z, y, x);
         const long long cv = (((long long)n * (dz / 2) + z / 2) * (dy / 2) + y / 2) * (dx / 2) + x / 2;
-        out[v * ocs + oco + ch] = in[cv * ics + ico + ch];
+        *reinterpret_cast<uint4 *>(out + v * ocs + oco + ch) =
+            *reinterpret_cast<const uint4 *>(in + cv * ics + ico + ch);
     }
 }
 
@@ -561,7 +565,8 @@ cudaError_t avgpool2_bwd(const Grid5 &g, TensorView dout, TensorView din, int c,
 }
 
 cudaError_t upsample2_fwd(const Grid5 &g, TensorView in, TensorView out, int c, cudaStream_t st) {
-    upsample_fwd_kernel<<<ew_blocks(g.voxels() * c), 256, 0, st>>>(
+    if (c % 8 || in.cstride % 8 || in.coff % 8 || out.cstride % 8 || out.coff % 8) return cudaErrorInvalidValue;
+    upsample_fwd_kernel<<<ew_blocks(g.voxels() * (c / 8)), 256, 0, st>>>(
         g.n, g.dz, g.dy, g.dx, static_cast<const __nv_bfloat16 *>(in.p), in.cstride, in.coff,
         static_cast<__nv_bfloat16 *>(out.p), out.cstride, out.coff, c);
     return cudaGetLastError();

@@ -68,7 +68,7 @@ __device__ __forceinline__ void raise_err(int *err) {
 // the next tile's MMAs and copies.  A K step stages CW channels of one tap: a
 // 128-voxel box of the input and the N x CW weights, in the K-major layout with
 // CW*2-byte swizzled rows; it feeds CW / 16 MMAs of 128 x N x 16.
-constexpr int kMaxStages = 16;
+constexpr int kMaxStages = 32;
 constexpr int kFwdThreads = 192;
 
 __host__ __device__ constexpr int stage_bytes_fwd2(int n, int cw) {
@@ -253,6 +253,226 @@ __global__ void __launch_bounds__(kFwdThreads, 1) conv_tc_fwd_kernel(const __gri
     if (warp == 0) tc::tmem_free(tmem, TCOLS);
 }
 
+// ---- plane-marching forward (small channel counts) --------------------------------
+// A CTA owns an 8 (x) x 16 (y) column of output voxels and a run of z planes of
+// one batch entry and marches up z.  Input planes z0-1 .. z1 (10 x 18 voxels: the
+// column with its halo) pass through a ring of MR shared-memory slots, one tiled
+// copy per 8 channels landing in the no-swizzle K-major layout (voxel rows of 16
+// bytes, x fastest).  For output plane z the A operand of tap (dx, dy, dz) is
+// then the slot of plane z+dz read from ((1+dx) + 10 (1+dy)) voxels on: 8
+// consecutive x rows form a core matrix and the 16 y rows follow 10 voxels (160
+// bytes) apart, the uniform group stride of the descriptor -- no data moves per
+// tap.  The 27 x cin x N weights stay resident for the CTA's whole life.  Warp
+// roles and the double-buffered accumulator are those of the persistent kernel.
+constexpr int kMarchRing = 4;
+constexpr int kPlaneHalf = 2944;  // bytes of one 8-channel half of a staged plane (180 x 16, padded to 128)
+
+template <int N, int CIN>
+__global__ void __launch_bounds__(kFwdThreads, 1) conv_tc_march_kernel(const __grid_constant__ CUtensorMap mx,
+                                                                       const __grid_constant__ CUtensorMap mw,
+                                                                       TcFwdArgs A, int tiles_y16, int zrun,
+                                                                       int nitems) {
+    constexpr int KCH = CIN / 16;
+    constexpr int SLOT = KCH * 2 * kPlaneHalf;
+    constexpr int WBYTES = 27 * KCH * 2 * N * 16;
+    constexpr uint32_t TCOLS = 2 * N <= 32 ? 32 : 2 * N <= 64 ? 64 : 128;
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t pfull[kMarchRing], pempty[kMarchRing], wfull, acc_full[2], acc_empty[2], drain;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int aborted;
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *wsm = smem;                           // weights [27][KCH][2 halves][N][16 B]
+    uint8_t *ring = smem + (WBYTES + 1023) / 1024 * 1024;  // [MR][KCH][2][kPlaneHalf]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    volatile int &stop = aborted;
+    if (A.err && *reinterpret_cast<volatile int *>(A.err)) return;
+
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, TCOLS);
+    if (tid == 32) {
+        for (int r = 0; r < kMarchRing; ++r) {
+            bulk::bar_init(&pfull[r], 1);
+            bulk::bar_init(&pempty[r], 1);
+        }
+        bulk::bar_init(&wfull, 1);
+        for (int b = 0; b < 2; ++b) {
+            bulk::bar_init(&acc_full[b], 1);
+            bulk::bar_init(&acc_empty[b], 4);
+        }
+        bulk::bar_init(&drain, 1);
+        bulk::bar_init_fence();
+        aborted = 0;
+        tc::prefetch_map(&mx);
+        tc::prefetch_map(&mw);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+    const int tz_runs = (A.dz + zrun - 1) / zrun;
+    // work item -> (x tile, y tile, z run, batch entry)
+    auto item = [&](int it, int &x0, int &y0, int &z0, int &z1, int &nb) {
+        int b = it;
+        const int tx = b % A.tiles_x;
+        b /= A.tiles_x;
+        const int ty = b % tiles_y16;
+        b /= tiles_y16;
+        const int tzr = b % tz_runs;
+        nb = b / tz_runs;
+        x0 = tx * 8;
+        y0 = ty * 16;
+        z0 = tzr * zrun;
+        z1 = min(z0 + zrun, A.dz);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            bulk::bar_expect(&wfull, WBYTES);
+            for (int t = 0; t < 27; ++t)
+                for (int kc = 0; kc < KCH; ++kc)
+                    for (int h = 0; h < 2; ++h)
+                        tc::load_3d(wsm + ((t * KCH + kc) * 2 + h) * N * 16, &mw, kc * 16 + h * 8, 0, t, &wfull);
+            long long G = 0, issued = 0;
+            for (int it = blockIdx.x; it < nitems && !stop; it += gridDim.x) {
+                int x0, y0, z0, z1, nb;
+                item(it, x0, y0, z0, z1, nb);
+                for (int j = 0; j < z1 - z0 + 2; ++j, ++G) {
+                    const int r = (int)(G % kMarchRing);
+                    const long long use = G / kMarchRing;
+                    if (use > 0 && !wait(&pempty[r], (unsigned)((use - 1) & 1))) {
+                        stop = 1;
+                        break;
+                    }
+                    uint8_t *slot = ring + r * SLOT;
+                    bulk::bar_expect(&pfull[r], KCH * 2 * 2880);
+                    for (int kc = 0; kc < KCH; ++kc)
+                        for (int h = 0; h < 2; ++h)
+                            tc::load_5d(slot + (kc * 2 + h) * kPlaneHalf, &mx, kc * 16 + h * 8, x0 - 1, y0 - 1,
+                                        z0 - 1 + j, nb, &pfull[r]);
+                    issued = G + 1;
+                }
+            }
+            for (long long q = issued > kMarchRing ? issued - kMarchRing : 0; q < issued; ++q)
+                wait(&pfull[q % kMarchRing], (unsigned)((q / kMarchRing) & 1));
+            wait(&wfull, 0);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            if (!wait(&wfull, 0)) stop = 1;
+            long long G0 = 0;  // global index of the item's first plane
+            int i = 0;         // accumulator uses (output planes) so far
+            for (int it = blockIdx.x; it < nitems && !stop; it += gridDim.x) {
+                int x0, y0, z0, z1, nb;
+                item(it, x0, y0, z0, z1, nb);
+                const int S = z1 - z0;
+                long long ready = G0;  // planes G0 .. ready-1 are known to be full
+                for (int s = 0; s < S && !stop; ++s, ++i) {
+                    for (; ready <= G0 + s + 2; ++ready)
+                        if (!wait(&pfull[ready % kMarchRing], (unsigned)((ready / kMarchRing) & 1))) {
+                            stop = 1;
+                            break;
+                        }
+                    const int buf = i & 1;
+                    if (!stop && i >= 2 && !wait(&acc_empty[buf], (unsigned)(((i >> 1) - 1) & 1))) stop = 1;
+                    if (stop) break;
+                    tc::fence_after_sync();
+                    const uint32_t d = tmem + (uint32_t)(buf * N);
+                    // descriptors of the three planes z-1, z, z+1 and of the weights; a tap
+                    // adds a constant to the start-address field (addresses stay < 256 KB)
+                    const int r0 = (int)((G0 + s) & (kMarchRing - 1));
+                    uint64_t pd[3];
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        pd[q] = tc::smem_desc(ring + ((r0 + q) & (kMarchRing - 1)) * SLOT, kPlaneHalf, 160);
+                    const uint64_t wd = tc::smem_desc(wsm, N * 16, 128);
+#pragma unroll
+                    for (int t = 0; t < 27; ++t) {
+                        const int off = ((1 + t % 3 - 1) + 10 * (1 + (t / 3) % 3 - 1)) * 16;
+#pragma unroll
+                        for (int kc = 0; kc < KCH; ++kc)
+                            tc::mma_bf16(d, pd[t / 9] + (uint64_t)((kc * 2 * kPlaneHalf + off) >> 4),
+                                         wd + (uint64_t)(((t * KCH + kc) * 2 * N * 16) >> 4), IDESC,
+                                         (t > 0 || kc > 0) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&acc_full[buf]);
+                    tc::mma_commit(&pempty[(G0 + s) % kMarchRing]);  // plane z-1 of this output plane is done
+                }
+                if (stop) break;
+                // the item's last two planes
+                tc::mma_commit(&pempty[(G0 + S) % kMarchRing]);
+                tc::mma_commit(&pempty[(G0 + S + 1) % kMarchRing]);
+                G0 += S + 2;
+            }
+            tc::mma_commit(&drain);
+        }
+    } else {
+        const int q = warp & 3;
+        const int m = q * 32 + lane;
+        int i = 0;
+        for (int it = blockIdx.x; it < nitems && !stop; it += gridDim.x) {
+            int x0, y0, z0, z1, nb;
+            item(it, x0, y0, z0, z1, nb);
+            for (int z = z0; z < z1; ++z, ++i) {
+                const int buf = i & 1;
+                if (!wait(&acc_full[buf], (unsigned)((i >> 1) & 1)) || stop) {
+                    if (lane == 0) stop = 1;
+                    break;
+                }
+                tc::fence_after_sync();
+                const int x = x0 + (m & 7), y = y0 + (m >> 3);
+                const bool in = x < A.dx && y < A.dy;
+                const long long vox = (((long long)nb * A.dz + z) * A.dy + y) * A.dx + x;
+#pragma unroll
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    float v[16];
+                    tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N + c0), v);
+                    if (!in) continue;
+                    if (A.y) {
+                        uint4 pk[2];
+                        uint32_t *w = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+                        for (int t = 0; t < 8; ++t) {
+                            float a = v[2 * t], bb = v[2 * t + 1];
+                            if (A.relu) {
+                                a = fmaxf(a, 0.f);
+                                bb = fmaxf(bb, 0.f);
+                            }
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(a, bb);
+                            w[t] = *reinterpret_cast<const uint32_t *>(&h2);
+                        }
+                        uint4 *dst = reinterpret_cast<uint4 *>(A.y + vox * A.ycs + A.yco + c0);
+                        dst[0] = pk[0];
+                        dst[1] = pk[1];
+                    }
+                    if (A.yf) {
+                        float4 *dst = reinterpret_cast<float4 *>(A.yf + vox * A.yfcs + A.yfco + c0);
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            float4 o = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]);
+                            if (A.relu) {
+                                o.x = fmaxf(o.x, 0.f);
+                                o.y = fmaxf(o.y, 0.f);
+                                o.z = fmaxf(o.z, 0.f);
+                                o.w = fmaxf(o.w, 0.f);
+                            }
+                            dst[t] = o;
+                        }
+                    }
+                }
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
+            }
+        }
+    }
+    __syncwarp();
+    wait(&drain, 0);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (stop && tid == 0) raise_err(A.err);
+    if (warp == 0) tc::tmem_free(tmem, TCOLS);
+}
+
 // ---- backward-weight ------------------------------------------------------------
 // A CTA: one tap, one 128-row block of output channels (M), all input channels
 // (N = cin <= 256, in one MMA per 16 voxels), a run of `boxes_per_cta` voxel
@@ -415,6 +635,23 @@ bool act_map(CUtensorMap *m, const Grid5 &g, TensorView t, int channels, int box
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the same map with the staged-plane box of the plane-marching kernel: 8
+// channels x 10 x 18 voxels x 1 plane
+bool plane_map(CUtensorMap *m, const Grid5 &g, TensorView t, int channels) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t cs = (cuuint64_t)t.cstride * 2;
+    const cuuint64_t dims[5] = {(cuuint64_t)channels, (cuuint64_t)g.dx, (cuuint64_t)g.dy, (cuuint64_t)g.dz,
+                                (cuuint64_t)g.n};
+    const cuuint64_t strides[4] = {cs, cs * g.dx, cs * g.dx * g.dy, cs * g.dx * g.dy * g.dz};
+    const cuuint32_t box[5] = {8, 10, 18, 1, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const void *base = static_cast<const __nv_bfloat16 *>(t.p) + t.coff;
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // BF16 weights [27][rows][cols]: box of box_c columns x `rows` rows of one tap
 bool weight_map(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int cols, int box_c = 8,
                 CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_NONE) {
@@ -431,11 +668,24 @@ bool weight_map(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int cols, int 
 
 int *g_err = nullptr;  // device error flag of the bounded waits (per process, device 0 context)
 
+int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
 template <int N, int CW>
 cudaError_t launch_fwd(const CUtensorMap &mx, const CUtensorMap &mw, const TcFwdArgs &a, int ntiles,
                        cudaStream_t st) {
     constexpr int STAGE = stage_bytes_fwd2(N, CW);
-    const int stages = std::max(2, std::min(kMaxStages, (200 * 1024) / STAGE));
+    // two CTAs per SM where their accumulators fit the 512 TMEM columns together
+    constexpr int per_sm = 2 * N <= 256 ? 2 : 1;
+    const int stages = std::max(2, std::min(kMaxStages, (per_sm == 2 ? 104 : 200) * 1024 / STAGE));
     const int smem = stages * STAGE + 1024;
     static bool attr = false;
     if (!attr) {
@@ -444,15 +694,35 @@ cudaError_t launch_fwd(const CUtensorMap &mx, const CUtensorMap &mw, const TcFwd
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
-    const int grid = std::min(ntiles, sms);
+    const int grid = std::min(ntiles, per_sm * sm_count());
     conv_tc_fwd_kernel<N, CW><<<grid, kFwdThreads, smem, st>>>(mx, mw, a, ntiles, stages);
+    return cudaGetLastError();
+}
+
+template <int N, int CIN>
+cudaError_t launch_march(const CUtensorMap &mx, const CUtensorMap &mw, const TcFwdArgs &a, const Grid5 &g,
+                         cudaStream_t st) {
+    constexpr int KCH = CIN / 16;
+    constexpr int WBYTES = 27 * KCH * 2 * N * 16;
+    const int smem = (WBYTES + 1023) / 1024 * 1024 + kMarchRing * KCH * 2 * kPlaneHalf + 1024;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(conv_tc_march_kernel<N, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int sms = sm_count();
+    const int ty16 = (g.dy + 15) / 16;
+    const long long columns = (long long)a.tiles_x * ty16 * g.n;
+    // about four work items per CTA, runs of at least 4 planes
+    const long long runs = std::max<long long>(1, std::min<long long>((4LL * sms + columns - 1) / columns,
+                                                                      (g.dz + 3) / 4));
+    const int zrun = (int)((g.dz + runs - 1) / runs);
+    const long long nitems = columns * ((g.dz + zrun - 1) / zrun);
+    if (nitems > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const int grid = (int)std::min<long long>(nitems, sms);
+    conv_tc_march_kernel<N, CIN><<<grid, kFwdThreads, smem, st>>>(mx, mw, a, ty16, zrun, (int)nitems);
     return cudaGetLastError();
 }
 
@@ -510,6 +780,38 @@ cudaError_t conv3d_fwd_tc(const Grid5 &g, TensorView x, int cin, const __nv_bflo
         (yf.p && (yf.cstride % 4 || yf.coff % 4 || (reinterpret_cast<uintptr_t>(yf.p) & 15))) ||
         x.coff + cin > x.cstride)
         return cudaErrorInvalidValue;
+    if (cin <= 48 && cout <= 32) {
+        // small channel counts: the plane-marching kernel (weights resident, planes reused by all taps)
+        CUtensorMap mx, mw;
+        if (!plane_map(&mx, g, x, cin) || !weight_map(&mw, w, cout, cin)) return cudaErrorInvalidValue;
+        TcFwdArgs a{};
+        a.y = static_cast<__nv_bfloat16 *>(y.p);
+        a.ycs = y.cstride;
+        a.yco = y.coff;
+        a.yf = static_cast<float *>(yf.p);
+        a.yfcs = yf.cstride;
+        a.yfco = yf.coff;
+        a.dz = g.dz;
+        a.dy = g.dy;
+        a.dx = g.dx;
+        a.tiles_x = (g.dx + 7) / 8;
+        a.tiles_y = (g.dy + 15) / 16;
+        a.tiles_z = g.dz;
+        a.cin = cin;
+        a.relu = relu;
+        cudaError_t e = err_flag(&a.err);
+        if (e != cudaSuccess) return e;
+        const int key = cin * 1000 + cout;
+        switch (key) {
+            case 16016: return launch_march<16, 16>(mx, mw, a, g, st);
+            case 16032: return launch_march<32, 16>(mx, mw, a, g, st);
+            case 32016: return launch_march<16, 32>(mx, mw, a, g, st);
+            case 32032: return launch_march<32, 32>(mx, mw, a, g, st);
+            case 48016: return launch_march<16, 48>(mx, mw, a, g, st);
+            case 48032: return launch_march<32, 48>(mx, mw, a, g, st);
+            default: break;
+        }
+    }
     // channels per K step: 64 (128-byte swizzled rows) where cin allows, else 32 or 16
     const int cw = cin % 64 == 0 ? 64 : cin % 32 == 0 ? 32 : 16;
     const CUtensorMapSwizzle sw = cw == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
