@@ -204,6 +204,21 @@ SIGNATURES = {
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
+    "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.POINTER(_vp)]),
+    "am_unet_destroy": (ctypes.c_int, [_vp]),
+    "am_unet_num_params": (ctypes.c_longlong, [_vp]),
+    "am_unet_get_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "am_unet_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "am_unet_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "am_unet_param_grad": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                          ctypes.POINTER(ctypes.c_float)]),
+    "am_unet_set_data": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _u8p]),
+    "am_unet_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
+    "am_unet_eval": (ctypes.c_int, [_vp, _dp]),
     "am_bracket_params_default": (None, [ctypes.POINTER(BracketParams), ctypes.c_double]),
     "am_bracket_build": (ctypes.c_int, [ctypes.POINTER(BracketParams), _dp, ctypes.c_int, _i8p, _dp, _i64p, _i64p,
                                         _i64p, _i64p, ctypes.c_int64]),
@@ -532,6 +547,84 @@ class Preconditioner:
         v = ctypes.c_double(0.0)
         check(load().am_precond_eval(self.handle, int(first), int(count), int(loss), ctypes.byref(v)),
               "am_precond_eval")
+        return v.value
+
+
+class UNet:
+    """Owns an ``am_unet`` handle: the density-predicting 3-D U-Net."""
+
+    def __init__(self, in_channels=4, out_channels=1, f0=32, seed=0):
+        h = _vp()
+        check(load().am_unet_create(int(in_channels), int(out_channels), int(f0), int(seed), ctypes.byref(h)),
+              "am_unet_create")
+        self.handle = h
+        self.in_channels, self.out_channels, self.f0 = int(in_channels), int(out_channels), int(f0)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().am_unet_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return int(load().am_unet_num_params(self.handle))
+
+    def get_params(self) -> np.ndarray:
+        w = np.zeros(self.num_params, np.float32)
+        check(load().am_unet_get_params(self.handle, w.ctypes.data_as(_fp)), "am_unet_get_params")
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.size != self.num_params:
+            raise ValueError("parameter count mismatch")
+        check(load().am_unet_set_params(self.handle, w.ctypes.data_as(_fp)), "am_unet_set_params")
+
+    def forward(self, x, sigmoid=True):
+        """x: (n, gz, gy, gx, in_channels) -> (n, gz, gy, gx, out_channels)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n, gz, gy, gx, c = x.shape
+        if c != self.in_channels:
+            raise ValueError("input channel count mismatch")
+        out = np.zeros((n, gz, gy, gx, self.out_channels), np.float32)
+        check(load().am_unet_forward(self.handle, n, gz, gy, gx, x.ctypes.data_as(_fp), out.ctypes.data_as(_fp),
+                                     int(bool(sigmoid))), "am_unet_forward")
+        return out
+
+    def param_grad(self, x, dout):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        dout = np.ascontiguousarray(dout, dtype=np.float32)
+        n, gz, gy, gx, _ = x.shape
+        g = np.zeros(self.num_params, np.float32)
+        check(load().am_unet_param_grad(self.handle, n, gz, gy, gx, x.ctypes.data_as(_fp), dout.ctypes.data_as(_fp),
+                                        g.ctypes.data_as(_fp)), "am_unet_param_grad")
+        return g
+
+    def set_data(self, inputs, targets, mask):
+        x = np.ascontiguousarray(inputs, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        S, gz, gy, gx, c = x.shape
+        if c != self.in_channels or t.shape != (S, gz, gy, gx) or m.shape != t.shape:
+            raise ValueError("training tensors have inconsistent shapes")
+        check(load().am_unet_set_data(self.handle, S, gz, gy, gx, x.ctypes.data_as(_fp), t.ctypes.data_as(_fp),
+                                      m.ctypes.data_as(_u8p)), "am_unet_set_data")
+
+    def train(self, epochs=50, batch=4, lr=1e-3, seed=0, verbose=0):
+        c = TrainConfig(int(epochs), int(batch), float(lr), 0.9, 0.999, 1e-8, int(seed), int(verbose), 0)
+        losses = np.zeros(max(int(epochs), 1), np.float32)
+        check(load().am_unet_train(self.handle, ctypes.byref(c), losses.ctypes.data_as(_fp)), "am_unet_train")
+        return losses[:int(epochs)]
+
+    def eval(self) -> float:
+        v = ctypes.c_double(0.0)
+        check(load().am_unet_eval(self.handle, ctypes.byref(v)), "am_unet_eval")
         return v.value
 
 

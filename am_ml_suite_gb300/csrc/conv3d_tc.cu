@@ -53,6 +53,7 @@ struct TcFwdArgs {
     int dz, dy, dx;
     int tiles_x, tiles_y, tiles_z;
     int cin, relu;
+    int wrow0;  // first weight row (output channel) of this launch; the output pointer is offset to match
     int *err;
 };
 
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) conv_tc_fwd_kernel(const __gri
                     uint8_t *sa = smem + s * STAGE;
                     bulk::bar_expect(&full[s], A_BYTES + N * CW * 2);
                     tc::load_5d(sa, &mx, kc * CW, x0 + dx, y0 + dy, z0 + dz, nb, &full[s]);
-                    tc::load_3d(sa + A_BYTES, &mw, kc * CW, 0, tap, &full[s]);
+                    tc::load_3d(sa + A_BYTES, &mw, kc * CW, A.wrow0, tap, &full[s]);
                     issued = g + 1;
                 }
             }
@@ -480,10 +481,11 @@ __global__ void __launch_bounds__(kFwdThreads, 1) conv_tc_march_kernel(const __g
 // channel groups x 128 voxels x 8 channels (MN-major core matrices: 8 voxels x 8
 // channels, 128 bytes) -- and X^T of the tap-shifted box, cin/8 groups likewise.
 struct TcWgArgs {
-    float *dw;  // [27][cout][cin]
+    float *dw;  // [27][cout][cin_total]; this launch adds columns cin_off .. cin_off + CIN
     int dz, dy, dx;
     int tiles_x, tiles_y, tiles_z, ntiles;  // voxel boxes of the whole batch
     int cin, cout, boxes_per_cta;
+    int cin_total, cin_off;
     int *err;
 };
 
@@ -585,7 +587,7 @@ __global__ void __launch_bounds__(128) conv_tc_wgrad_kernel(const __grid_constan
         if (lane == 0) raise_err(A.err);
     } else if (nbox > 0) {
         const int co = mblk * 128 + warp * 32 + lane;
-        float *dst = A.dw + ((size_t)tap * A.cout + co) * CIN;
+        float *dst = A.dw + ((size_t)tap * A.cout + co) * A.cin_total + A.cin_off;
 #pragma unroll 1
         for (int c0 = 0; c0 < CIN; c0 += 16) {
             float v[16];
@@ -649,6 +651,20 @@ bool plane_map(CUtensorMap *m, const Grid5 &g, TensorView t, int channels) {
     const void *base = static_cast<const __nv_bfloat16 *>(t.p) + t.coff;
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// BF16 weights [27][rows][cols]: box of box_c columns x box_rows rows of one tap
+bool weight_map_rows(CUtensorMap *m, const __nv_bfloat16 *w, int rows, int box_rows, int cols, int box_c,
+                     CUtensorMapSwizzle sw) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, 27};
+    const cuuint64_t strides[2] = {(cuuint64_t)cols * 2, (cuuint64_t)cols * rows * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)box_c, (cuuint32_t)box_rows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(w), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -736,7 +752,8 @@ cudaError_t launch_fwd_n(int cout, const CUtensorMap &mx, const CUtensorMap &mw,
         case 64: return launch_fwd<64, CW>(mx, mw, a, ntiles, st);
         case 96: return launch_fwd<96, CW>(mx, mw, a, ntiles, st);
         case 128: return launch_fwd<128, CW>(mx, mw, a, ntiles, st);
-        default: return launch_fwd<192, CW>(mx, mw, a, ntiles, st);
+        case 192: return launch_fwd<192, CW>(mx, mw, a, ntiles, st);
+        default: return launch_fwd<256, CW>(mx, mw, a, ntiles, st);
     }
 }
 
@@ -771,11 +788,53 @@ bool tc_aligned(TensorView t) {
 
 }  // namespace
 
+namespace {
+
+bool fwd_n_ok(int n) { return n == 16 || n == 32 || n == 48 || n == 64 || n == 96 || n == 128 || n == 192 || n == 256; }
+
+// output channels row0 .. row0 + n of a convolution with cout_total weight rows
+cudaError_t fwd_generic(const Grid5 &g, TensorView x, int cin, const __nv_bfloat16 *w, int cout_total, int row0,
+                        int n, TensorView y, TensorView yf, int relu, cudaStream_t st) {
+    // channels per K step: 64 (128-byte swizzled rows) where cin allows, else 32 or 16
+    const int cw = cin % 64 == 0 ? 64 : cin % 32 == 0 ? 32 : 16;
+    const CUtensorMapSwizzle sw = cw == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                  : cw == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                             : CU_TENSOR_MAP_SWIZZLE_32B;
+    CUtensorMap mx, mw;
+    if (!act_map(&mx, g, x, cin, cw, sw) || !weight_map_rows(&mw, w, cout_total, n, cin, cw, sw))
+        return cudaErrorInvalidValue;
+    TcFwdArgs a{};
+    a.y = y.p ? static_cast<__nv_bfloat16 *>(y.p) : nullptr;
+    a.ycs = y.cstride;
+    a.yco = y.coff + row0;
+    a.yf = static_cast<float *>(yf.p);
+    a.yfcs = yf.cstride;
+    a.yfco = yf.coff + row0;
+    a.dz = g.dz;
+    a.dy = g.dy;
+    a.dx = g.dx;
+    a.tiles_x = (g.dx + kBoxX - 1) / kBoxX;
+    a.tiles_y = (g.dy + kBoxY - 1) / kBoxY;
+    a.tiles_z = (g.dz + kBoxZ - 1) / kBoxZ;
+    a.cin = cin;
+    a.relu = relu;
+    a.wrow0 = row0;
+    cudaError_t e = err_flag(&a.err);
+    if (e != cudaSuccess) return e;
+    const long long ntiles = (long long)a.tiles_x * a.tiles_y * a.tiles_z * g.n;
+    if (ntiles < 1 || ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+    if (cw == 64) return launch_fwd_n<64>(n, mx, mw, a, (int)ntiles, st);
+    if (cw == 32) return launch_fwd_n<32>(n, mx, mw, a, (int)ntiles, st);
+    return launch_fwd_n<16>(n, mx, mw, a, (int)ntiles, st);
+}
+
+}  // namespace
+
 cudaError_t conv3d_fwd_tc(const Grid5 &g, TensorView x, int cin, const __nv_bfloat16 *w, int cout, TensorView y,
                           TensorView yf, int relu, cudaStream_t st) {
-    if (cin % 16 || cin > 256 || !(cout == 16 || cout == 32 || cout == 48 || cout == 64 || cout == 96 ||
-                                   cout == 128 || cout == 192) ||
-        !tc_aligned(x) ||
+    // more than 256 output channels: two launches of half the channels each (an MMA's N is at most 256)
+    const bool split = cout > 256 && cout % 32 == 0 && fwd_n_ok(cout / 2);
+    if (cin % 16 || cin > 512 || (!fwd_n_ok(cout) && !split) || !tc_aligned(x) ||
         (reinterpret_cast<uintptr_t>(w) & 15) || (y.p && !tc_aligned(y)) ||
         (yf.p && (yf.cstride % 4 || yf.coff % 4 || (reinterpret_cast<uintptr_t>(yf.p) & 15))) ||
         x.coff + cin > x.cstride)
@@ -812,45 +871,25 @@ cudaError_t conv3d_fwd_tc(const Grid5 &g, TensorView x, int cin, const __nv_bflo
             default: break;
         }
     }
-    // channels per K step: 64 (128-byte swizzled rows) where cin allows, else 32 or 16
-    const int cw = cin % 64 == 0 ? 64 : cin % 32 == 0 ? 32 : 16;
-    const CUtensorMapSwizzle sw = cw == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
-                                  : cw == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
-                                             : CU_TENSOR_MAP_SWIZZLE_32B;
-    CUtensorMap mx, mw;
-    if (!act_map(&mx, g, x, cin, cw, sw) || !weight_map(&mw, w, cout, cin, cw, sw)) return cudaErrorInvalidValue;
-    TcFwdArgs a{};
-    a.y = static_cast<__nv_bfloat16 *>(y.p);
-    a.ycs = y.cstride;
-    a.yco = y.coff;
-    a.yf = static_cast<float *>(yf.p);
-    a.yfcs = yf.cstride;
-    a.yfco = yf.coff;
-    a.dz = g.dz;
-    a.dy = g.dy;
-    a.dx = g.dx;
-    a.tiles_x = (g.dx + kBoxX - 1) / kBoxX;
-    a.tiles_y = (g.dy + kBoxY - 1) / kBoxY;
-    a.tiles_z = (g.dz + kBoxZ - 1) / kBoxZ;
-    a.cin = cin;
-    a.relu = relu;
-    cudaError_t e = err_flag(&a.err);
-    if (e != cudaSuccess) return e;
-    const long long ntiles = (long long)a.tiles_x * a.tiles_y * a.tiles_z * g.n;
-    if (ntiles < 1 || ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-    if (cw == 64) return launch_fwd_n<64>(cout, mx, mw, a, (int)ntiles, st);
-    if (cw == 32) return launch_fwd_n<32>(cout, mx, mw, a, (int)ntiles, st);
-    return launch_fwd_n<16>(cout, mx, mw, a, (int)ntiles, st);
+    if (split) {
+        const cudaError_t e = fwd_generic(g, x, cin, w, cout, 0, cout / 2, y, yf, relu, st);
+        if (e != cudaSuccess) return e;
+        return fwd_generic(g, x, cin, w, cout, cout / 2, cout / 2, y, yf, relu, st);
+    }
+    return fwd_generic(g, x, cin, w, cout, 0, cout, y, yf, relu, st);
 }
 
-cudaError_t conv3d_wgrad_tc(const Grid5 &g, TensorView x, int cin, TensorView dy, int cout, float *dw,
-                            cudaStream_t st) {
-    if (!(cin == 16 || cin == 32 || cin == 48 || cin == 64 || cin == 96 || cin == 128 || cin == 192) ||
-        cout % 16 || cout > 256 || !tc_aligned(x) || !tc_aligned(dy) || x.coff + cin > x.cstride ||
-        dy.coff + cout > dy.cstride)
-        return cudaErrorInvalidValue;
+namespace {
+
+bool wg_cin_ok(int c) { return c == 16 || c == 32 || c == 48 || c == 64 || c == 96 || c == 128 || c == 192 || c == 256; }
+
+// weight-gradient columns cin_off .. cin_off + cin of a convolution with cin_total inputs
+cudaError_t wgrad_part(const Grid5 &g, TensorView x, int cin, int cin_total, int cin_off, TensorView dy, int cout,
+                       float *dw, cudaStream_t st) {
     CUtensorMap mdy, mx;
-    if (!act_map(&mdy, g, dy, cout) || !act_map(&mx, g, x, cin)) return cudaErrorInvalidValue;
+    TensorView xs = x;
+    xs.coff += cin_off;
+    if (!act_map(&mdy, g, dy, cout) || !act_map(&mx, g, xs, cin)) return cudaErrorInvalidValue;
     TcWgArgs a{};
     a.dw = dw;
     a.dz = g.dz;
@@ -862,6 +901,8 @@ cudaError_t conv3d_wgrad_tc(const Grid5 &g, TensorView x, int cin, TensorView dy
     a.ntiles = a.tiles_x * a.tiles_y * a.tiles_z * g.n;
     a.cin = cin;
     a.cout = cout;
+    a.cin_total = cin_total;
+    a.cin_off = cin_off;
     // enough CTAs for about four waves over 152 SMs, each reducing >= 4 boxes
     const long long per_tap = std::max<long long>(1, (152LL * 16) / (27LL * ((cout + 127) / 128)));
     a.boxes_per_cta = (int)std::max<long long>(4, (a.ntiles + per_tap - 1) / per_tap);
@@ -875,8 +916,26 @@ cudaError_t conv3d_wgrad_tc(const Grid5 &g, TensorView x, int cin, TensorView dy
         case 64: return launch_wg<64>(mdy, mx, a, grid, st);
         case 96: return launch_wg<96>(mdy, mx, a, grid, st);
         case 128: return launch_wg<128>(mdy, mx, a, grid, st);
-        default: return launch_wg<192>(mdy, mx, a, grid, st);
+        case 192: return launch_wg<192>(mdy, mx, a, grid, st);
+        default: return launch_wg<256>(mdy, mx, a, grid, st);
     }
+}
+
+}  // namespace
+
+cudaError_t conv3d_wgrad_tc(const Grid5 &g, TensorView x, int cin, TensorView dy, int cout, float *dw,
+                            cudaStream_t st) {
+    // more than 256 input channels: two launches of half the columns each (an MMA's N is at most 256)
+    const bool split = cin > 256 && wg_cin_ok(cin / 2) && cin % 32 == 0;
+    if ((!wg_cin_ok(cin) && !split) || cout % 16 || cout > 256 || !tc_aligned(x) || !tc_aligned(dy) ||
+        x.coff + cin > x.cstride || dy.coff + cout > dy.cstride)
+        return cudaErrorInvalidValue;
+    if (split) {
+        const cudaError_t e = wgrad_part(g, x, cin / 2, cin, 0, dy, cout, dw, st);
+        if (e != cudaSuccess) return e;
+        return wgrad_part(g, x, cin / 2, cin, cin / 2, dy, cout, dw, st);
+    }
+    return wgrad_part(g, x, cin, cin, 0, dy, cout, dw, st);
 }
 
 cudaError_t conv3d_tc_error(int *flag, bool clear, cudaStream_t st) {

@@ -111,8 +111,9 @@ def batch_config(nat, pr, max_iterations=50):
                               cg_tol=1e-6, cg_max_iterations=200000)
 
 
-def run_batch(args, nat, world, rank):
-    """Batched workload: one step = one SIMP iteration of every problem."""
+def run_batch(args, nat, world, rank, emit=True):
+    """Batched workload: one step = one SIMP iteration of every problem.  Prints
+    the JSON line when `emit`; returns it."""
     import torch
 
     probs = build_batch256()
@@ -235,7 +236,10 @@ def run_batch(args, nat, world, rank):
                          "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": alg, "avg_ms": plan["ms"]},
             "gpu_launches": int(l1 - l0), "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,
         }
-        print(json.dumps(line))
+        if emit:
+            print(json.dumps(line))
+        return line
+    return None
 
 
 class ClockSampler:
@@ -534,6 +538,9 @@ def main():
                          "CPU, so the two lines compare like for like; the other arms are in `arms`)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="skip the short runs of the bracket (config 2) and the 256-problem batch (config 3) "
+                         "reported in `other_workloads`")
     ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd",
                                         "filter", "oc", "vcycle", "vcycle_defl"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
@@ -763,6 +770,34 @@ def main():
     if not args.no_cpu_baseline and rank == 0 and "jacobi" in results:
         cpu = cpu_baseline(W, results["jacobi"]["pcg_iterations_per_solve"])
 
+    # ---- the other benchmark configurations, short runs on this GPU ----------
+    other = None
+    if rank == 0 and world == 1 and not args.no_other_workloads and args.workload == "cantilever256":
+        other = {}
+        Wb = build_workload("bracket192")
+        time_arm(nat, torch, Wb, "jacobi", 2)
+        rb, pb = time_arm(nat, torch, Wb, "jacobi", min(args.steps, 8), keep=True)
+        lb = pb.layout_info()
+        kb_ms, _ = pb.bench_kernel(0, reps=10, flush_l2=True)
+        pb.close()
+        bb = 53 * lb["nodes"] + 4 * lb["elements"]
+        other["bracket192"] = {
+            "config": "192x96x96 bracket (config 2), Jacobi PCG with FP64 residual replacement, rel-res 1e-6, "
+                      "SIMP steps 1..K of a fresh problem",
+            "value": rb["value"], "unit": "SIMP iters/s", "steps": min(args.steps, 8),
+            "pcg_solve_ms": rb["pcg_solve_ms"], "pcg_iterations_per_solve": rb["pcg_iterations_per_solve"],
+            "solver_residual_max": rb["solver_residual_max"],
+            "roofline_ku": {"achieved": bb / (kb_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                            "frac": bb / (kb_ms * 1e-3) / 1e9 / peak, "avg_ms": kb_ms, "algorithmic_bytes": bb}}
+        import types
+
+        lbatch = run_batch(types.SimpleNamespace(steps=3, warmup=2, no_e2e=True, no_cpu_baseline=True), nat, 1, 0,
+                           emit=False)
+        other["batch256"] = {k: lbatch[k] for k in ("metric", "value", "unit", "ms_per_step",
+                                                   "pcg_iterations_per_problem_step", "roofline")}
+        other["batch256"]["steps"] = 3
+        other["batch256"]["autotuned_plan"] = lbatch["config"]["autotuned_plan"]
+
     if rank == 0:
         ref = results.get("jacobi")
         line = {
@@ -786,6 +821,7 @@ def main():
             "clocks": clk.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "other_workloads": other,
         }
         print(json.dumps(line))
     if world > 1:

@@ -369,6 +369,40 @@ am_status am_precond_eval(am_precond *m, long long first, long long count, int l
  * FP64 residual accepts every solve, as with Jacobi. */
 am_status am_problem_set_preconditioner(am_problem *p, am_precond *m);
 
+/* ---- density-predicting U-Net (the reference's am.ai TopOptUNet) -----------------------
+ * A 3-D U-Net predicting the optimised density field from a problem encoding: the
+ * network the reference declares in src/am/ai/model.py:18-67 (in_channels 4,
+ * out_channels 1, features (32, 64, 128, 256)) and leaves unimplemented.  Four levels
+ * of width f0, 2 f0, 4 f0, 8 f0 (two 3x3x3 convolutions + ReLU each), mean pooling
+ * down, nearest upsampling up, concatenated skips, a 3x3x3 output convolution and a
+ * sigmoid; BF16 weights and activations, FP32 accumulate, on the tensor cores.
+ * Tensors are channels-last [n][gz][gy][gx][c] on grids whose dimensions are
+ * multiples of 8. */
+typedef struct am_unet am_unet;
+
+/* 1 <= in_channels, out_channels <= 16; f0 = 16 or 32. */
+am_status am_unet_create(int in_channels, int out_channels, int f0, uint64_t seed, am_unet **out);
+am_status am_unet_destroy(am_unet *u);
+long long am_unet_num_params(am_unet *u);
+/* FP32 master weights, layer by layer, each [27 taps][cout][cin] (channels padded to 16). */
+am_status am_unet_get_params(am_unet *u, float *w);
+am_status am_unet_set_params(am_unet *u, const float *w);
+/* in [n][gz][gy][gx][in_channels] -> out [n][gz][gy][gx][out_channels] (sigmoid != 0:
+ * the sigmoid of the output, else the raw output). */
+am_status am_unet_forward(am_unet *u, int n, int gz, int gy, int gx, const float *in, float *out, int sigmoid);
+/* Weight gradient of sum(raw output * dout) (for gradient checks). */
+am_status am_unet_param_grad(am_unet *u, int n, int gz, int gy, int gx, const float *in, const float *dout,
+                             float *grad);
+/* Training set on the device: inputs [S][gz][gy][gx][in_channels], target densities
+ * [S][gz][gy][gx], mask [S][gz][gy][gx] (nonzero: the cell counts in the loss). */
+am_status am_unet_set_data(am_unet *u, int n_samples, int gz, int gy, int gx, const float *inputs,
+                           const float *targets, const uint8_t *mask);
+/* Adam on the mean squared error of the sigmoid output against the targets over the
+ * masked cells; epoch_loss (nullable) receives each epoch's mean.  cfg->loss unused. */
+am_status am_unet_train(am_unet *u, const am_train_config *cfg, float *epoch_loss);
+/* Mean squared error over the whole training set. */
+am_status am_unet_eval(am_unet *u, double *mse);
+
 /* ---- batched SIMP ---------------------------------------------------------------
  * Many independent C++-variant problems of uneven sizes run together: one launch
  * of each kernel family per step for the whole batch (persistent CTAs over a
