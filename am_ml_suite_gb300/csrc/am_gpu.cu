@@ -112,6 +112,9 @@ struct am_problem {
     KuLaunch plan32, plan64;
     KuLaunch plan3;           // TMA-staged FP32 PCG K*u (ku3)
     int ku3_stages = 4;
+    // the solver's K*u: 1 = ku3b_kernel (no CTA barrier per plane, 5 stages),
+    // 0 = ku3_kernel (tensor-store output tiles, ku3_stages stages)
+    int ku3_variant = 1;
     Ku3Maps *maps3 = nullptr;  // tensor maps of the FP32 PCG vectors (built on first use)
     bool pad_dirty = true;     // scales or constraint bits changed since the padded copies were made
     int nblocks_vec = 0;
@@ -304,6 +307,9 @@ am_status ku3_ready(am_problem *P) {
 
 // one FP32 PCG K*u step: p = D^-1 r + beta p_prev, q = mask(K p), p.q -> alpha
 cudaError_t pcg_ku32(am_problem *P) {
+    if (P->ku3_variant == 1)
+        return ku3b_pcg(P->maps3, P->plan3, P->L, P->M32, P->q32v.p, P->p32a.p, P->p32b.p, P->partial.p, P->S, 5,
+                        P->st);
     return ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, P->ku3_stages, P->st);
 }
 
@@ -1034,7 +1040,7 @@ am_status am_ku_pcg_step(am_problem *P, const am_simp_config *cfg, const double 
     CKS(check_problem(P));
     CKS(check_cfg(P, cfg));
     if (!rho || !r || !p_prev) return fail(AM_ERR_INVALID_ARG, "null array");
-    if (impl != 2 && impl != 3) return fail(AM_ERR_INVALID_ARG, "impl must be 2 or 3");
+    if (impl < 2 || impl > 4) return fail(AM_ERR_INVALID_ARG, "impl must be 2, 3 or 4");
     if (!std::isfinite(beta)) return fail(AM_ERR_INVALID_ARG, "beta must be finite");
     if (load_case < 0 || load_case >= (int)P->cases.size()) return fail(AM_ERR_INVALID_ARG, "load case not set");
     if (impl == 2 && P->plan32.warps != 8) return fail(AM_ERR_INVALID_ARG, "grid too large for the impl-2 kernel");
@@ -1060,6 +1066,8 @@ am_status am_ku_pcg_step(am_problem *P, const am_simp_config *cfg, const double 
     CK(cudaMemcpyAsync(P->S, &run, sizeof(Scalars), cudaMemcpyHostToDevice, P->st));
     if (impl == 3)
         CK(pcg_ku32(P));
+    else if (impl == 4)
+        CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 4, P->st));
     else
         CK(ku2_pcg(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p, P->mask.p,
                    P->q32v.p, P->partial.p, P->S, P->st));
@@ -1431,6 +1439,13 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
                 break;
             case 5:
                 CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 3, P->st));
+                break;
+            case 12:
+                CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 4, P->st));
+                break;
+            case 13:
+                CK(ku3b_pcg(P->maps3, P->plan3, P->L, P->M32, P->q32v.p, P->p32a.p, P->p32b.p, P->partial.p, P->S,
+                            4, P->st));
                 break;
             case 8:  // the SIMP loop's FP64 shared-memory stencil
                 CK(filter_cpp<double>(P->L, taps_of(P), P->dc.p, P->rho.p, P->dcf.p, P->st));

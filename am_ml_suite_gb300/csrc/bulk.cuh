@@ -29,6 +29,11 @@ __device__ __forceinline__ void copy_g2s(void *dst, const void *src, unsigned by
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
 }
+// one plain arrival (release: this thread's earlier shared-memory accesses are
+// ordered before the phase completes)
+__device__ __forceinline__ void bar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // orders this thread's earlier shared-memory accesses before later copies into them
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

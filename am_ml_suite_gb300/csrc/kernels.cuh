@@ -55,6 +55,11 @@ KuLaunch ku3_plan(const Layout &L, int sms = 152);
 // `stages` (3 or 4) shared-memory stages
 cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,
                     Scalars *S, int stages, cudaStream_t st);
+// The same step without a CTA barrier per plane (ku3b_kernel): p and q bitwise
+// those of ku3_pcg; q and the new p are written to the raw vectors q and pa / pb
+// (the map pair's parity as in ku3_pcg).  stages 4 or 5.
+cudaError_t ku3b_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, float *q, float *pa,
+                     float *pb, double *partial, Scalars *S, int stages, cudaStream_t st);
 // the previous register-direct kernel (ku2_kernel) for the same PCG step (measurement)
 cudaError_t ku2_pcg(const KuLaunch &K, const Layout &L, const Modal<float> &M, const float *s, float *pa, float *pb,
                     const float *r, const float *dinv, const uint8_t *mask, float *q, double *partial, Scalars *S,

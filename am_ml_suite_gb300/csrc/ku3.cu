@@ -129,9 +129,16 @@ KuLaunch ku3_plan(const Layout &L, int sms) {
 cudaError_t ku3_init_attributes() {
     cudaError_t e = cudaFuncSetAttribute(ku3_kernel<8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Ku3Shape<8, 3>::SMEM_ALLOC);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(ku3_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                Ku3Shape<8, 4>::SMEM_ALLOC);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ku3_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Ku3Shape<8, 4>::SMEM_ALLOC);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ku3b_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Ku3bShape<8, 4>::SMEM_ALLOC);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ku3b_kernel<8, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Ku3bShape<8, 5>::SMEM_ALLOC);
+    return e;
 }
 
 cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,
@@ -149,6 +156,38 @@ cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const 
         ku3_kernel<8, 4><<<K.ntiles(), 256, Ku3Shape<8, 4>::SMEM_ALLOC, st>>>(*T, a);
     else if (stages == 3)
         ku3_kernel<8, 3><<<K.ntiles(), 256, Ku3Shape<8, 3>::SMEM_ALLOC, st>>>(*T, a);
+    else
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+cudaError_t ku3b_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, float *q, float *pa,
+                     float *pb, double *partial, Scalars *S, int stages, cudaStream_t st) {
+    if (!T || K.warps != 8 || K.tx != Ku3Shape<8, 4>::TX || K.ty != Ku3Shape<8, 4>::TY) return cudaErrorInvalidValue;
+    // the kernel forms node offsets in 32-bit arithmetic
+    if (3 * L.cs >= (1LL << 31) || L.sxy >= (1LL << 31)) return cudaErrorInvalidValue;
+    Ku3bArgs a{};
+    a.M = M;
+    a.partial = partial;
+    a.S = S;
+    a.q = q;
+    a.pa = pa;
+    a.pb = pb;
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tz = K.tz;
+    a.nx = L.nx;
+    a.ny = L.ny;
+    a.nz = L.nz;
+    a.sx = L.sx;
+    a.sxy = (int)L.sxy;
+    a.cs = (int)L.cs;
+    if (stages == 5)
+        ku3b_kernel<8, 5><<<K.ntiles(), 256, Ku3bShape<8, 5>::SMEM_ALLOC, st>>>(*T, a);
+    else if (stages == 4)
+        ku3b_kernel<8, 4><<<K.ntiles(), 256, Ku3bShape<8, 4>::SMEM_ALLOC, st>>>(*T, a);
     else
         return cudaErrorInvalidValue;
     cudaError_t e = cudaGetLastError();

@@ -357,4 +357,299 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
     }
 }
 
+// ---- the same product without a CTA-wide barrier per plane -----------------------
+// ku3b_kernel computes exactly what ku3_kernel computes (same staging, same
+// arithmetic, same order of every sum: p and q bitwise equal, p.q equal), but
+// the warps of a CTA are no longer held in lockstep:
+//   * stage reuse: each stage has a "full" barrier (the tensor copies' bytes) and
+//     an "empty" one that every warp arrives on once it has read the plane;
+//     thread 0 refills the stage of plane j-1 while its warp works on plane j,
+//     so a warp may run one plane ahead of the slowest before it waits, and
+//     S-1 planes are in flight;
+//   * the one node row shared by warps w-1 and w goes through a two-slot
+//     mailbox per warp pair with its own full/empty barriers, so a warp waits
+//     only for its lower neighbour's row, never for the whole CTA;
+//   * q and p of the owned nodes leave as coalesced per-lane global stores (rows
+//     of 28 consecutive floats) instead of shared tiles and tensor stores, so no
+//     warp waits for a tile to drain and no proxy fence is issued per plane.
+// Every wait is bounded (one second) and warp-uniform (a wait counts as
+// successful only if it succeeded in every lane); a warp whose wait runs out
+// raises the CTA's failure flag and leaves the plane loop, the others leave at
+// their next plane or when their own wait runs out, thread 0 waits (bounded)
+// for its copies in flight, and the launch reports Scalars::kerr.
+struct Ku3bArgs {
+    Modal<float> M;
+    double *partial;  // per-tile p.q
+    Scalars *S;
+    float *q, *pa, *pb;  // outputs: q = mask(K p); p into pa (odd iterations) or pb (even)
+    int tiles_x, tiles_y, tz, nx, ny, nz;
+    int sx, sxy, cs;  // node row, plane and component strides (the host checks 3 cs < 2^31)
+};
+
+template <int W, int S>
+struct Ku3bShape {
+    using B = Ku3Shape<W, S>;
+    static constexpr int STAGE = B::STAGE;
+    static constexpr int OFF_XCH = S * STAGE;
+    // mailbox [W][2][3][32]: slot w (w >= 1) carries warp w-1's row 2 to warp w
+    static constexpr int XCH_B = W * 2 * 3 * 32 * 4;
+    static constexpr int OFF_RED = OFF_XCH + XCH_B;
+    static constexpr int OFF_BAR = OFF_RED + B::r128(2 * W * 8);
+    // full[S], empty[S], xfull[W][2], xempty[W][2]
+    static constexpr int NBAR = 2 * S + 4 * W;
+    static constexpr int OFF_FLAG = OFF_BAR + 8 * NBAR;
+    static constexpr int SMEM = OFF_FLAG + 8;
+    static constexpr int SMEM_ALLOC = SMEM + 1024;
+};
+
+// true if the wait succeeded in every lane of the (fully active) warp
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, unsigned parity) {
+    return __all_sync(0xffffffffu, bulk::bar_wait(bar, parity)) != 0;
+}
+
+template <int W, int S>
+__global__ void __launch_bounds__(32 * W, 2) ku3b_kernel(const __grid_constant__ Ku3Maps T, const Ku3bArgs A) {
+    using namespace k2;
+    using Sh0 = Ku3Shape<W, S>;
+    using Sh = Ku3bShape<W, S>;
+    constexpr int TX = Sh0::TX, BX = Sh0::BX, BY = Sh0::BY, BXM = Sh0::BXM;
+    extern __shared__ __align__(1024) unsigned char ku3_smem[];
+    unsigned char *smem = ku3_smem + ((1024u - (bulk::smem_addr(ku3_smem) & 1023u)) & 1023u);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + Sh::OFF_BAR);
+    uint64_t *empty = full + S;
+    uint64_t *xfull = empty + S;     // [W][2]
+    uint64_t *xempty = xfull + 2 * W;  // [W][2]
+    float(*xch)[2][3][32] = reinterpret_cast<float(*)[2][3][32]>(smem + Sh::OFF_XCH);
+    double *red = reinterpret_cast<double *>(smem + Sh::OFF_RED);
+    volatile int &s_fail = reinterpret_cast<int *>(smem + Sh::OFF_FLAG)[0];
+    int &last_flag = reinterpret_cast<int *>(smem + Sh::OFF_FLAG)[1];
+
+    if (A.S->done) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int b = blockIdx.x;
+    const int tx_ = b % A.tiles_x;
+    b /= A.tiles_x;
+    const int ty_ = b % A.tiles_y;
+    const int tz_ = b / A.tiles_y;
+    const int x0 = tx_ * TX, y0 = ty_ * Sh0::TY, z0 = tz_ * A.tz;
+    const int z1 = min(z0 + A.tz, A.nz + 1);
+    const int np = z1 - z0 + 2;  // planes z0-1 .. z1 pass through the stages
+    const bool odd = (A.S->it & 1) != 0;
+    const float beta = (float)A.S->beta;
+    const bool use_p = beta != 0.f;
+    const CUtensorMap *map_pin = odd ? &T.pb : &T.pa;
+    float *const pout = odd ? A.pa : A.pb;
+    const int xm0 = (x0 - 1) & ~15;
+    const int col = lane + 3;
+    const int mcol = x0 - 1 - xm0 + lane;
+    const bool own_lane = lane >= 1 && lane <= TX;
+    const unsigned tx_bytes = (unsigned)(Sh0::VEC_B * (use_p ? 2 : 1) + Sh0::DIN_B + Sh0::MSK_B + Sh0::SCL_B);
+    // stores: this lane's node column, rows y0+2w-1 (q), y0+2w (q, p), y0+2w+1 (p)
+    const int gx = x0 - 1 + lane;
+    const bool colok = own_lane && gx <= A.nx;
+    const int ya = y0 + 2 * w - 1;
+    const bool okq0 = colok && w >= 1 && ya <= A.ny;
+    const bool okq1 = colok && ya + 1 <= A.ny;
+    const bool okp2 = colok && w < W - 1 && ya + 2 <= A.ny;
+    const int oq0 = ya * A.sx + gx, oq1 = oq0 + A.sx, op2 = oq1 + A.sx;
+    const float f0 = (own_lane && w >= 1) ? 1.f : 0.f;
+    const float f1 = own_lane ? 1.f : 0.f;
+
+    auto issue = [&](int j, int st) {
+        const int iz = z0 - 1 + j;
+        unsigned char *sb = smem + st * Sh::STAGE;
+        bulk::bar_expect(&full[st], tx_bytes);
+        tma::load4(sb + Sh0::OFF_R, &T.r, x0 - 4, y0 - 1, iz, 0, &full[st]);
+        if (use_p) tma::load4(sb + Sh0::OFF_P, map_pin, x0 - 4, y0 - 1, iz, 0, &full[st]);
+        tma::load3(sb + Sh0::OFF_D, &T.d, x0 - 4, y0 - 1, iz, &full[st]);
+        tma::load3(sb + Sh0::OFF_M, &T.m, xm0, y0 - 1, iz, &full[st]);
+        tma::load3(sb + Sh0::OFF_S, &T.s, x0 - 4, y0 - 1, iz - 1, &full[st]);
+    };
+    auto read_plane = [&](int st, float (&v)[3][3], unsigned &mbits, float &sA, float &sB) {
+        const unsigned char *sb = smem + st * Sh::STAGE;
+        const float *Rs = reinterpret_cast<const float *>(sb + Sh0::OFF_R);
+        const float *Ps = reinterpret_cast<const float *>(sb + Sh0::OFF_P);
+        const float *Ds = reinterpret_cast<const float *>(sb + Sh0::OFF_D);
+        const float *Ss = reinterpret_cast<const float *>(sb + Sh0::OFF_S);
+        const uint8_t *Ms = sb + Sh0::OFF_M;
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) {
+            const int o = (2 * w + rr) * BX + col;
+            const float d = Ds[o];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float rv = Rs[c * BY * BX + o];
+                const float pv = use_p ? Ps[c * BY * BX + o] : 0.f;
+                v[rr][c] = fmaf(beta, pv, d * rv);
+            }
+        }
+        mbits = (unsigned)Ms[(2 * w) * BXM + mcol] | ((unsigned)Ms[(2 * w + 1) * BXM + mcol] << 8);
+        sA = Ss[(2 * w) * BX + col];
+        sB = Ss[(2 * w + 1) * BX + col];
+    };
+    auto faces = [&](const float (&v)[3][3], Face (&F)[3]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float n0 = __shfl_down_sync(0xffffffffu, v[0][c], 1);
+            const float n1 = __shfl_down_sync(0xffffffffu, v[1][c], 1);
+            const float n2 = __shfl_down_sync(0xffffffffu, v[2][c], 1);
+            F[c] = face_modes(v[0][c], v[1][c], v[2][c], n0, n1, n2);
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S; ++k) {
+            bulk::bar_init(&full[k], 1);
+            bulk::bar_init(&empty[k], W);
+        }
+        for (int k = 0; k < 2 * W; ++k) {
+            bulk::bar_init(&xfull[k], 1);
+            bulk::bar_init(&xempty[k], 1);
+        }
+        bulk::bar_init_fence();
+        s_fail = 0;
+    }
+    __syncthreads();
+    int issued = 0;  // planes whose copies thread 0 has issued
+    if (threadIdx.x == 0)
+        for (; issued < S && issued < np; ++issued) issue(issued, issued);
+
+    const float2 lam = splat(A.M.lam), mu = splat(A.M.mu), twomu = splat(2.f * A.M.mu), thrmu = splat(3.f * A.M.mu);
+    Face FB[3], CT[3];
+    float pcur[2][3];
+    unsigned mcur;
+    Acc<float> dot;
+    int j = 0;  // the plane being consumed (planes < j are read)
+    bool ok = warp_wait(&full[0], 0u);
+    if (ok) {
+        j = 1;
+        float v[3][3], sA, sB;
+        read_plane(0, v, mcur, sA, sB);
+        __syncwarp();
+        if (lane == 0) bulk::bar_arrive(&empty[0]);
+        faces(v, FB);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            CT[c].ss = CT[c].sd = CT[c].ds = CT[c].dd = make_float2(0.f, 0.f);
+            pcur[0][c] = v[0][c];
+            pcur[1][c] = v[1][c];
+        }
+    }
+    // stage and phase of plane j
+    int st = 1 % S, ph = S == 1 ? 1 : 0;
+    if (ok) {
+#pragma unroll 2
+        for (; j < np; ++j) {
+            if (s_fail || !warp_wait(&full[st], (unsigned)ph)) {
+                ok = false;
+                break;
+            }
+            float v[3][3], sA, sB;
+            unsigned mnew;
+            read_plane(st, v, mnew, sA, sB);
+            __syncwarp();
+            if (lane == 0) bulk::bar_arrive(&empty[st]);
+            // refill the stage of plane j-1 (= issued - S) once every warp has read it
+            if (threadIdx.x == 0 && issued < np) {
+                const int k = issued - S;
+                if (bulk::bar_wait(&empty[k % S], (unsigned)(k / S) & 1u)) {
+                    bulk::proxy_fence();
+                    issue(issued, k % S);
+                    ++issued;
+                } else {
+                    s_fail = 1;
+                }
+            }
+            Face FT[3];
+            faces(v, FT);
+            float V[3][3];
+            layer_math(FB, FT, CT, make_float2(sA, sB), A.M, lam, mu, twomu, thrmu, V);
+            // mailbox slot o, used for the u-th time: hand row 2 up, take the row below
+            const int o = j & 1;
+            const unsigned u = (unsigned)(j - 1) >> 1;
+            if (w < W - 1) {
+                if (u >= 1 && !warp_wait(&xempty[2 * (w + 1) + o], (u - 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) xch[w + 1][o][c][lane] = V[2][c];
+                __syncwarp();
+                if (lane == 0) bulk::bar_arrive(&xfull[2 * (w + 1) + o]);
+            }
+            float below[3] = {0.f, 0.f, 0.f};
+            if (w > 0) {
+                if (!warp_wait(&xfull[2 * w + o], u & 1u)) {
+                    ok = false;
+                    break;
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) below[c] = xch[w][o][c][lane];
+                __syncwarp();
+                if (lane == 0) bulk::bar_arrive(&xempty[2 * w + o]);
+            }
+            // q of plane z0-2+j (rows ya, ya+1), p of plane z0-1+j (rows ya+1, ya+2)
+            const bool qplane = j >= 2, pplane = j <= z1 - z0;
+            const int zq = (z0 - 2 + j) * A.sxy, zp = zq + A.sxy;
+            float ds0 = 0.f, ds1 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float v0 = V[0][c] + below[c];
+                const float q0 = ((mcur >> c) & 1u) ? 0.f : v0;
+                const float q1 = ((mcur >> (8 + c)) & 1u) ? 0.f : V[1][c];
+                float *qc = A.q + c * A.cs;
+                float *pc = pout + c * A.cs;
+                if (qplane && okq0) qc[zq + oq0] = q0;
+                if (qplane && okq1) qc[zq + oq1] = q1;
+                if (pplane && okq1) pc[zp + oq1] = v[1][c];
+                if (pplane && okp2) pc[zp + op2] = v[2][c];
+                ds0 = fmaf(pcur[0][c], q0, ds0);
+                ds1 = fmaf(pcur[1][c], q1, ds1);
+            }
+            if (qplane) dot.add(fmaf(f0, ds0, f1 * ds1));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                FB[c] = FT[c];
+                pcur[0][c] = v[0][c];
+                pcur[1][c] = v[1][c];
+            }
+            mcur = mnew;
+            if (++st == S) {
+                st = 0;
+                ph ^= 1;
+            }
+        }
+    }
+    if (!ok) s_fail = 1;
+    __syncthreads();
+    if (s_fail) {
+        // a wait ran out: wait (bounded) for this CTA's copies still in flight
+        // (every plane issued and not yet consumed), then flag the launch
+        if (threadIdx.x == 0) {
+            for (int k = j; k < issued; ++k) bulk::bar_wait(&full[k % S], (unsigned)(k / S) & 1u);
+            atomicExch(&A.S->kerr, 1);
+        }
+    }
+
+    double dv[1] = {dot.value()};
+    block_sum<1>(dv, red);
+    if (threadIdx.x == 0) A.partial[2 * blockIdx.x] = dv[0];
+    if (!arrive_last_n(&A.S->cnt_ku, &last_flag, gridDim.x)) return;
+    double tot[1];
+    reduce_partials<1>(A.partial, gridDim.x, 2, tot, red);
+    if (threadIdx.x == 0) {
+        Scalars *Sc = A.S;
+        const double pq = tot[0];
+        Sc->pq = pq;
+        if (!(pq > 0.0) || !isfinite(pq)) {
+            Sc->status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+            Sc->done = 1;
+            Sc->alpha = 0.0;
+        } else {
+            Sc->alpha = Sc->rz / pq;
+        }
+        Sc->cnt_ku = 0;
+    }
+}
+
 }  // namespace amk

@@ -541,7 +541,8 @@ def main():
     ap.add_argument("--no-other-workloads", action="store_true",
                     help="skip the short runs of the bracket (config 2) and the 256-problem batch (config 3) "
                          "reported in `other_workloads`")
-    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "update_even", "update_odd",
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "ku3tile", "ku3b4",
+                                        "update_even", "update_odd",
                                         "filter", "oc", "vcycle", "vcycle_defl"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
     ap.add_argument("--reps", type=int, default=3)
@@ -678,7 +679,7 @@ def main():
         p.set_loads([W["F"]], [W["fixed"]])
         p.simp_begin(simp_config(nat, W), W["rho0"])
         which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7,
-                 "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11}[args.probe]
+                 "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11, "ku3tile": 12, "ku3b4": 13}[args.probe]
         if which in (8, 9):
             p.simp_step()  # the filter and OC probes time the state a SIMP step leaves
         avg, mn = p.bench_kernel(which, reps=args.reps, flush_l2=True)
@@ -730,7 +731,7 @@ def main():
     # ku3: reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B),
     # scale (4 B per element); writes p, q (3 x 4 B each per node)
     alg_bytes = 53 * nodes + 4 * nel
-    ku_roof = {"bound": "hbm", "kernel": "ku3_kernel<8,4> (tensor-copy staged p-update + FP32 K*p + p.q)",
+    ku_roof = {"bound": "hbm", "kernel": "ku3b_kernel<8,5> (tensor-copy staged p-update + FP32 K*p + p.q, no CTA barrier per plane)",
                "achieved": alg_bytes / (ku_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                "frac": alg_bytes / (ku_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
                "traffic": ku_traffic_per_launch(W, nodes, nel), "algorithmic_bytes": alg_bytes,

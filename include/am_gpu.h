@@ -202,8 +202,10 @@ am_status am_ku_apply(am_problem *p, const am_simp_config *cfg, const double *rh
  * with the operator of rho, its Jacobi diagonal D and the constraint bits of load
  * case `load_case` (fixed and orphan DOFs), p = D^-1 r + beta p_prev and
  * q = mask(K p) in FP32, and *pq = p.q.  Vectors in the reference DOF order, FP64
- * in and out.  impl 3: the tensor-copy staged kernel the solver uses; impl 2: the
- * register-direct kernel it replaced (same arithmetic). */
+ * in and out.  impl 3: the kernel the solver uses (tensor-copy staged, no CTA-wide
+ * barrier per plane); impl 4: the staged kernel with a CTA barrier per plane and
+ * tensor-store output tiles; impl 2: the register-direct kernel (all three the
+ * same arithmetic, bitwise equal results). */
 am_status am_ku_pcg_step(am_problem *p, const am_simp_config *cfg, const double *rho, int load_case,
                          const double *r, const double *p_prev, double beta, int impl, double *p_out,
                          double *q_out, double *pq);
@@ -278,7 +280,9 @@ long long am_launch_count(void);
 /* Times `reps` single launches of one kernel on the problem's stream with CUDA
  * events, after am_simp_begin (on the state the last am_simp_step left, or, before
  * the first step, on the initial density with zero vectors): which = 0 the
- * fused FP32 PCG K*u (the tensor-copy staged kernel with 4 stages), 1 the FP64
+ * fused FP32 PCG K*u the solver runs (tensor-copy staged, 5 stages, no CTA-wide
+ * barrier per plane), 12 / 13 the staged kernel with a CTA barrier per plane (4
+ * stages) / the barrier-free one with 4 stages, 1 the FP64
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
  * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
