@@ -112,9 +112,9 @@ struct am_problem {
     KuLaunch plan32, plan64;
     KuLaunch plan3;           // TMA-staged FP32 PCG K*u (ku3)
     int ku3_stages = 4;
-    // the solver's K*u: 1 = ku3b_kernel (no CTA barrier per plane, 5 stages),
-    // 0 = ku3_kernel (tensor-store output tiles, ku3_stages stages)
-    int ku3_variant = 1;
+    // the solver's K*u: 0 = ku3_kernel (tensor-store output tiles, ku3_stages
+    // stages; the faster on GB300), 1 = ku3b_kernel (no CTA barrier per plane)
+    int ku3_variant = 0;
     Ku3Maps *maps3 = nullptr;  // tensor maps of the FP32 PCG vectors (built on first use)
     bool pad_dirty = true;     // scales or constraint bits changed since the padded copies were made
     int nblocks_vec = 0;
@@ -1067,7 +1067,8 @@ am_status am_ku_pcg_step(am_problem *P, const am_simp_config *cfg, const double 
     if (impl == 3)
         CK(pcg_ku32(P));
     else if (impl == 4)
-        CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 4, P->st));
+        CK(ku3b_pcg(P->maps3, P->plan3, P->L, P->M32, P->q32v.p, P->p32a.p, P->p32b.p, P->partial.p, P->S, 5,
+                    P->st));
     else
         CK(ku2_pcg(P->plan32, P->L, P->M32, P->s32.p, P->p32a.p, P->p32b.p, P->r32.p, P->dinv32.p, P->mask.p,
                    P->q32v.p, P->partial.p, P->S, P->st));

@@ -7,9 +7,10 @@
 // 2x2x2 mean pooling down, nearest upsampling up, skip connections by
 // concatenation, a 3x3x3 output convolution and a sigmoid: the predicted density.
 // Tensors are channels-last BF16 on the element grid padded to multiples of 8;
-// input and output channel counts are padded to 16.  Training minimises the mean
-// squared error of the sigmoid output against target densities over the cells
-// inside each sample's domain, with Adam on FP32 master weights.
+// input and output channel counts are padded to 16.  Training minimises the binary
+// cross-entropy of the sigmoid output against target densities over the cells
+// inside each sample's domain, with Adam on FP32 master weights, and reports the
+// mean squared error.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -97,9 +98,12 @@ __global__ void gout_kernel(long long V, const float *__restrict__ dout, int cou
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
         for (int k = 0; k < 16; ++k) g[v * 16 + k] = __float2bfloat16(k < cout ? dout[v * cout + k] : 0.f);
 }
-// masked squared error of sigmoid(out[:, 0]) against t; d loss / d out (channel 0)
-// scaled by `scale` into g (BF16, other channels zero); sum of squares and count
-// into acc[0..1]
+// masked squared error of y = sigmoid(out[:, 0]) against t into acc[0..1] (sum of
+// squares, count); into g (BF16, other channels zero) the gradient of the binary
+// cross-entropy -t log y - (1-t) log(1-y) with respect to the logit, y - t, scaled
+// by `scale` -- unlike the squared error's (y - t) y (1 - y) it does not vanish
+// where the sigmoid saturates, so a network pushed to all-void or all-solid
+// outputs early in training still recovers
 __global__ void mse_kernel(long long V, const float *__restrict__ out16, const float *__restrict__ t,
                            const uint8_t *__restrict__ m, double scale, bf16 *__restrict__ g, double *acc) {
     __shared__ double red[2 * 8];
@@ -112,7 +116,7 @@ __global__ void mse_kernel(long long V, const float *__restrict__ out16, const f
             const float d = y - t[v];
             se += (double)d * d;
             cnt += 1.0;
-            gr = (float)(2.0 * scale) * d * y * (1.f - y);
+            gr = (float)scale * d;
         }
         if (g) {
             g[v * 16] = __float2bfloat16(gr);

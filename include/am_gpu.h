@@ -202,10 +202,11 @@ am_status am_ku_apply(am_problem *p, const am_simp_config *cfg, const double *rh
  * with the operator of rho, its Jacobi diagonal D and the constraint bits of load
  * case `load_case` (fixed and orphan DOFs), p = D^-1 r + beta p_prev and
  * q = mask(K p) in FP32, and *pq = p.q.  Vectors in the reference DOF order, FP64
- * in and out.  impl 3: the kernel the solver uses (tensor-copy staged, no CTA-wide
- * barrier per plane); impl 4: the staged kernel with a CTA barrier per plane and
- * tensor-store output tiles; impl 2: the register-direct kernel (all three the
- * same arithmetic, bitwise equal results). */
+ * in and out.  impl 3: the kernel the solver uses (tensor-copy staged, a CTA
+ * barrier per plane, tensor-store output tiles); impl 4: the staged kernel
+ * without a CTA-wide barrier per plane (per-warp-pair mailboxes, per-lane
+ * stores); impl 2: the register-direct kernel (all three the same arithmetic,
+ * bitwise equal results). */
 am_status am_ku_pcg_step(am_problem *p, const am_simp_config *cfg, const double *rho, int load_case,
                          const double *r, const double *p_prev, double beta, int impl, double *p_out,
                          double *q_out, double *pq);
@@ -280,9 +281,9 @@ long long am_launch_count(void);
 /* Times `reps` single launches of one kernel on the problem's stream with CUDA
  * events, after am_simp_begin (on the state the last am_simp_step left, or, before
  * the first step, on the initial density with zero vectors): which = 0 the
- * fused FP32 PCG K*u the solver runs (tensor-copy staged, 5 stages, no CTA-wide
- * barrier per plane), 12 / 13 the staged kernel with a CTA barrier per plane (4
- * stages) / the barrier-free one with 4 stages, 1 the FP64
+ * fused FP32 PCG K*u the solver runs (tensor-copy staged, 4 stages, a CTA
+ * barrier per plane), 12 the same kernel, 13 the staged kernel without a
+ * CTA-wide barrier per plane (4 stages), 1 the FP64
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
  * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
@@ -401,8 +402,9 @@ am_status am_unet_param_grad(am_unet *u, int n, int gz, int gy, int gx, const fl
  * [S][gz][gy][gx], mask [S][gz][gy][gx] (nonzero: the cell counts in the loss). */
 am_status am_unet_set_data(am_unet *u, int n_samples, int gz, int gy, int gx, const float *inputs,
                            const float *targets, const uint8_t *mask);
-/* Adam on the mean squared error of the sigmoid output against the targets over the
- * masked cells; epoch_loss (nullable) receives each epoch's mean.  cfg->loss unused. */
+/* Adam on the binary cross-entropy of the sigmoid output against the target
+ * densities over the masked cells; epoch_loss (nullable) receives each epoch's mean
+ * squared error of the sigmoid output.  cfg->loss unused. */
 am_status am_unet_train(am_unet *u, const am_train_config *cfg, float *epoch_loss);
 /* Mean squared error over the whole training set. */
 am_status am_unet_eval(am_unet *u, double *mse);

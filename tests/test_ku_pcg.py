@@ -8,9 +8,9 @@ diagonal and mask zeroing the fixed and orphan DOFs.  Checked against
     tolerance), masked DOFs exactly 0, p.q against numpy's dot of the returned
     vectors within 1e-6 of sum |p||q| (a node's three products are summed in
     FP32, the nodes in double-float);
-  * the staged kernel with a CTA barrier per plane and tensor-store output
-    tiles (impl 4) and the register-direct kernel (impl 2): p and q bitwise
-    equal, p.q equal to the impl-4 kernel's.
+  * the staged kernel without a CTA-wide barrier per plane (impl 4) and the
+    register-direct kernel (impl 2): p and q bitwise equal, p.q equal to the
+    impl-4 kernel's.
 Shapes span several 28-column, 15-row and z-chunk tiles, odd remainders and a
 single element.
 """
@@ -65,7 +65,7 @@ def test_pcg_step_matches_oracle_and_previous_kernel(shape, beta):
     p4, q4, pq4 = p.ku_pcg_step(cfg, rho, r, p_prev, beta, impl=4)
     assert np.array_equal(p3, p2) and np.array_equal(p4, p2)
     assert np.array_equal(q3, q2) and np.array_equal(q4, q2)
-    # the barrier-free and the barrier-per-plane staged kernels sum in the same order
+    # the barrier-per-plane and the barrier-free staged kernels sum in the same order
     assert pq3 == pq4
 
     s = O.scales(0, rho.ravel(), None, 3.0, 1e-9, 0.01, 1.0)
