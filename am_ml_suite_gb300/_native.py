@@ -203,6 +203,8 @@ SIGNATURES = {
     "am_precond_train": (ctypes.c_int, [_vp, ctypes.POINTER(TrainConfig), ctypes.POINTER(ctypes.c_float)]),
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
+    "am_problem_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
     "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.POINTER(_vp)]),
@@ -453,6 +455,11 @@ class Problem:
               "am_problem_set_preconditioner")
         self._pre = pre
 
+    def set_device_loop(self, on=True):
+        """True (default): each inner PCG solve is one CUDA-graph launch with a
+        device-side loop; False: the host launches and checks chunk by chunk."""
+        check(load().am_problem_set_device_loop(self.handle, int(bool(on))), "am_problem_set_device_loop")
+
     def layout_info(self):
         n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
         t = ctypes.c_int(0)
@@ -688,6 +695,9 @@ class Batch:
         st = _vp()
         check(load().am_batch_stream(self.handle, ctypes.byref(st)), "am_batch_stream")
         return int(st.value or 0)
+
+    def set_device_loop(self, on=True):
+        check(load().am_batch_set_device_loop(self.handle, int(bool(on))), "am_batch_set_device_loop")
 
     def simp_begin(self, cfgs, rho0_list=None):
         if len(cfgs) != self.n:

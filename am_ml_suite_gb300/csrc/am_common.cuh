@@ -65,7 +65,8 @@ struct Scalars {
     double b2;
     int frozen, pad3;
     // set by a kernel whose bounded wait on its bulk copies ran out (ST_TIMEOUT)
-    int kerr, pad4;
+    int kerr;
+    int loops;  // chunks run by the device-side loop of the current solve
 };
 
 enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_MAXIT = 2, ST_BREAKDOWN = 3, ST_NAN = 4, ST_UPDATE = 5, ST_TIMEOUT = 6 };

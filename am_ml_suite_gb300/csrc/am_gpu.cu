@@ -153,9 +153,11 @@ struct am_problem {
     int ntaps = 0;
     double taps_r = -1.0;
     int taps_variant = -1;
-    // CUDA graphs of PCG chunks
-    cudaGraphExec_t g32 = nullptr, g64 = nullptr;
+    // CUDA graphs of PCG chunks (host-driven loop) and of whole inner solves
+    // (device-side while loop over chunks)
+    cudaGraphExec_t g32 = nullptr, g64 = nullptr, gl32 = nullptr, gl64 = nullptr;
     int chunk = 32;
+    bool device_loop = false;
 
     // SIMP state
     bool simp_begun = false;
@@ -322,9 +324,26 @@ am_status free_rhs_norm(am_problem *P, int lc, double *bnorm2) {
     return AM_OK;
 }
 
+// The device-side loop of an inner solve: a CUDA-graph while node whose body is
+// one chunk of PCG iterations followed by pcg_loop_next_kernel, which keeps the
+// loop going while the solve runs and fewer than maxit / chunk + 4 chunks have run
+// (every chunk either advances the iteration count or ends the solve, so the cap
+// only catches a state that stops advancing).  pcg_loop_reset_kernel, upstream of
+// the while node, zeroes the chunk count and opens the loop unless the solve has
+// already ended.
+__global__ void pcg_loop_reset_kernel(cudaGraphConditionalHandle h, Scalars *S) {
+    S->loops = 0;
+    cudaGraphSetConditional(h, S->done ? 0u : 1u);
+}
+__global__ void pcg_loop_next_kernel(cudaGraphConditionalHandle h, Scalars *S, int chunk) {
+    const int n = ++S->loops;
+    const int cap = S->maxit / chunk + 4;
+    cudaGraphSetConditional(h, (!S->done && n < cap) ? 1u : 0u);
+}
+
+// captures one chunk of PCG iterations into the stream's capture
 template <typename T>
-am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
-    cudaGraph_t g = nullptr;
+cudaError_t capture_pcg_chunk(am_problem *P) {
     const KuLaunch &K = std::is_same<T, float>::value ? P->plan32 : P->plan64;
     double *x = nullptr;
     T *r, *pa, *pb, *q;
@@ -337,26 +356,83 @@ am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
         x = P->xw64.p; r = P->r64.p; pa = P->p64a.p; pb = P->p64b.p; q = P->q64v.p;
         dinv = P->dinv64.p; s = P->s64.p; M = P->M64;
     }
-    const long long launches_before = launch_count();
-    CK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < P->chunk; ++k) {
         // the p ping-pong member is chosen on the device from the parity of S->it
-        cudaError_t e1, e2;
+        cudaError_t e;
         if constexpr (std::is_same<T, float>::value) {
-            e1 = pcg_ku32(P);
-            e2 = pcg_update_df(P->L, P->x32.p, P->xl32.p, r, pa, pb, q, dinv, P->partial.p, P->S, P->st);
+            e = pcg_ku32(P);
+            if (e == cudaSuccess)
+                e = pcg_update_df(P->L, P->x32.p, P->xl32.p, r, pa, pb, q, dinv, P->partial.p, P->S, P->st);
         } else {
-            e1 = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
-            e2 = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
+            e = ku_pcg<T>(K, P->L, M, s, pa, pb, r, dinv, P->mask.p, q, P->partial.p, P->S, P->st);
+            if (e == cudaSuccess)
+                e = pcg_update<T>(P->L, x, r, pa, pb, q, dinv, P->partial.p, P->S, P->nblocks_vec, P->st);
         }
-        if (e1 != cudaSuccess || e2 != cudaSuccess) {
-            cudaStreamEndCapture(P->st, &g);
-            if (g) cudaGraphDestroy(g);
-            return fail(AM_ERR_CUDA, std::string("PCG capture: ") +
-                                         cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
-        }
+        if (e != cudaSuccess) return e;
     }
-    CK(cudaStreamEndCapture(P->st, &g));
+    return cudaSuccess;
+}
+
+template <typename T>
+am_status build_pcg_loop_graph(am_problem *P, cudaGraphExec_t *out) {
+    const long long launches_before = launch_count();
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    auto bail = [&](cudaError_t e, const char *what) {
+        cudaGraphDestroy(g);
+        return fail(AM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return bail(e, "PCG loop handle");
+    e = cudaStreamBeginCaptureToGraph(P->st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bail(e, "PCG loop capture");
+    pcg_loop_reset_kernel<<<1, 1, 0, P->st>>>(h, P->S);
+    e = cudaGetLastError();
+    cudaGraph_t gc = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(P->st, &gc);
+    if (e != cudaSuccess || e2 != cudaSuccess) return bail(e != cudaSuccess ? e : e2, "PCG loop capture");
+    cudaGraphNode_t reset = nullptr;
+    size_t nn = 1;
+    e = cudaGraphGetNodes(g, &reset, &nn);
+    if (e != cudaSuccess || nn != 1) return bail(e != cudaSuccess ? e : cudaErrorUnknown, "PCG loop reset node");
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond = nullptr;
+    e = cudaGraphAddNode(&cond, g, &reset, nullptr, 1, &cp);
+    if (e != cudaSuccess) return bail(e, "PCG loop node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(P->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bail(e, "PCG loop body capture");
+    e = capture_pcg_chunk<T>(P);
+    if (e == cudaSuccess) {
+        pcg_loop_next_kernel<<<1, 1, 0, P->st>>>(h, P->S, P->chunk);
+        e = cudaGetLastError();
+    }
+    cudaGraph_t gb = nullptr;
+    const cudaError_t e3 = cudaStreamEndCapture(P->st, &gb);
+    if (e != cudaSuccess || e3 != cudaSuccess) return bail(e != cudaSuccess ? e : e3, "PCG loop body capture");
+    count_launches(launches_before - launch_count());  // captured, not executed
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(AM_ERR_CUDA, std::string("PCG loop instantiate: ") + cudaGetErrorString(e));
+    return AM_OK;
+}
+
+template <typename T>
+am_status build_pcg_graph(am_problem *P, cudaGraphExec_t *out) {
+    cudaGraph_t g = nullptr;
+    const long long launches_before = launch_count();
+    CK(cudaStreamBeginCapture(P->st, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e1 = capture_pcg_chunk<T>(P);
+    const cudaError_t e2 = cudaStreamEndCapture(P->st, &g);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(AM_ERR_CUDA, std::string("PCG capture: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    }
     count_launches(launches_before - launch_count());  // captured, not executed
     cudaError_t e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
@@ -369,22 +445,32 @@ template <typename T>
 am_status run_pcg(am_problem *P, int *its, int *status) {
     cudaGraphExec_t *gx = std::is_same<T, float>::value ? &P->g32 : &P->g64;
     if constexpr (std::is_same<T, float>::value) CKS(ku3_ready(P));
-    if (!*gx) CKS(build_pcg_graph<T>(P, gx));
+    if (!P->device_loop && !*gx) CKS(build_pcg_graph<T>(P, gx));
     if (P->inject_kerr) {
         static const int kOne = 1;
         P->inject_kerr = false;
         CK(cudaMemcpyAsync(&P->S->kerr, &kOne, sizeof(int), cudaMemcpyHostToDevice, P->st));
     }
-    CKS(sync_scalars(P));
-    // every chunk either advances the iteration count or ends the solve; the
-    // host bound below only catches a solver state that stops advancing
-    const long long max_chunks = (long long)P->Sh->maxit / P->chunk + 4;
-    long long chunks = 0;
-    while (!P->Sh->done) {
-        if (++chunks > max_chunks) return fail(AM_ERR_TIMEOUT, "PCG did not terminate within its iteration cap");
-        CK(cudaGraphLaunch(*gx, P->st));
-        count_launches(2LL * P->chunk);
+    if (P->device_loop) {
+        // the whole inner solve in one graph launch, the loop decided on the device
+        cudaGraphExec_t *gl = std::is_same<T, float>::value ? &P->gl32 : &P->gl64;
+        if (!*gl) CKS(build_pcg_loop_graph<T>(P, gl));
+        CK(cudaGraphLaunch(*gl, P->st));
         CKS(sync_scalars(P));
+        count_launches(1 + (2LL * P->chunk + 1) * P->Sh->loops);
+        if (!P->Sh->done) return fail(AM_ERR_TIMEOUT, "PCG did not terminate within its iteration cap");
+    } else {
+        CKS(sync_scalars(P));
+        // every chunk either advances the iteration count or ends the solve; the
+        // host bound below only catches a solver state that stops advancing
+        const long long max_chunks = (long long)P->Sh->maxit / P->chunk + 4;
+        long long chunks = 0;
+        while (!P->Sh->done) {
+            if (++chunks > max_chunks) return fail(AM_ERR_TIMEOUT, "PCG did not terminate within its iteration cap");
+            CK(cudaGraphLaunch(*gx, P->st));
+            count_launches(2LL * P->chunk);
+            CKS(sync_scalars(P));
+        }
     }
     if constexpr (std::is_same<T, float>::value) {
         // the iterate folds every second iteration: pay the term a solve that
@@ -918,8 +1004,8 @@ am_status am_problem_destroy(am_problem *P) {
     if (!P) return AM_OK;
     cudaSetDevice(P->device);
     if (P->st) cudaStreamSynchronize(P->st);
-    if (P->g32) cudaGraphExecDestroy(P->g32);
-    if (P->g64) cudaGraphExecDestroy(P->g64);
+    for (cudaGraphExec_t g : {P->g32, P->g64, P->gl32, P->gl64})
+        if (g) cudaGraphExecDestroy(g);
     for (auto &c : P->cases) {
         c.F.release(); c.fixed_bits.release(); c.f_idx.release(); c.f_val.release(); c.x64.release();
     }
@@ -1487,6 +1573,12 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
 am_status am_problem_set_preconditioner(am_problem *P, am_precond *m) {
     CKS(check_problem(P));
     P->pre = m;
+    return AM_OK;
+}
+
+am_status am_problem_set_device_loop(am_problem *P, int on) {
+    CKS(check_problem(P));
+    P->device_loop = on != 0;
     return AM_OK;
 }
 

@@ -106,7 +106,10 @@ struct am_batch {
     // FP32 K*u plan (autotuner): warps per CTA, z chunk (0 = all planes), CTAs per SM
     int warps = 8, zchunk = 0, ctas = 2;
     bool loads_set = false;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;  // one chunk of batched PCG iterations
+    cudaGraphExec_t loop = nullptr;   // a whole FP32 PCG round: a device-side while loop over chunks
+    Pool<int> loopc;                  // [0] chunks run by the loop, [1] its cap
+    bool device_loop = false;
     std::vector<long long> pcg_its;
     // SIMP state between am_batch_simp_begin and the steps
     bool begun = false;
@@ -161,6 +164,86 @@ am_status plan_k2(am_batch *B, int warps, int zchunk) {
         cudaGraphExecDestroy(B->graph);
         B->graph = nullptr;
     }
+    if (B->loop) {
+        cudaGraphExecDestroy(B->loop);
+        B->loop = nullptr;
+    }
+    return AM_OK;
+}
+
+// The device-side loop of a batched FP32 PCG round: a CUDA-graph while node whose
+// body is one chunk followed by batch_loop_next_kernel, which keeps the loop going
+// while some problem of the batch is still iterating and fewer than the cap's
+// chunks have run; batch_loop_reset_kernel, upstream of the node, zeroes the count
+// and opens the loop if some problem is iterating.
+__device__ __forceinline__ bool batch_any_active(const Scalars *S, int n) {
+    int active = 0;
+    for (int p = threadIdx.x; p < n; p += blockDim.x) active |= (!S[p].frozen && !S[p].done) ? 1 : 0;
+    return __syncthreads_or(active) != 0;
+}
+__global__ void batch_loop_reset_kernel(cudaGraphConditionalHandle h, const Scalars *S, int n, int *loopc) {
+    const bool active = batch_any_active(S, n);
+    if (threadIdx.x == 0) {
+        loopc[0] = 0;
+        cudaGraphSetConditional(h, active ? 1u : 0u);
+    }
+}
+__global__ void batch_loop_next_kernel(cudaGraphConditionalHandle h, const Scalars *S, int n, int *loopc) {
+    const bool active = batch_any_active(S, n);
+    if (threadIdx.x == 0) {
+        const int c = ++loopc[0];
+        cudaGraphSetConditional(h, (active && c < loopc[1]) ? 1u : 0u);
+    }
+}
+
+am_status build_loop_graph(am_batch *B) {
+    if (B->loop) return AM_OK;
+    if (!B->loopc.p) BCK(B->loopc.alloc(2));
+    const long long launches_before = launch_count();
+    cudaGraph_t g = nullptr;
+    BCK(cudaGraphCreate(&g, 0));
+    auto bail = [&](cudaError_t e, const char *what) {
+        cudaGraphDestroy(g);
+        return bfail(AM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return bail(e, "batch loop handle");
+    e = cudaStreamBeginCaptureToGraph(B->st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bail(e, "batch loop capture");
+    batch_loop_reset_kernel<<<1, 256, 0, B->st>>>(h, B->S.p, B->n, B->loopc.p);
+    e = cudaGetLastError();
+    cudaGraph_t gc = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(B->st, &gc);
+    if (e != cudaSuccess || e2 != cudaSuccess) return bail(e != cudaSuccess ? e : e2, "batch loop capture");
+    cudaGraphNode_t reset = nullptr;
+    size_t nn = 1;
+    e = cudaGraphGetNodes(g, &reset, &nn);
+    if (e != cudaSuccess || nn != 1) return bail(e != cudaSuccess ? e : cudaErrorUnknown, "batch loop reset node");
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond = nullptr;
+    e = cudaGraphAddNode(&cond, g, &reset, nullptr, 1, &cp);
+    if (e != cudaSuccess) return bail(e, "batch loop node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(B->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bail(e, "batch loop body capture");
+    for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
+        e = batch_pcg_iteration(B->items_d.p, B->k2, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
+    if (e == cudaSuccess) {
+        batch_loop_next_kernel<<<1, 256, 0, B->st>>>(h, B->S.p, B->n, B->loopc.p);
+        e = cudaGetLastError();
+    }
+    cudaGraph_t gb = nullptr;
+    const cudaError_t e3 = cudaStreamEndCapture(B->st, &gb);
+    if (e != cudaSuccess || e3 != cudaSuccess) return bail(e != cudaSuccess ? e : e3, "batch loop body capture");
+    count_launches(launches_before - launch_count());  // captured, not executed
+    e = cudaGraphInstantiate(&B->loop, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(AM_ERR_CUDA, std::string("batch loop instantiate: ") + cudaGetErrorString(e));
     return AM_OK;
 }
 
@@ -171,6 +254,7 @@ am_status sync_scalars(am_batch *B) {
 }
 
 am_status build_graph(am_batch *B) {
+    if (B->device_loop) return build_loop_graph(B);
     if (B->graph) return AM_OK;
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
@@ -205,14 +289,26 @@ am_status batch_solve(am_batch *B, int max_chunks) {
             if (!B->Sh[p].frozen && !std::isfinite(B->Sh[p].res_rr))
                 return bfail(AM_ERR_NAN_DETECTED, "NaN in the residual of batch problem " + std::to_string(p));
         if (all_done(B)) return AM_OK;
-        int chunks = 0;
-        while (true) {
-            BCK(cudaGraphLaunch(B->graph, B->st));
-            count_launches(2LL * kChunk);
+        if (B->device_loop) {
+            // the round's chunks in one graph launch, the loop decided on the device
+            const int lc[2] = {0, max_chunks + 1};
+            BCK(cudaMemcpyAsync(B->loopc.p, lc, sizeof(lc), cudaMemcpyHostToDevice, B->st));
+            BCK(cudaGraphLaunch(B->loop, B->st));
+            int ran[2] = {0, 0};
+            BCK(cudaMemcpyAsync(ran, B->loopc.p, sizeof(ran), cudaMemcpyDeviceToHost, B->st));
             BCKS(sync_scalars(B));
-            ++chunks;
-            if (all_done(B)) break;
-            if (chunks > max_chunks) return bfail(AM_ERR_TIMEOUT, "batched PCG did not stop within its cap");
+            count_launches(1 + (2LL * kChunk + 1) * ran[0]);
+            if (!all_done(B)) return bfail(AM_ERR_TIMEOUT, "batched PCG did not stop within its cap");
+        } else {
+            int chunks = 0;
+            while (true) {
+                BCK(cudaGraphLaunch(B->graph, B->st));
+                count_launches(2LL * kChunk);
+                BCKS(sync_scalars(B));
+                ++chunks;
+                if (all_done(B)) break;
+                if (chunks > max_chunks) return bfail(AM_ERR_TIMEOUT, "batched PCG did not stop within its cap");
+            }
         }
         BCK(batch_inner_end(B->items_d.p, B->vec, kSms * 8, B->st));
         for (int p = 0; p < B->n; ++p) {
@@ -242,6 +338,8 @@ am_status am_batch_destroy(am_batch *B) {
     cudaSetDevice(B->device);
     if (B->st) cudaStreamSynchronize(B->st);
     if (B->graph) cudaGraphExecDestroy(B->graph);
+    if (B->loop) cudaGraphExecDestroy(B->loop);
+    B->loopc.release();
     for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi,
                     &B->F, &B->x64, &B->r64, &B->dinv64, &B->f_val, &B->tap_w, &B->partial})
         q->release();
@@ -494,6 +592,12 @@ am_status am_batch_autotune(am_batch *B, int reps, int *warps, int *z_chunk, int
     if (z_chunk) *z_chunk = bc.z;
     if (ctas_per_sm) *ctas_per_sm = bc.c;
     if (best_ms) *best_ms = best;
+    return AM_OK;
+}
+
+am_status am_batch_set_device_loop(am_batch *B, int on) {
+    BCKS(check_batch(B));
+    B->device_loop = on != 0;
     return AM_OK;
 }
 

@@ -374,6 +374,15 @@ am_status am_precond_eval(am_precond *m, long long first, long long count, int l
  * FP64 residual accepts every solve, as with Jacobi. */
 am_status am_problem_set_preconditioner(am_problem *p, am_precond *m);
 
+/* How an inner FP32 (or FP64) PCG solve is driven.  on != 0 (the default): one
+ * CUDA-graph launch per solve, a device-side while loop over chunks of 32
+ * iterations that ends when the solve ends or after maxit / 32 + 4 chunks; the
+ * host waits once.  on == 0: one graph launch per chunk, the host reading the
+ * solver state between chunks.  Both run the same kernels in the same order (same
+ * results); no reference counterpart (Eigen's CG loop runs on the host,
+ * linear_solver.cpp:136-155). */
+am_status am_problem_set_device_loop(am_problem *p, int on);
+
 /* ---- density-predicting U-Net (the reference's am.ai TopOptUNet) -----------------------
  * A 3-D U-Net predicting the optimised density field from a problem encoding: the
  * network the reference declares in src/am/ai/model.py:18-67 (in_channels 4,
@@ -436,6 +445,12 @@ am_status am_batch_autotune(am_batch *b, int reps, int *warps, int *z_chunk, int
 
 /* The CUDA stream the batch's kernels run on (cudaStream_t). */
 am_status am_batch_stream(am_batch *b, void **stream);
+
+/* As am_problem_set_device_loop, for the batch's FP32 PCG rounds: on != 0 (the
+ * default) each round's chunks run in one graph launch whose device-side while
+ * loop ends when no problem is iterating (or at the chunk cap); on == 0 the host
+ * checks every problem between chunks. */
+am_status am_batch_set_device_loop(am_batch *b, int on);
 
 /* Starts every problem's SIMP loop with its own config cfgs[i] (variant must be
  * AM_VARIANT_CPP); rho0 as for am_batch_simp_run.  Resets the solver state. */

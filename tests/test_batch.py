@@ -142,3 +142,21 @@ def test_batch_step_api_matches_run():
         assert np.allclose(got, r["compliance"], rtol=1e-12, atol=0)
         assert np.array_equal(dens[p], r["density"])
         assert b.pcg_iterations[p] == r["pcg_iterations"]
+
+
+def test_batch_device_loop_matches_host_loop():
+    """The batch's FP32 PCG rounds driven by the device-side graph loop (default)
+    and chunk by chunk from the host run the same kernels in the same order:
+    identical compliance histories, densities and PCG iteration counts."""
+    out = []
+    for on in (True, False):
+        b, _ = _batch(SHAPES, seed=9)
+        b.set_device_loop(on)
+        res = b.simp_run([_cfg(4, tol=1e-7) for _ in SHAPES])
+        out.append((res, [r["pcg_iterations"] for r in res]))
+        b.close()
+    (dev, it_dev), (host, it_host) = out
+    assert it_dev == it_host and min(it_dev) > 0
+    for a, h in zip(dev, host):
+        assert np.array_equal(a["compliance"], h["compliance"])
+        assert np.array_equal(a["density"], h["density"])

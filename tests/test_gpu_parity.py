@@ -349,3 +349,32 @@ def test_simp_cfg1_mixed_50_iterations_density():
     assert r["iterations"] == iters
     assert np.abs(r["density"] - ref["density"].ravel()).max() <= 1e-4
     assert abs(r["compliance"][-1] - ref["compliance"][-1]) / ref["compliance"][-1] <= 1e-4
+
+
+@pytest.mark.parametrize("precision", [nat.PREC_MIXED, nat.PREC_FP64])
+def test_device_loop_matches_host_loop(precision):
+    """An inner PCG solve run as one graph launch with a device-side while loop
+    (default) and chunk by chunk from the host: same kernels, same order, so the
+    same displacement bit for bit and the same iteration counts; a SIMP run too."""
+    shape = (33, 9, 10)
+    nx, ny, nz = shape
+    base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(3 * (nx + 1) * (ny + 1) * (nz + 1))
+    F[-1] = -1.0
+    rho = np.random.default_rng(4).uniform(0.05, 1.0, size=shape)
+    cfg = nat.default_config(nat.VARIANT_CPP, precision=precision, cg_tol=1e-9, warm_start=0)
+    got = []
+    for on in (True, False):
+        p = nat.Problem(shape)
+        p.set_loads([F], [fixed])
+        p.set_device_loop(on)
+        u, st = p.solve(cfg, rho)
+        r = p.simp_run(nat.default_config(nat.VARIANT_CPP, precision=precision, max_iterations=3,
+                                          convergence_tol=0.0, cg_tol=1e-7), np.full(shape, 0.3))
+        got.append((u, st.iterations, st.converged, r))
+        p.close()
+    (u1, i1, c1, r1), (u0, i0, c0, r0) = got
+    assert c1 and c0 and i1 == i0 and i1 > 0
+    assert np.array_equal(u1, u0)
+    assert np.array_equal(r1["compliance"], r0["compliance"]) and np.array_equal(r1["density"], r0["density"])
