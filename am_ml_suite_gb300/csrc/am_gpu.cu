@@ -157,7 +157,7 @@ struct am_problem {
     // (device-side while loop over chunks)
     cudaGraphExec_t g32 = nullptr, g64 = nullptr, gl32 = nullptr, gl64 = nullptr;
     int chunk = 32;
-    bool device_loop = false;
+    bool device_loop = true;
 
     // SIMP state
     bool simp_begun = false;

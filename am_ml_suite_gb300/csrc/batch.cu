@@ -109,7 +109,7 @@ struct am_batch {
     cudaGraphExec_t graph = nullptr;  // one chunk of batched PCG iterations
     cudaGraphExec_t loop = nullptr;   // a whole FP32 PCG round: a device-side while loop over chunks
     Pool<int> loopc;                  // [0] chunks run by the loop, [1] its cap
-    bool device_loop = false;
+    bool device_loop = true;
     std::vector<long long> pcg_its;
     // SIMP state between am_batch_simp_begin and the steps
     bool begun = false;

@@ -731,13 +731,25 @@ cudaError_t launch_march(const CUtensorMap &mx, const CUtensorMap &mw, const TcF
     const int sms = sm_count();
     const int ty16 = (g.dy + 15) / 16;
     const long long columns = (long long)a.tiles_x * ty16 * g.n;
-    // about four work items per CTA, runs of at least 4 planes
-    const long long runs = std::max<long long>(1, std::min<long long>((4LL * sms + columns - 1) / columns,
+    // a CTA spends most of a plane step waiting on copies and MMAs: as many CTAs per
+    // SM as registers and shared memory allow (at most 4; their accumulators take at
+    // most 4 x 64 of the 512 tensor-memory columns), about four work items each, runs
+    // of at least 4 planes
+    static int per_sm = 0;
+    if (!per_sm) {
+        int nb = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, conv_tc_march_kernel<N, CIN>, kFwdThreads, smem) !=
+            cudaSuccess)
+            nb = 1;
+        per_sm = std::max(1, std::min(4, nb));
+    }
+    const long long ctas = (long long)per_sm * sms;
+    const long long runs = std::max<long long>(1, std::min<long long>((4LL * ctas + columns - 1) / columns,
                                                                       (g.dz + 3) / 4));
     const int zrun = (int)((g.dz + runs - 1) / runs);
     const long long nitems = columns * ((g.dz + zrun - 1) / zrun);
     if (nitems > 0x7fffffffLL) return cudaErrorInvalidValue;
-    const int grid = (int)std::min<long long>(nitems, sms);
+    const int grid = (int)std::min<long long>(nitems, ctas);
     conv_tc_march_kernel<N, CIN><<<grid, kFwdThreads, smem, st>>>(mx, mw, a, ty16, zrun, (int)nitems);
     return cudaGetLastError();
 }

@@ -354,6 +354,7 @@ ARM_DESC = {
 _inner_tol = 0.0
 _mg_deflation = 1
 _mixed_solver = "reliable"
+_host_loop = False
 MIXED_SOLVER = {"reliable": 0, "flexible": 1}
 
 
@@ -441,6 +442,7 @@ def time_arm(nat, torch, W, arm, steps, pre=None, keep=False):
     CUDA events on the library's stream (allocation and set-up of the fresh state
     included).  Returns the per-step results and, if keep, the open problem."""
     p = nat.Problem(W["shape"], 1.0, 1.0, 0.3)
+    p.set_device_loop(not _host_loop)
     p.set_loads([W["F"]], [W["fixed"]])
     if pre is not None:
         p.set_preconditioner(pre)
@@ -502,6 +504,7 @@ def e2e_run(nat, torch, W, arm, iterations, pre_weights=None):
         w_h, _tw = pinned(pre_weights, torch.float32)
     cfg = simp_config(nat, W, max_iterations=iterations, arm=arm)
     q = nat.Problem(W["shape"], 1.0, 1.0, 0.3)
+    q.set_device_loop(not _host_loop)
     pre = nat.Preconditioner(seed=0, capacity=0) if w_h is not None else None
     torch.cuda.synchronize()
     te0 = time.perf_counter()
@@ -561,9 +564,13 @@ def main():
     ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
                     help="jacobi arm: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
                          "flexible CG over FP32 inner solves (flexible)")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="drive every inner PCG solve chunk by chunk from the host instead of the device-side "
+                         "graph loop (same results; the measurement baseline of the loop)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global _mixed_solver, _inner_tol, _mg_deflation
+    global _mixed_solver, _inner_tol, _mg_deflation, _host_loop
+    _host_loop = args.host_loop
     _mixed_solver = args.mixed_solver
     _mg_deflation = args.mg_deflation
     _inner_tol = args.inner_tol
@@ -809,6 +816,7 @@ def main():
                        "description": W["desc"], "precision": "mixed", "primary_arm": primary,
                        "arms": {a: ARM_DESC[a] for a in arms}, "window": "SIMP steps 1..K of a fresh problem",
                        "cg_tol": 1e-6, "l2": "working set per step > 129 MB L2; roofline probes flush L2",
+                       "solver_loop": "host, chunk by chunk" if _host_loop else "device-side CUDA-graph while loop",
                        "parallelism": f"replicas x{world}"},
             "pcg_solve_ms": results[primary]["pcg_solve_ms"],
             "pcg_iterations_per_solve": results[primary]["pcg_iterations_per_solve"],

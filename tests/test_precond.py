@@ -23,26 +23,40 @@ def _split(w):
     return out
 
 
-def _unet_reference(x, ws):
-    """float64 CPU reference: x (n, gz, gy, gx, 4); ws per layer [27][cout][cin]."""
+def _unet_reference(x, ws, bf16_forward=False):
+    """float64 CPU reference: x (n, gz, gy, gx, 4); ws per layer [27][cout][cin].
+
+    bf16_forward: round the input, every stored activation (ReLU outputs, pooled
+    tensors) and the weights to BF16 where the GPU network stores them, and
+    differentiate that forward pass exactly -- the GPU's arithmetic with exact
+    sums and exact gradients."""
     torch = pytest.importorskip("torch")
     F = torch.nn.functional
     W = [torch.tensor(w, dtype=torch.float64, requires_grad=True) for w in ws]
 
+    def bf(t):
+        if not bf16_forward:
+            return t
+        # rounded values in the forward pass, the identity for the gradient
+        return t + (t.detach().to(torch.bfloat16).to(torch.float64) - t.detach())
+
     def conv(l, t, relu=True):
         cout, cin = W[l].shape[1], t.shape[1]
-        k = W[l][:, :, :cin].reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)
+        k = bf(W[l])[:, :, :cin].reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)
         y = F.conv3d(t, k, padding=1)
-        return F.relu(y) if relu else y
+        return bf(F.relu(y)) if relu else y
 
     def up(t):
         return F.interpolate(t, scale_factor=2, mode="nearest")
 
-    t = torch.tensor(x, dtype=torch.float64).permute(0, 4, 1, 2, 3)
+    def pool(t):
+        return bf(F.avg_pool3d(t, 2))
+
+    t = bf(torch.tensor(x, dtype=torch.float64).permute(0, 4, 1, 2, 3))
     e1 = conv(1, conv(0, t))
-    e2 = conv(3, conv(2, F.avg_pool3d(e1, 2)))
-    e3 = conv(5, conv(4, F.avg_pool3d(e2, 2)))
-    e4 = conv(7, conv(6, F.avg_pool3d(e3, 2)))
+    e2 = conv(3, conv(2, pool(e1)))
+    e3 = conv(5, conv(4, pool(e2)))
+    e4 = conv(7, conv(6, pool(e3)))
     d3 = conv(9, conv(8, torch.cat([up(e4), e3], 1)))
     d2 = conv(11, conv(10, torch.cat([up(d3), e2], 1)))
     d1 = conv(13, conv(12, torch.cat([up(d2), e1], 1)))
@@ -89,14 +103,28 @@ def test_network_forward_and_weight_gradients_match_reference():
         errs.append(_rel(gg, gr))
         coss.append(float((gr * gg).sum() / (np.linalg.norm(gr) * np.linalg.norm(gg))))
     print("relative gradient error per layer", np.round(errs, 4), "cosine", np.round(coss, 5))
-    # The gradients are stored in BF16 after every backward stage and pass through
-    # ReLU masks taken from BF16 activations, so their error grows with depth from
-    # the output: <= 2 % at the output layer, <= 20 % at the bottleneck, with the
-    # direction (cosine) within 2 % everywhere.
+    # Against the float64 network the error grows with depth from the output (<= 2 %
+    # at the output layer, <= 20 % at the bottleneck, direction within 2 %): that is
+    # the BF16 forward pass -- activations and weights rounded where they are
+    # stored, which moves values and flips ReLU masks --, not the backward pass: a
+    # CPU emulation of the BF16 forward differentiated exactly gives the same
+    # per-layer errors whether or not its gradients are rounded to BF16.
     assert errs[14] <= 2e-2 and errs[13] <= 6e-2, errs
     assert max(errs) <= 0.2, errs
     assert min(coss) >= 0.98, coss
     assert np.all(g[0][:, :, 4:] == 0.0)  # padding input channels get no gradient
+    # Against that emulation (same rounding points, exact sums and gradients) every
+    # layer's gradient agrees to a few per mille: what remains is FP32 summation
+    # order, BF16 gradient storage and the rare ReLU mask that flips between them.
+    ref_b, W_b = _unet_reference(x.astype(np.float64), ws, bf16_forward=True)
+    assert _rel(got, ref_b.detach().numpy()) <= 1e-2
+    (ref_b * torch.tensor(dout, dtype=torch.float64)).sum().backward()
+    errs_b = []
+    for l, (cin, _) in enumerate(SPEC):
+        used = 4 if l == 0 else cin
+        errs_b.append(_rel(g[l][:, :, :used].astype(np.float64), W_b[l].grad.numpy()[:, :, :used]))
+    print("relative gradient error per layer against the BF16-forward emulation", np.round(errs_b, 4))
+    assert max(errs_b) <= 2e-2, errs_b
 
 
 def test_untrained_network_is_the_jacobi_step():
