@@ -204,6 +204,7 @@ SIGNATURES = {
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
     "am_problem_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_problem_set_residual_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
     "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
@@ -460,6 +461,11 @@ class Problem:
         device-side loop; False: the host launches and checks chunk by chunk."""
         check(load().am_problem_set_device_loop(self.handle, int(bool(on))), "am_problem_set_device_loop")
 
+    def set_residual_arithmetic(self, mode):
+        """RESID_DOUBLE_FLOAT (default) or RESID_FP64: the arithmetic of the mixed
+        solvers' residual replacements and acceptance test."""
+        check(load().am_problem_set_residual_arithmetic(self.handle, int(mode)), "am_problem_set_residual_arithmetic")
+
     def layout_info(self):
         n, e, cs = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_longlong(0)
         t = ctypes.c_int(0)
@@ -636,6 +642,7 @@ class UNet:
 
 
 CONV_MMA_SYNC, CONV_TCGEN05 = 0, 1
+RESID_DOUBLE_FLOAT, RESID_FP64 = 0, 1
 
 
 def set_conv_kernels(impl: int):

@@ -158,6 +158,7 @@ struct am_problem {
     cudaGraphExec_t g32 = nullptr, g64 = nullptr, gl32 = nullptr, gl64 = nullptr;
     int chunk = 32;
     bool device_loop = true;
+    bool resid_df = true;  // mixed solvers: residuals in double-float (false: FP64 kernel)
 
     // SIMP state
     bool simp_begun = false;
@@ -313,6 +314,18 @@ cudaError_t pcg_ku32(am_problem *P) {
         return ku3b_pcg(P->maps3, P->plan3, P->L, P->M32, P->q32v.p, P->p32a.p, P->p32b.p, P->partial.p, P->S, 5,
                         P->st);
     return ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, P->ku3_stages, P->st);
+}
+
+// r = mask(f - K x) (+ element energies into ce): the residual replacements and
+// the acceptance test of the mixed-precision solvers.  Double-float on the FP32
+// pipes by default (kudf.cuh); the FP64 kernel when `native` (FP64 precision) or
+// the problem's residual arithmetic is set to FP64.
+cudaError_t solver_resid(am_problem *P, bool native, const double *x, const double *f, double *ce) {
+    if (P->resid_df && !native)
+        return ku_resid_df(P->plan64, P->L, P->M64, P->s64.p, x, f, P->dinv64.p, P->mask.p, P->r64.p, ce,
+                           P->partial.p, P->S, P->st);
+    return ku_resid(P->plan64, P->L, P->M64, P->s64.p, x, f, P->dinv64.p, P->mask.p, P->r64.p, ce, P->partial.p,
+                    P->S, P->st);
 }
 
 // ||F||^2 over the free DOFs of case lc (mask already built)
@@ -620,8 +633,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         CKS(ensure_vectors(P, true));
         const int max_rounds = c.max_outer > 0 ? c.max_outer : 200;
         const double red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.1;
-        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
-                    want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+        CK(solver_resid(P, fp64, C.x64.p, C.F.p, want_ce ? P->ce.p : nullptr));
         CKS(sync_scalars(P));
         double rel = std::sqrt(P->Sh->res_rr / bnorm2);
         int total = 0, rounds = 0, restart = 0, stt = ST_RUNNING;
@@ -642,8 +654,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
                 break;
             }
             CK(df_accumulate(P->x32.p, P->xl32.p, C.x64.p, 3 * P->L.cs, P->nblocks_vec, P->st));
-            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
-                        want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+            CK(solver_resid(P, fp64, C.x64.p, C.F.p, want_ce ? P->ce.p : nullptr));
             CKS(sync_scalars(P));
             rel = std::sqrt(P->Sh->res_rr / bnorm2);
             nan = !std::isfinite(rel);
@@ -682,8 +693,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         const double inner_red = (c.inner_tol > 0.0 && c.inner_tol < 1.0) ? c.inner_tol : 0.01;
         const int inner_cap = std::max(50, maxit / 4);
         CK(cudaMemsetAsync(&P->S->o_status, 0, sizeof(int), P->st));
-        CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
-                    want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+        CK(solver_resid(P, fp64, C.x64.p, C.F.p, want_ce ? P->ce.p : nullptr));
         CKS(sync_scalars(P));
         double rel = std::sqrt(P->Sh->res_rr / bnorm2);
         int total = 0, outer = 0;
@@ -778,8 +788,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             }
             if (rel <= tol) {
                 // accept on the recomputed FP64 residual (and element energies)
-                CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p,
-                            P->r64.p, want_ce ? P->ce.p : nullptr, P->partial.p, P->S, P->st));
+                CK(solver_resid(P, fp64, C.x64.p, C.F.p, want_ce ? P->ce.p : nullptr));
                 CKS(sync_scalars(P));
                 rel = std::sqrt(P->Sh->res_rr / bnorm2);
             }
@@ -787,8 +796,7 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
         if (nan) return fail(AM_ERR_NAN_DETECTED, "NaN in the mixed-precision solve");
         if (want_ce && rel > tol) {
             // not converged: element energies of the returned iterate
-            CK(ku_resid(P->plan64, P->L, P->M64, P->s64.p, C.x64.p, C.F.p, P->dinv64.p, P->mask.p, P->r64.p,
-                        P->ce.p, P->partial.p, P->S, P->st));
+            CK(solver_resid(P, fp64, C.x64.p, C.F.p, P->ce.p));
             CKS(sync_scalars(P));
             rel = std::sqrt(P->Sh->res_rr / bnorm2);
         }
@@ -1530,6 +1538,10 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
             case 12:
                 CK(ku3_pcg(P->maps3, P->plan3, P->L, P->M32, P->partial.p, P->S, 4, P->st));
                 break;
+            case 14:
+                CK(ku_resid_df(P->plan64, P->L, P->M64, P->s64.p, P->cases[0].x64.p, P->cases[0].F.p,
+                               P->dinv64.p, P->mask.p, P->r64.p, nullptr, P->partial.p, P->S, P->st));
+                break;
             case 13:
                 CK(ku3b_pcg(P->maps3, P->plan3, P->L, P->M32, P->q32v.p, P->p32a.p, P->p32b.p, P->partial.p, P->S,
                             4, P->st));
@@ -1573,6 +1585,13 @@ am_status am_bench_kernel(am_problem *P, int which, int reps, int flush_l2, doub
 am_status am_problem_set_preconditioner(am_problem *P, am_precond *m) {
     CKS(check_problem(P));
     P->pre = m;
+    return AM_OK;
+}
+
+am_status am_problem_set_residual_arithmetic(am_problem *P, int mode) {
+    CKS(check_problem(P));
+    if (mode != AM_RESID_DOUBLE_FLOAT && mode != AM_RESID_FP64) return fail(AM_ERR_INVALID_ARG, "unknown residual mode");
+    P->resid_df = mode == AM_RESID_DOUBLE_FLOAT;
     return AM_OK;
 }
 

@@ -6,6 +6,7 @@
 #include "batch.cuh"
 #include "kernels.cuh"
 #include "ku.cuh"
+#include "kudf.cuh"
 #include "bulk.cuh"
 #include "ku2.cuh"
 
@@ -94,6 +95,9 @@ cudaError_t ku_init_attributes() {
     AMK_ATTR(double, 32, 4, KU_DOT)
     AMK_ATTR(double, 32, 8, KU_DOT)
 #undef AMK_ATTR
+    if ((e = cudaFuncSetAttribute(ku_resid_df_kernel<32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)KuShape<32, 4>::smem_bytes<double>())) != cudaSuccess)
+        return e;
     if ((e = update_init_attributes()) != cudaSuccess) return e;
     return filter_init_attributes();
 }
@@ -227,6 +231,31 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
     a.partial = partial;
     a.S = S;
     return dispatch_ku<double, KU_RESID>(K, a, st);
+}
+
+cudaError_t ku_resid_df(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
+                        const double *x, const double *f, const double *dinv, const uint8_t *mask, double *r,
+                        double *ce, double *partial, Scalars *S, cudaStream_t st) {
+    if (!(K.tx == 32 && K.ty == 4) || K.warps > 0) return cudaErrorInvalidValue;
+    KuArgs<double> a{};
+    a.L = L;
+    a.s = s;
+    a.u = x;
+    a.f = f;
+    a.dinv = dinv;
+    a.mask = mask;
+    a.y = r;
+    a.ce = ce;
+    a.energy = ce != nullptr;
+    a.partial = partial;
+    a.S = S;
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tiles_z = K.tiles_z;
+    a.tz = K.tz;
+    using Sh = KuShape<32, 4>;
+    ku_resid_df_kernel<32, 4><<<K.ntiles(), Sh::NT, Sh::smem_bytes<double>(), st>>>(a, modal_dflt(M));
+    return counted(cudaGetLastError());
 }
 
 cudaError_t ku_dot(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,

@@ -80,6 +80,12 @@ cudaError_t ku_pcg(const KuLaunch &K, const Layout &L, const Modal<T> &M, const 
 cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
                      const double *x, const double *f, const double *dinv, const uint8_t *mask,
                      double *r, double *ce, double *partial, Scalars *S, cudaStream_t st);
+// The same residual with the element operator and node sums in double-float
+// arithmetic on the FP32 pipes (kudf.cuh); FP64 inputs, outputs and sums.  The
+// 32 x 4 FP64 tile plan only.
+cudaError_t ku_resid_df(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
+                        const double *x, const double *f, const double *dinv, const uint8_t *mask, double *r,
+                        double *ce, double *partial, Scalars *S, cudaStream_t st);
 
 // ---- PCG vector kernels ------------------------------------------------------
 // FP64 PCG: x += alpha p; r -= alpha q (p = the pair member written this

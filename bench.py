@@ -544,7 +544,7 @@ def main():
     ap.add_argument("--no-other-workloads", action="store_true",
                     help="skip the short runs of the bracket (config 2) and the 256-problem batch (config 3) "
                          "reported in `other_workloads`")
-    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "ku3tile", "ku3b4",
+    ap.add_argument("--probe", choices=["ku", "resid", "update", "conv", "ku2", "ku3s3", "ku3tile", "ku3b4", "resid_df",
                                         "update_even", "update_odd",
                                         "filter", "oc", "vcycle", "vcycle_defl"],
                     help="only time `reps` launches of one kernel after set-up (bounded command for ncu)")
@@ -686,7 +686,7 @@ def main():
         p.set_loads([W["F"]], [W["fixed"]])
         p.simp_begin(simp_config(nat, W), W["rho0"])
         which = {"ku": 0, "resid": 1, "update": 2, "ku2": 4, "ku3s3": 5, "update_even": 6, "update_odd": 7,
-                 "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11, "ku3tile": 12, "ku3b4": 13}[args.probe]
+                 "filter": 8, "oc": 9, "vcycle": 10, "vcycle_defl": 11, "ku3tile": 12, "ku3b4": 13, "resid_df": 14}[args.probe]
         if which in (8, 9):
             p.simp_step()  # the filter and OC probes time the state a SIMP step leaves
         avg, mn = p.bench_kernel(which, reps=args.reps, flush_l2=True)
@@ -732,6 +732,7 @@ def main():
     nodes, nel = lay["nodes"], lay["elements"]
     ku_ms, ku_min = keep_p.bench_kernel(0, reps=20, flush_l2=True)
     res_ms, _ = keep_p.bench_kernel(1, reps=5, flush_l2=True)
+    res_df_ms, _ = keep_p.bench_kernel(14, reps=5, flush_l2=True)
     upd_ms, upd_min = keep_p.bench_kernel(2, reps=20, flush_l2=True)
     keep_p.close()
     peak, peak_kind = measured_peaks()
@@ -824,7 +825,8 @@ def main():
             "compliance_last": results[primary]["compliance"][-1],
             "arms": {a: arm_summary(r, ref) for a, r in results.items()},
             "roofline": roof,
-            "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_fp64": res_ms, "pcg_update_fp32": upd_ms},
+            "kernels_ms": {"ku_pcg_fp32": ku_ms, "ku_resid_double_float": res_df_ms, "ku_resid_fp64": res_ms,
+                           "pcg_update_fp32": upd_ms},
             "roofline_ku": ku_roof, "roofline_update": upd_roof, "roofline_conv": conv_roof,
             "gpu_launches": results[primary]["gpu_launches"],
             "clocks": clk.summary(),

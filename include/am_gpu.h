@@ -286,6 +286,7 @@ long long am_launch_count(void);
  * CTA-wide barrier per plane (4 stages), 1 the FP64
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
  * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
+ * 14 the double-float residual of the mixed solvers (1 is its FP64 form),
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
  * and folded iterate) iteration, 8 the C++ cone sensitivity filter
  * (shared-memory stencil), 9 one OC bisection pass (double-float) -- these two
@@ -382,6 +383,16 @@ am_status am_problem_set_preconditioner(am_problem *p, am_precond *m);
  * results); no reference counterpart (Eigen's CG loop runs on the host,
  * linear_solver.cpp:136-155). */
 am_status am_problem_set_device_loop(am_problem *p, int on);
+
+/* The arithmetic of the residuals r = mask(f - K u) (with the element energies)
+ * that the mixed-precision solvers (AM_PREC_MIXED) recompute at every residual
+ * replacement and accept a solve on.  AM_RESID_DOUBLE_FLOAT (the default): the
+ * element operator and node sums as double-float pairs on the FP32 pipes (~48
+ * significant bits; FP64 inputs, outputs and dot products), several times faster
+ * than FP64 on GB300; AM_RESID_FP64: the FP64 kernel.  AM_PREC_FP64 solves always
+ * use the FP64 kernel.  No reference counterpart (the reference solves in FP64). */
+enum { AM_RESID_DOUBLE_FLOAT = 0, AM_RESID_FP64 = 1 };
+am_status am_problem_set_residual_arithmetic(am_problem *p, int mode);
 
 /* ---- density-predicting U-Net (the reference's am.ai TopOptUNet) -----------------------
  * A 3-D U-Net predicting the optimised density field from a problem encoding: the

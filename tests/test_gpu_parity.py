@@ -378,3 +378,34 @@ def test_device_loop_matches_host_loop(precision):
     assert c1 and c0 and i1 == i0 and i1 > 0
     assert np.array_equal(u1, u0)
     assert np.array_equal(r1["compliance"], r0["compliance"]) and np.array_equal(r1["density"], r0["density"])
+
+
+def test_double_float_residual_matches_fp64_residual():
+    """The mixed solvers' residuals in double-float (default) and in FP64: the same
+    solves to rel-res 1e-10 agree to 1e-9 in displacement, 4-step SIMP compliance
+    histories to 1e-9 and densities to 1e-6; both solves are accepted on their own
+    residual."""
+    shape = (33, 9, 10)
+    nx, ny, nz = shape
+    base = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    fixed = (3 * base[:, None] + np.arange(3)).ravel()
+    F = np.zeros(3 * (nx + 1) * (ny + 1) * (nz + 1))
+    F[-1] = -1.0
+    rho = np.random.default_rng(6).uniform(0.02, 1.0, size=shape)
+    out = []
+    for mode in (nat.RESID_DOUBLE_FLOAT, nat.RESID_FP64):
+        p = nat.Problem(shape)
+        p.set_loads([F], [fixed])
+        p.set_residual_arithmetic(mode)
+        u, st = p.solve(nat.default_config(nat.VARIANT_CPP, cg_tol=1e-10, warm_start=0), rho)
+        assert st.converged and st.residual <= 1e-10
+        r = p.simp_run(nat.default_config(nat.VARIANT_CPP, max_iterations=4, convergence_tol=0.0, cg_tol=1e-9),
+                       np.full(shape, 0.3))
+        out.append((u, r))
+        p.close()
+    (u_df, r_df), (u_64, r_64) = out
+    assert np.linalg.norm(u_df - u_64) <= 1e-9 * np.linalg.norm(u_64)
+    assert np.allclose(r_df["compliance"], r_64["compliance"], rtol=1e-9, atol=0)
+    assert np.abs(r_df["density"] - r_64["density"]).max() <= 1e-6
+    with pytest.raises(nat.AmError):
+        nat.Problem(shape).set_residual_arithmetic(7)
