@@ -1745,13 +1745,12 @@ cudaError_t batch_prepare_solve(const BatchItem *it, WorkList vec, WorkList prob
 }
 
 __global__ void __launch_bounds__(KuShape<32, 4>::NT) b_resid_kernel(const BatchItem *items, WorkList W,
-                                                                     Modal<double> M, int energy) {
+                                                                     Modal<dflt> Mdf, int energy) {
     AMK_BATCH_LOOP(W) {
         const BatchItem &it = items[_k.x];
         if (it.S->frozen) continue;
         KuArgs<double> a{};
         a.L = it.L;
-        a.M = M;
         a.s = it.s64;
         a.u = it.x64;
         a.f = it.F;
@@ -1766,15 +1765,17 @@ __global__ void __launch_bounds__(KuShape<32, 4>::NT) b_resid_kernel(const Batch
         a.tiles_y = it.k64_tiles_y;
         a.tiles_z = it.k64_tiles_z;
         a.tz = it.k64_tz;
-        ku_tile_body<double, 32, 4, KU_RESID>(a, Blk{_k.y, it.n_k64});
+        ku_resid_df_body<32, 4>(a, Mdf, Blk{_k.y, it.n_k64});
         __syncthreads();
     }
 }
+// the batch's residuals (FP64 defect correction) in double-float, as the
+// single-problem mixed solver's (kudf.cuh)
 cudaError_t batch_resid(const BatchItem *it, WorkList k64, const BatchConst &C, int energy, int grid,
                         cudaStream_t st) {
     using Sh = KuShape<32, 4>;
     const size_t smem = Sh::template smem_bytes<double>();
-    b_resid_kernel<<<std::max(1, std::min(grid, k64.n)), Sh::NT, smem, st>>>(it, k64, C.M64, energy);
+    b_resid_kernel<<<std::max(1, std::min(grid, k64.n)), Sh::NT, smem, st>>>(it, k64, modal_dflt(C.M64), energy);
     return counted(cudaGetLastError());
 }
 
