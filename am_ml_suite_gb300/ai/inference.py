@@ -36,11 +36,30 @@ def element_loads(domain: VoxelDomain, load_cases: List[LoadCase]) -> np.ndarray
     return np.moveaxis(e, -1, 0)
 
 
+def element_constraints(domain: VoxelDomain, load_cases: List[LoadCase]) -> np.ndarray:
+    """(3, nx, ny, nz): per element and component, the fraction of its 8 nodes
+    whose DOF of that component is constrained in some load case."""
+    nx, ny, nz = domain.shape
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    fixed = np.zeros(3 * nn)
+    for lc in load_cases:
+        idx = np.asarray(lc.get_constrained_dofs(), dtype=np.int64)
+        fixed[idx[(idx >= 0) & (idx < 3 * nn)]] = 1.0
+    f = fixed.reshape(nx + 1, ny + 1, nz + 1, 3)
+    e = np.zeros((nx, ny, nz, 3))
+    for di in (0, 1):
+        for dj in (0, 1):
+            for dk in (0, 1):
+                e += f[di:di + nx, dj:dj + ny, dk:dk + nz]
+    return np.moveaxis(e / 8.0, -1, 0)
+
+
 class AIOptimizer:
     """Density prediction by a trained TopOptUNet (inference.py:18-113).
 
     The encoding: channel 0 the domain (-1 void, 0 design, 1 fixed), channels 1-3
-    the loads on the elements (element_loads).  A model predicts designs for the
+    the loads on the elements (element_loads), channels 4-6 of a 7-channel model
+    the constrained DOFs (element_constraints).  A model predicts designs for the
     SIMP parameters it was trained with (volume fraction, filter radius, penalty:
     stored in the checkpoint)."""
 
@@ -55,10 +74,21 @@ class AIOptimizer:
     def load_model(self, model_path: Union[str, Path]) -> None:
         self.model = load_pretrained(str(model_path))
 
-    def encode_problem(self, domain: VoxelDomain, load_cases: List[LoadCase]) -> np.ndarray:
-        """Input tensor (4, nx, ny, nz)."""
+    def encode_problem(self, domain: VoxelDomain, load_cases: List[LoadCase],
+                       channels: Optional[int] = None) -> np.ndarray:
+        """Input tensor (C, nx, ny, nz), the layout inference.py:61-79 of the
+        reference sets out: channel 0 the domain, channels 1-3 the loads and, for a
+        7-channel model, channels 4-6 the constrained DOFs (element_constraints).
+        C is the loaded model's in_channels (4 without a model) unless given."""
+        if channels is None:
+            channels = self.model.in_channels if self.model is not None else 4
+        if channels not in (4, 7):
+            raise ValueError("the encoding has 4 or 7 channels")
         g = np.asarray(domain.grid, dtype=np.float32)
-        return np.concatenate([g[None], element_loads(domain, load_cases).astype(np.float32)], axis=0)
+        parts = [g[None], element_loads(domain, load_cases).astype(np.float32)]
+        if channels == 7:
+            parts.append(element_constraints(domain, load_cases).astype(np.float32))
+        return np.concatenate(parts, axis=0)
 
     def predict(self, domain: VoxelDomain, load_cases: List[LoadCase],
                 threshold: Optional[float] = 0.5) -> np.ndarray:

@@ -1,6 +1,6 @@
 """Training set and training of the density-predicting U-Net.
 
-    python -m am_ml_suite_gb300.ai.train out.npz [n_train] [f0] [epochs]
+    python -m am_ml_suite_gb300.ai.train out.npz [n_train] [f0] [epochs] [channels: 4 or 7]
 
 The samples are BRK-A-01 brackets at 5 mm (24 x 12 x 16 elements, the resolution of
 the reference's recorded run data/brk_a_01) with the eyelet load of static case 1
@@ -38,7 +38,7 @@ def random_case(domain_shape, rng) -> LoadCase:
     return lc
 
 
-def make_samples(n: int, seed: int, verbose=False):
+def make_samples(n: int, seed: int, verbose=False, channels=4):
     from ..numerical.fem import MaterialProperties
     from ..numerical.topopt import SIMPOptimizer, SIMPParams
 
@@ -52,7 +52,7 @@ def make_samples(n: int, seed: int, verbose=False):
     for i in range(n):
         lc = random_case(dom.shape, rng)
         res = SIMPOptimizer(dom, [lc], MaterialProperties(E=1.0, nu=0.3), prm, verbose=False).run()
-        X.append(enc.encode_problem(dom, [lc]))
+        X.append(enc.encode_problem(dom, [lc], channels=channels))
         T.append(res.density)
         cases.append(lc)
         if verbose and (i + 1) % 16 == 0:
@@ -73,10 +73,10 @@ def padded(dom, X, T):
     return x, t, m
 
 
-def train(n_train=160, n_test=16, f0=32, epochs=60, batch=8, lr=1e-3, seed=0, verbose=False):
-    dom, X, T, cases = make_samples(n_train + n_test, seed, verbose)
+def train(n_train=160, n_test=16, f0=32, epochs=60, batch=8, lr=1e-3, seed=0, verbose=False, channels=4):
+    dom, X, T, cases = make_samples(n_train + n_test, seed, verbose, channels)
     x, t, m = padded(dom, X[:n_train], T[:n_train])
-    model = TopOptUNet(4, 1, (f0, 2 * f0, 4 * f0, 8 * f0), seed=seed)
+    model = TopOptUNet(channels, 1, (f0, 2 * f0, 4 * f0, 8 * f0), seed=seed)
     model.net.set_data(x, t, m)
     t0 = time.time()
     losses = model.net.train(epochs=epochs, batch=batch, lr=lr, seed=seed, verbose=int(verbose))
@@ -88,7 +88,8 @@ def train(n_train=160, n_test=16, f0=32, epochs=60, batch=8, lr=1e-3, seed=0, ve
     held = []
     for i in range(n_train, n_train + n_test):
         held.append(ai.validate_against_numerical(dom, [cases[i]], numerical_density=T[i]))
-    summary = {"n_train": n_train, "n_test": n_test, "f0": f0, "epochs": epochs, "train_s": train_s,
+    summary = {"n_train": n_train, "n_test": n_test, "f0": f0, "channels": channels, "epochs": epochs,
+               "train_s": train_s,
                "mse_first": float(losses[0]), "mse_last": float(losses[-1]),
                "held_out_iou_mean": float(np.mean([h["iou"] for h in held])),
                "held_out_compliance_error_mean": float(np.mean([h["compliance_error"] for h in held])),
@@ -102,6 +103,7 @@ if __name__ == "__main__":
     n = int(sys.argv[2]) if len(sys.argv) > 2 else 160
     f0 = int(sys.argv[3]) if len(sys.argv) > 3 else 32
     ep = int(sys.argv[4]) if len(sys.argv) > 4 else 60
-    model, summary, held = train(n_train=n, f0=f0, epochs=ep, verbose=True)
+    ch = int(sys.argv[5]) if len(sys.argv) > 5 else 4
+    model, summary, held = train(n_train=n, f0=f0, epochs=ep, verbose=True, channels=ch)
     model.save(out)
     print(json.dumps(summary))

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from am_ml_suite_gb300 import _native as nat
-from am_ml_suite_gb300.core import BoundaryCondition, DistributedLoad, LoadCase, PointLoad, VoxelDomain
+from am_ml_suite_gb300.core import DOF, BoundaryCondition, DistributedLoad, LoadCase, PointLoad, VoxelDomain
 
 
 def _spec(f0):
@@ -77,6 +77,15 @@ def test_encoding_and_arguments():
     assert e[2, nx - 1, 0, 0] == -1.0 and np.count_nonzero(e) == 1  # one corner node: 1/8 of it, rescaled
     x = AIOptimizer(device="cuda").encode_problem(dom, [lc])
     assert x.shape == (4, nx, ny, nz) and np.array_equal(x[0], grid.astype(np.float32))
+    # 7 channels: the constrained DOFs of the x = 0 face (component z only) on the elements
+    fixed_nodes = np.array([j * (nz + 1) + k for j in range(ny + 1) for k in range(nz + 1)])
+    lc.boundary_conditions = [BoundaryCondition(node_indices=fixed_nodes, constrained_dofs=[DOF.UZ])]
+    x7 = AIOptimizer().encode_problem(dom, [lc], channels=7)
+    assert x7.shape == (7, nx, ny, nz) and np.array_equal(x7[:4], x)
+    assert np.all(x7[4] == 0) and np.all(x7[5] == 0)
+    assert np.all(x7[6][0] == 0.5) and np.all(x7[6][1:] == 0)  # half of an x = 0 element's nodes
+    with pytest.raises(ValueError):
+        AIOptimizer().encode_problem(dom, [lc], channels=5)
     with pytest.raises(ValueError):
         TopOptUNet(features=(32, 64, 128, 512))
     with pytest.raises(ValueError):
