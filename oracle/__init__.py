@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the SIMP inner loop -- TEST INFRASTRUCTURE ONLY.
 
-This package is the checker of the CUDA path.  Only ``tests/``,
+This package is the oracle the CUDA path is tested against.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the cpu_baseline / reference arm of
 ``bench.py`` may import it; the product package ``am_ml_suite_gb300`` never
 does, and has no CPU fallback.

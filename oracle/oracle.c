@@ -1,8 +1,9 @@
 /*
  * oracle.c -- FP64 CPU restatement of the reference SIMP inner loop.
  *
- * TEST INFRASTRUCTURE ONLY (the checker, never the product): loaded by tests/,
- * __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm.
+ * TEST INFRASTRUCTURE ONLY (the oracle the tests compare against, never the
+ * product): loaded by tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / reference arm.
  * Every function cites the reference file:line whose behaviour it restates;
  * the declarations and the layout convention are in oracle.h.
  */

@@ -1,7 +1,7 @@
 /*
  * oracle.h -- FP64 CPU restatement of the reference SIMP inner loop.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle of the CUDA path's tests:
  * only tests/, __graft_entry__.smoke() and the cpu_baseline / reference arm of
  * bench.py may load it.  The product library (libamgpu.so) never links or
  * calls it, and has no CPU fallback.

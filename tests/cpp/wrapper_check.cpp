@@ -5,7 +5,7 @@
 //                       exception types (runs without a GPU)
 //   wrapper_check gpu   a 24x12x6 cantilever through run() with and without a
 //                       callback and through runIteration(), against the FP64
-//                       CPU oracle (liboracle.so, the tests' checker)
+//                       CPU oracle (liboracle.so)
 #include <cmath>
 #include <cstdio>
 #include <cstring>
