@@ -23,22 +23,35 @@ def _split(w):
     return out
 
 
-def _unet_reference(x, ws, bf16_forward=False):
+def _unet_reference(x, ws, bf16_forward=False, bf16_grads=False):
     """float64 CPU reference: x (n, gz, gy, gx, 4); ws per layer [27][cout][cin].
 
     bf16_forward: round the input, every stored activation (ReLU outputs, pooled
     tensors) and the weights to BF16 where the GPU network stores them, and
     differentiate that forward pass exactly -- the GPU's arithmetic with exact
-    sums and exact gradients."""
+    sums and exact gradients.  bf16_grads: also round the gradient reaching each
+    of those stored tensors to BF16, as the GPU's backward pass stores it."""
     torch = pytest.importorskip("torch")
     F = torch.nn.functional
     W = [torch.tensor(w, dtype=torch.float64, requires_grad=True) for w in ws]
 
+    def rnd(t):
+        return t.to(torch.bfloat16).to(torch.float64)
+
+    class _Round(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, t):
+            return rnd(t)
+
+        @staticmethod
+        def backward(ctx, g):
+            return rnd(g) if bf16_grads else g
+
     def bf(t):
         if not bf16_forward:
             return t
-        # rounded values in the forward pass, the identity for the gradient
-        return t + (t.detach().to(torch.bfloat16).to(torch.float64) - t.detach())
+        # rounded values in the forward pass; the gradient exact or rounded
+        return _Round.apply(t)
 
     def conv(l, t, relu=True):
         cout, cin = W[l].shape[1], t.shape[1]
