@@ -181,6 +181,15 @@ public:
         return *this;
     }
 
+    /* Engine knobs with no reference counterpart: who drives an inner solve's loop
+     * (am_problem_set_device_loop) and the arithmetic of the mixed solvers'
+     * residuals (am_problem_set_residual_arithmetic: AM_RESID_DOUBLE_FLOAT or
+     * AM_RESID_FP64). */
+    void setDeviceLoop(bool on) { detail::check(am_problem_set_device_loop(p_, on ? 1 : 0), "setDeviceLoop"); }
+    void setResidualArithmetic(int mode) {
+        detail::check(am_problem_set_residual_arithmetic(p_, mode), "setResidualArithmetic");
+    }
+
     /* One iteration (runIteration, topology_optimizer.cpp:294-384) on `density`,
      * which is updated in place.  The first call starts the loop on the device
      * (design mask from this density, as run() does); later calls continue it

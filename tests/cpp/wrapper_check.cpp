@@ -157,6 +157,14 @@ static int gpu_checks() {
     d.compliance_history = hist;
     d.final_density = rho;
     compare(d, "runIteration");
+    // the engine knobs: host-driven loop and FP64 residuals give the oracle's answers too
+    opt.setDeviceLoop(false);
+    opt.setResidualArithmetic(AM_RESID_FP64);
+    compare(opt.run(std::vector<double>((size_t)nel, 0.3), F, fixed), "run (host loop, FP64 residuals)");
+    opt.setDeviceLoop(true);
+    opt.setResidualArithmetic(AM_RESID_DOUBLE_FLOAT);
+    EXPECT(throws<std::invalid_argument>([&] { opt.setResidualArithmetic(9); }),
+           "an unknown residual mode is std::invalid_argument");
     // solve(): reference tolerance semantics
     auto sol = opt.solve(std::vector<double>((size_t)nel, 0.5), F, fixed);
     EXPECT(sol.second.converged && sol.second.residual <= 1e-10, "solve converged");
