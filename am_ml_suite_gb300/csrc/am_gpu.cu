@@ -754,6 +754,9 @@ am_status solve_case(am_problem *P, const am_simp_config &c, int lc, bool want_c
             if (mg_on && mg_f32)  // the V-cycle is FP32: its outer product need not be FP64 either
                 CK(ku_dot_f32(P->plan32, P->L, P->M32, P->s32.p, P->p64a.p, P->mask.p, P->x32.p, P->q32v.p,
                               P->q64v.p, P->partial.p, P->S, P->nblocks_vec, P->st));
+            else if (P->resid_df && !fp64)  // the FP64-accurate outer product in double-float
+                CK(ku_dot_df(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p,
+                             P->S, P->st));
             else
                 CK(ku_dot(P->plan64, P->L, P->M64, P->s64.p, P->p64a.p, P->mask.p, P->q64v.p, P->partial.p, P->S,
                           P->st));

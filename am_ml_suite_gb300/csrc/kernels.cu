@@ -95,7 +95,10 @@ cudaError_t ku_init_attributes() {
     AMK_ATTR(double, 32, 4, KU_DOT)
     AMK_ATTR(double, 32, 8, KU_DOT)
 #undef AMK_ATTR
-    if ((e = cudaFuncSetAttribute(ku_resid_df_kernel<32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(ku_df_kernel<32, 4, KU_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)KuShape<32, 4>::smem_bytes<double>())) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(ku_df_kernel<32, 4, KU_DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)KuShape<32, 4>::smem_bytes<double>())) != cudaSuccess)
         return e;
     if ((e = update_init_attributes()) != cudaSuccess) return e;
@@ -254,7 +257,27 @@ cudaError_t ku_resid_df(const KuLaunch &K, const Layout &L, const Modal<double> 
     a.tiles_z = K.tiles_z;
     a.tz = K.tz;
     using Sh = KuShape<32, 4>;
-    ku_resid_df_kernel<32, 4><<<K.ntiles(), Sh::NT, Sh::smem_bytes<double>(), st>>>(a, modal_dflt(M));
+    ku_df_kernel<32, 4, KU_RESID><<<K.ntiles(), Sh::NT, Sh::smem_bytes<double>(), st>>>(a, modal_dflt(M));
+    return counted(cudaGetLastError());
+}
+
+cudaError_t ku_dot_df(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
+                      const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st) {
+    if (!(K.tx == 32 && K.ty == 4) || K.warps > 0) return cudaErrorInvalidValue;
+    KuArgs<double> a{};
+    a.L = L;
+    a.s = s;
+    a.u = p;
+    a.mask = mask;
+    a.y = q;
+    a.partial = partial;
+    a.S = S;
+    a.tiles_x = K.tiles_x;
+    a.tiles_y = K.tiles_y;
+    a.tiles_z = K.tiles_z;
+    a.tz = K.tz;
+    using Sh = KuShape<32, 4>;
+    ku_df_kernel<32, 4, KU_DOT><<<K.ntiles(), Sh::NT, Sh::smem_bytes<double>(), st>>>(a, modal_dflt(M));
     return counted(cudaGetLastError());
 }
 
@@ -1765,7 +1788,7 @@ __global__ void __launch_bounds__(KuShape<32, 4>::NT) b_resid_kernel(const Batch
         a.tiles_y = it.k64_tiles_y;
         a.tiles_z = it.k64_tiles_z;
         a.tz = it.k64_tz;
-        ku_resid_df_body<32, 4>(a, Mdf, Blk{_k.y, it.n_k64});
+        ku_df_body<32, 4, KU_RESID>(a, Mdf, Blk{_k.y, it.n_k64});
         __syncthreads();
     }
 }

@@ -86,6 +86,9 @@ cudaError_t ku_resid(const KuLaunch &K, const Layout &L, const Modal<double> &M,
 cudaError_t ku_resid_df(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s,
                         const double *x, const double *f, const double *dinv, const uint8_t *mask, double *r,
                         double *ce, double *partial, Scalars *S, cudaStream_t st);
+// ku_dot (q = mask(K p), p.q -> the outer flexible CG's alpha) in double-float
+cudaError_t ku_dot_df(const KuLaunch &K, const Layout &L, const Modal<double> &M, const double *s, const double *p,
+                      const uint8_t *mask, double *q, double *partial, Scalars *S, cudaStream_t st);
 
 // ---- PCG vector kernels ------------------------------------------------------
 // FP64 PCG: x += alpha p; r -= alpha q (p = the pair member written this

@@ -1,5 +1,6 @@
-// kudf.cuh -- the FP64-accurate residual r = mask(f - K u) of the mixed-precision
-// solver in double-float arithmetic on the FP32 pipes.
+// kudf.cuh -- the FP64-accurate residual r = mask(f - K u) and outer product
+// q = mask(K p) of the mixed-precision solvers in double-float arithmetic on the
+// FP32 pipes.
 //
 // GB300 issues FP64 at a small fraction of its FP32 rate, and the residual
 // replacements of the mixed solver (one FP64 K*u every time the FP32 recursion
@@ -102,11 +103,13 @@ inline Modal<dflt> modal_dflt(const Modal<double> &M) {
     return Modal<dflt>{to_dflt(M.lam), to_dflt(M.mu), to_dflt(M.c1), to_dflt(M.c2), to_dflt(M.c3), to_dflt(M.c7)};
 }
 
-// The ku_tile_body RESID pass with the element operator and the node gather in
-// double-float: staged planes and element corner sums hold dflt (8 bytes, the
-// shared-memory layout of the FP64 kernel); u, f, s, dinv, r and ce are FP64.
-template <int TX, int TY>
-__device__ __forceinline__ void ku_resid_df_body(const KuArgs<double> &A, const Modal<dflt> &M, const Blk B) {
+// The ku_tile_body RESID and DOT passes with the element operator and the node
+// gather in double-float: staged planes and element corner sums hold dflt (8
+// bytes, the shared-memory layout of the FP64 kernel); u, f, s, dinv, the output
+// (r = mask(f - K u), or q = mask(K u) for DOT) and ce are FP64.
+template <int TX, int TY, int MODE = KU_RESID>
+__device__ __forceinline__ void ku_df_body(const KuArgs<double> &A, const Modal<dflt> &M, const Blk B) {
+    static_assert(MODE == KU_RESID || MODE == KU_DOT, "double-float K*u: residual or outer product");
     using Sh = KuShape<TX, TY>;
     constexpr int EX = Sh::EX, NE = Sh::NE, SX = Sh::SX, NS = Sh::NS, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -160,7 +163,7 @@ __device__ __forceinline__ void ku_resid_df_body(const KuArgs<double> &A, const 
                 se = A.s[e];
             }
             dflt yo[3][8];
-            const bool want_en = A.energy && e >= 0 && exl >= 1 && eyl >= 1 && ez >= z0;
+            const bool want_en = MODE == KU_RESID && A.energy && e >= 0 && exl >= 1 && eyl >= 1 && ez >= z0;
             if (se != 0.0 || want_en) {
                 const dflt *ub = us + (ez & 1) * 3 * NS;
                 const dflt *ut = us + ((ez + 1) & 1) * 3 * NS;
@@ -212,14 +215,24 @@ __device__ __forceinline__ void ku_resid_df_body(const KuArgs<double> &A, const 
             if (ez >= z0 && ix <= L.nx && iy <= L.ny) {
                 const long long n = node_index(L, ix, iy, ez);
                 const unsigned m = A.mask[n];
-                const double dv = A.dinv ? A.dinv[n] : 0.0;
+                if (MODE == KU_RESID) {
+                    const double dv = A.dinv ? A.dinv[n] : 0.0;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    // f - (hi + lo): the two FP64 subtractions keep the product's ~48 bits
-                    const double rr = ((m >> c) & 1u) ? 0.0 : (A.f[n + c * cs] - (double)val[c].hi) - (double)val[c].lo;
-                    A.y[n + c * cs] = rr;
-                    d0.add_prod(rr, rr);
-                    d1.add_prod(rr, dv * rr);
+                    for (int c = 0; c < 3; ++c) {
+                        // f - (hi + lo): the two FP64 subtractions keep the product's ~48 bits
+                        const double rr =
+                            ((m >> c) & 1u) ? 0.0 : (A.f[n + c * cs] - (double)val[c].hi) - (double)val[c].lo;
+                        A.y[n + c * cs] = rr;
+                        d0.add_prod(rr, rr);
+                        d1.add_prod(rr, dv * rr);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const double q = ((m >> c) & 1u) ? 0.0 : from_dflt(val[c]);
+                        A.y[n + c * cs] = q;
+                        d0.add_prod(A.u[n + c * cs], q);
+                    }
                 }
             }
         }
@@ -235,15 +248,27 @@ __device__ __forceinline__ void ku_resid_df_body(const KuArgs<double> &A, const 
     double tot[2];
     reduce_partials<2>(A.partial, B.n, 2, tot, red);
     if (tid == 0) {
-        A.S->res_rr = tot[0];
-        A.S->res_rz = tot[1];
-        A.S->cnt_ku = 0;
+        Scalars *S = A.S;
+        if (MODE == KU_DOT) {
+            const double pq = tot[0];
+            S->o_pq = pq;
+            if (!(pq > 0.0) || !isfinite(pq)) {
+                S->o_status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+                S->o_alpha = 0.0;
+            } else {
+                S->o_alpha = S->o_zr / pq;
+            }
+        } else {
+            S->res_rr = tot[0];
+            S->res_rz = tot[1];
+        }
+        S->cnt_ku = 0;
     }
 }
 
-template <int TX, int TY>
-__global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_resid_df_kernel(KuArgs<double> A, Modal<dflt> M) {
-    ku_resid_df_body<TX, TY>(A, M, grid_blk());
+template <int TX, int TY, int MODE>
+__global__ void __launch_bounds__(KuShape<TX, TY>::NT) ku_df_kernel(KuArgs<double> A, Modal<dflt> M) {
+    ku_df_body<TX, TY, MODE>(A, M, grid_blk());
 }
 
 }  // namespace amk
