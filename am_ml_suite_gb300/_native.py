@@ -206,6 +206,7 @@ SIGNATURES = {
     "am_problem_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_problem_set_residual_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_batch_set_plan": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
     "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.POINTER(_vp)]),
@@ -705,6 +706,10 @@ class Batch:
 
     def set_device_loop(self, on=True):
         check(load().am_batch_set_device_loop(self.handle, int(bool(on))), "am_batch_set_device_loop")
+
+    def set_plan(self, warps, z_chunk=0, ctas_per_sm=2):
+        """Pins the batched K*u plan: warps 0 (per problem), 4 or 8."""
+        check(load().am_batch_set_plan(self.handle, int(warps), int(z_chunk), int(ctas_per_sm)), "am_batch_set_plan")
 
     def simp_begin(self, cfgs, rho0_list=None):
         if len(cfgs) != self.n:

@@ -101,9 +101,10 @@ struct am_batch {
     Pool<BatchItem> items_d;
     std::vector<BatchItem> items;
     // work lists
-    Pool<int2> w_elem, w_vec, w_k2, w_k64, w_prob, w_chunk;
-    WorkList elem{}, vec{}, k2{}, k64{}, prob{}, chunk{};
-    // FP32 K*u plan (autotuner): warps per CTA, z chunk (0 = all planes), CTAs per SM
+    Pool<int2> w_elem, w_vec, w_k2, w_k2b, w_k64, w_prob, w_chunk;
+    WorkList elem{}, vec{}, k2{}, k2b{}, k64{}, prob{}, chunk{};
+    // FP32 K*u plan (autotuner): warps per CTA (0: each problem's own, 4 or 8), z chunk
+    // (0 = all planes), CTAs per SM
     int warps = 8, zchunk = 0, ctas = 2;
     bool loads_set = false;
     cudaGraphExec_t graph = nullptr;  // one chunk of batched PCG iterations
@@ -132,31 +133,55 @@ am_status upload_worklist(am_batch *B, Pool<int2> &pool, WorkList &wl, const std
 }
 
 // FP32 K*u tiles of every problem for the plan (warps, zchunk); work items in
-// descending tile height so the persistent grid ends with the short ones.
+// descending tile height so the persistent grid ends with the short ones.  warps 0:
+// per problem the tile height (4 or 8 warps: 7 or 15 node rows) that computes
+// fewer element slots on its grid; the 8-warp problems' tiles go to list k2, the
+// 4-warp ones' to k2b.
 am_status plan_k2(am_batch *B, int warps, int zchunk) {
     struct T {
         int p, b, h;
     };
-    std::vector<T> t;
+    std::vector<T> t8, t4;
     for (int p = 0; p < B->n; ++p) {
         const Layout &L = B->L[p];
         BatchItem &it = B->items[p];
-        it.k2_tiles_x = div_up_i(L.nx + 1, 30);
-        it.k2_tiles_y = div_up_i(L.ny + 1, 2 * warps - 1);
         const int planes = L.nz + 1;
-        it.k2_tz = zchunk > 0 ? std::min(zchunk, planes) : planes;
-        it.k2_tiles_z = div_up_i(planes, it.k2_tz);
+        const int tz = zchunk > 0 ? std::min(zchunk, planes) : planes;
+        const int tiles_z = div_up_i(planes, tz);
+        int w = warps;
+        if (w == 0) {
+            // element slots: 32 lanes x 2w rows per tile and plane, a halo plane per z chunk
+            auto slots = [&](int ww) {
+                return (long long)div_up_i(L.nx + 1, 30) * div_up_i(L.ny + 1, 2 * ww - 1) * 64 * ww *
+                       (planes + tiles_z);
+            };
+            w = slots(4) < slots(8) ? 4 : 8;
+        }
+        it.k2_tiles_x = div_up_i(L.nx + 1, 30);
+        it.k2_tiles_y = div_up_i(L.ny + 1, 2 * w - 1);
+        it.k2_tz = tz;
+        it.k2_tiles_z = tiles_z;
         it.n_k2 = it.k2_tiles_x * it.k2_tiles_y * it.k2_tiles_z;
+        auto &tl = (warps == 0 && w == 4) ? t4 : t8;
         for (int b = 0; b < it.n_k2; ++b) {
             const int tzi = b / (it.k2_tiles_x * it.k2_tiles_y);
             const int h = std::min(it.k2_tz, planes - tzi * it.k2_tz);
-            t.push_back(T{p, b, h});
+            tl.push_back(T{p, b, h});
         }
     }
-    std::stable_sort(t.begin(), t.end(), [](const T &a, const T &b) { return a.h > b.h; });
-    std::vector<int2> w(t.size());
-    for (size_t i = 0; i < t.size(); ++i) w[i] = make_int2(t[i].p, t[i].b);
-    BCKS(upload_worklist(B, B->w_k2, B->k2, w));
+    auto upload = [&](std::vector<T> &t, Pool<int2> &pool, WorkList &wl) -> am_status {
+        std::stable_sort(t.begin(), t.end(), [](const T &a, const T &b) { return a.h > b.h; });
+        std::vector<int2> w(t.size());
+        for (size_t i = 0; i < t.size(); ++i) w[i] = make_int2(t[i].p, t[i].b);
+        if (w.empty()) {
+            wl.w = nullptr;
+            wl.n = 0;
+            return AM_OK;
+        }
+        return upload_worklist(B, pool, wl, w);
+    };
+    BCKS(upload(t8, B->w_k2, B->k2));
+    BCKS(upload(t4, B->w_k2b, B->k2b));
     BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
     B->warps = warps;
     B->zchunk = zchunk;
@@ -232,7 +257,7 @@ am_status build_loop_graph(am_batch *B) {
     e = cudaStreamBeginCaptureToGraph(B->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return bail(e, "batch loop body capture");
     for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
-        e = batch_pcg_iteration(B->items_d.p, B->k2, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
+        e = batch_pcg_iteration(B->items_d.p, B->k2, B->k2b, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
     if (e == cudaSuccess) {
         batch_loop_next_kernel<<<1, 256, 0, B->st>>>(h, B->S.p, B->n, B->loopc.p);
         e = cudaGetLastError();
@@ -260,7 +285,7 @@ am_status build_graph(am_batch *B) {
     BCK(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
-        e = batch_pcg_iteration(B->items_d.p, B->k2, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
+        e = batch_pcg_iteration(B->items_d.p, B->k2, B->k2b, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
     cudaError_t e2 = cudaStreamEndCapture(B->st, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -345,7 +370,7 @@ am_status am_batch_destroy(am_batch *B) {
         q->release();
     for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32, &B->xh, &B->xl}) q->release();
     for (auto *q : {&B->design, &B->mask, &B->fixed_bits}) q->release();
-    for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k64, &B->w_prob, &B->w_chunk}) q->release();
+    for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k2b, &B->w_k64, &B->w_prob, &B->w_chunk}) q->release();
     B->f_idx.release();
     B->tap_d.release();
     B->S.release();
@@ -557,13 +582,24 @@ am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed,
     return AM_OK;
 }
 
+am_status am_batch_set_plan(am_batch *B, int warps, int z_chunk, int ctas_per_sm) {
+    BCKS(check_batch(B));
+    if (!(warps == 0 || warps == 4 || warps == 8) || z_chunk < 0 || ctas_per_sm < 1 || ctas_per_sm > 4)
+        return bfail(AM_ERR_INVALID_ARG, "plan: warps 0, 4 or 8; z_chunk >= 0; 1-4 CTAs per SM");
+    BCKS(plan_k2(B, warps, z_chunk));
+    B->ctas = ctas_per_sm;
+    return AM_OK;
+}
+
 am_status am_batch_autotune(am_batch *B, int reps, int *warps, int *z_chunk, int *ctas_per_sm, double *best_ms) {
     BCKS(check_batch(B));
     if (reps < 1) return bfail(AM_ERR_INVALID_ARG, "reps must be >= 1");
     struct Cand {
         int w, z, c;
     };
-    const Cand cands[] = {{8, 0, 2}, {8, 16, 2}, {8, 8, 2}, {8, 0, 1}, {4, 0, 4}, {4, 16, 4}, {4, 8, 4}, {4, 0, 2}};
+    // w = 0: each problem's own tile height (4 or 8 warps)
+    const Cand cands[] = {{8, 0, 2}, {8, 16, 2}, {8, 8, 2}, {8, 0, 1}, {4, 0, 4}, {4, 16, 4},
+                          {4, 8, 4}, {4, 0, 2}, {0, 0, 2}, {0, 16, 2}, {0, 8, 2}};
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
@@ -571,9 +607,9 @@ am_status am_batch_autotune(am_batch *B, int reps, int *warps, int *z_chunk, int
     Cand bc = cands[0];
     for (const Cand &c : cands) {
         BCKS(plan_k2(B, c.w, c.z));
-        BCK(batch_ku_plain(B->items_d.p, B->k2, B->C, c.w, kSms * c.c, B->st));  // warm-up
+        BCK(batch_ku_plain(B->items_d.p, B->k2, B->k2b, B->C, c.w, kSms * c.c, B->st));  // warm-up
         BCK(cudaEventRecord(e0, B->st));
-        for (int r = 0; r < reps; ++r) BCK(batch_ku_plain(B->items_d.p, B->k2, B->C, c.w, kSms * c.c, B->st));
+        for (int r = 0; r < reps; ++r) BCK(batch_ku_plain(B->items_d.p, B->k2, B->k2b, B->C, c.w, kSms * c.c, B->st));
         BCK(cudaEventRecord(e1, B->st));
         BCK(cudaEventSynchronize(e1));
         float ms = 0.f;

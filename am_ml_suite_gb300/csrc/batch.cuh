@@ -76,14 +76,16 @@ cudaError_t batch_resid(const BatchItem *it, WorkList k64, const BatchConst &C, 
 cudaError_t batch_inner_start(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
 // x64 = xh + xl after an FP32 PCG round
 cudaError_t batch_inner_end(const BatchItem *it, WorkList vec, int grid, cudaStream_t st);
-// one FP32 PCG iteration for every active problem: fused K*p (warps = 4 or 8) +
-// the bulk-copy update over `chunks` ((problem, chunk of 2048 DOFs) items)
-cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList chunks, const BatchConst &C, int warps,
-                                int grid_k2, int grid_vec, cudaStream_t st);
+// one FP32 PCG iteration for every active problem: fused K*p + the bulk-copy
+// update over `chunks` ((problem, chunk of 2048 DOFs) items).  warps = 4 or 8: one
+// tile height for every problem, tiles in k2; warps = 0: each problem's own, the
+// 8-warp problems' tiles in k2 and the 4-warp ones' in k2b
+cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList k2b, WorkList chunks, const BatchConst &C,
+                                int warps, int grid_k2, int grid_vec, cudaStream_t st);
 // DOFs per chunk of the batched update's work items
 constexpr int BATCH_UPD_CHUNK = 2048;
 // plain FP32 K*u (y = q32, u = pa) over the batch, for the autotuner
-cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
+cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
                            cudaStream_t st);
 // sensitivities + u.F, filter, OC bisection (FP64), new density copied into rho
 cudaError_t batch_update(const BatchItem *it, WorkList elem, WorkList prob, int grid, cudaStream_t st);

@@ -2065,23 +2065,36 @@ cudaError_t batch_inner_end(const BatchItem *it, WorkList vec, int grid, cudaStr
     return counted(cudaGetLastError());
 }
 static_assert(BATCH_UPD_CHUNK == UPD_K, "batched update chunk");
-cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList vec, const BatchConst &C, int warps,
-                                int grid_k2, int grid_vec, cudaStream_t st) {
-    const int g2 = std::max(1, std::min(grid_k2, k2.n));
-    if (warps == 8) b_ku2_kernel<8, KU_PCG><<<g2, 256, 0, st>>>(it, k2, C.M32);
-    else if (warps == 4) b_ku2_kernel<4, KU_PCG><<<g2, 128, 0, st>>>(it, k2, C.M32);
-    else return cudaErrorInvalidValue;
-    if (cudaError_t e = counted(cudaGetLastError())) return e;
+// The batched FP32 K*u of one plan: warps 8 or 4 for every problem (list k2), or
+// 0 -- each problem's own tile height, list k2 holding the 8-warp problems' tiles
+// and k2b the 4-warp ones (two launches).
+template <int MODE>
+static cudaError_t batch_ku_launch(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps,
+                                   int grid, cudaStream_t st) {
+    if (warps == 8 || (warps == 0 && k2.n > 0))
+        b_ku2_kernel<8, MODE><<<std::max(1, std::min(grid, k2.n)), 256, 0, st>>>(it, k2, C.M32);
+    else if (warps == 4)
+        b_ku2_kernel<4, MODE><<<std::max(1, std::min(grid, k2.n)), 128, 0, st>>>(it, k2, C.M32);
+    else if (warps != 0)
+        return cudaErrorInvalidValue;
+    if (warps != 0 || k2.n > 0)
+        if (cudaError_t e = counted(cudaGetLastError())) return e;
+    if (warps == 0 && k2b.n > 0) {
+        // a 4-warp CTA holds half the threads: twice the CTAs in the persistent grid
+        b_ku2_kernel<4, MODE><<<std::max(1, std::min(2 * grid, k2b.n)), 128, 0, st>>>(it, k2b, C.M32);
+        if (cudaError_t e = counted(cudaGetLastError())) return e;
+    }
+    return cudaSuccess;
+}
+cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList k2b, WorkList vec, const BatchConst &C,
+                                int warps, int grid_k2, int grid_vec, cudaStream_t st) {
+    if (cudaError_t e = batch_ku_launch<KU_PCG>(it, k2, k2b, C, warps, grid_k2, st)) return e;
     b_update_df_kernel<<<std::max(1, std::min(grid_vec, vec.n)), 256, UPD_SMEM, st>>>(it, vec);
     return counted(cudaGetLastError());
 }
-cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, const BatchConst &C, int warps, int grid,
+cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
                            cudaStream_t st) {
-    const int g2 = std::max(1, std::min(grid, k2.n));
-    if (warps == 8) b_ku2_kernel<8, KU_PLAIN><<<g2, 256, 0, st>>>(it, k2, C.M32);
-    else if (warps == 4) b_ku2_kernel<4, KU_PLAIN><<<g2, 128, 0, st>>>(it, k2, C.M32);
-    else return cudaErrorInvalidValue;
-    return counted(cudaGetLastError());
+    return batch_ku_launch<KU_PLAIN>(it, k2, k2b, C, warps, grid, st);
 }
 
 __global__ void __launch_bounds__(256) b_sens_kernel(const BatchItem *items, WorkList W) {

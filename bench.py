@@ -231,7 +231,10 @@ def run_batch(args, nat, world, rank, emit=True):
                        "autotuned_plan": plan, "l2": "working set per step > 129 MB L2",
                        "parallelism": f"problems sharded over {world} ranks (LPT by cost)" if world > 1 else "1 GPU"},
             "pcg_iterations_per_problem_step": float(np.mean(its_per_step)),
-            "roofline": {"bound": "hbm", "kernel": f"b_ku2_kernel<{plan['warps']},KU_PLAIN> (batched FP32 K*u)",
+            "roofline": {"bound": "hbm",
+                         "kernel": ("b_ku2_kernel<8|4,KU_PLAIN> (batched FP32 K*u, tile height per problem)"
+                                    if plan["warps"] == 0 else
+                                    f"b_ku2_kernel<{plan['warps']},KU_PLAIN> (batched FP32 K*u)"),
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": alg, "avg_ms": plan["ms"]},
             "gpu_launches": int(l1 - l0), "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,

@@ -449,10 +449,14 @@ am_status am_batch_destroy(am_batch *b);
 am_status am_batch_set_loads(am_batch *b, const double *F, const int64_t *fixed, const int64_t *n_fixed);
 
 /* Autotuner of the batched FP32 K*u: times `reps` launches of each candidate plan
- * (4 or 8 warps per CTA, z chunks of 8, 16 or all node planes, 1-4 CTAs per SM in
- * the persistent grid) and keeps the fastest for the following runs.  Outputs
- * (nullable) the chosen plan and its time per launch. */
+ * (4 or 8 warps per CTA for every problem, or -- warps 0 -- per problem the tile
+ * height that computes fewer element slots on its grid; z chunks of 8, 16 or all
+ * node planes; 1-4 CTAs per SM in the persistent grid) and keeps the fastest for
+ * the following runs.  Outputs (nullable) the chosen plan and its time per launch. */
 am_status am_batch_autotune(am_batch *b, int reps, int *warps, int *z_chunk, int *ctas_per_sm, double *best_ms);
+/* Pins a plan of the batched FP32 K*u without timing: warps 0 (per problem), 4 or 8;
+ * z_chunk 0 (all planes) or >= 1; ctas_per_sm 1-4. */
+am_status am_batch_set_plan(am_batch *b, int warps, int z_chunk, int ctas_per_sm);
 
 /* The CUDA stream the batch's kernels run on (cudaStream_t). */
 am_status am_batch_stream(am_batch *b, void **stream);
