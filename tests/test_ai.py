@@ -181,3 +181,25 @@ def test_train_predict_validate_and_checkpoint(tmp_path):
     assert again.features == (16, 32, 64, 128) and again.meta["volume_fraction"] == 0.3
     assert np.array_equal(again.predict(enc.encode_problem(dom, [cases[11]])),
                           model.predict(enc.encode_problem(dom, [cases[11]])))
+
+
+@pytest.mark.gpu
+def test_seven_channel_model_predicts_and_round_trips(tmp_path):
+    """The 7-channel encoding (constrained DOFs on channels 4-6) through a
+    TopOptUNet(7, ...): prediction shape and range, checkpoint round trip, and the
+    optimizer encoding for the loaded model's channel count."""
+    from am_ml_suite_gb300.ai import AIOptimizer, TopOptUNet, load_pretrained
+
+    shape = (16, 8, 8)
+    nx, ny, nz = shape
+    dom = VoxelDomain(grid=np.zeros(shape, np.int8), resolution_mm=1000.0)
+    lc = _cantilever_family(np.random.default_rng(5), shape)
+    model = TopOptUNet(7, 1, (16, 32, 64, 128), seed=2)
+    x = AIOptimizer().encode_problem(dom, [lc], channels=7)
+    rho = model.predict(x)
+    assert rho.shape == shape and np.all((rho > 0) & (rho < 1))
+    path = str(tmp_path / "u7.npz")
+    model.save(path)
+    ai = AIOptimizer(model_path=path)
+    assert ai.model.in_channels == 7 and ai.encode_problem(dom, [lc]).shape == (7, nx, ny, nz)
+    assert np.array_equal(ai.model.predict(x), load_pretrained(path).predict(x))
