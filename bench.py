@@ -308,13 +308,18 @@ def measured_bf16_peak():
 
 def ku_traffic_per_launch(W, nodes, elements):
     """DRAM bytes per launch of the fused FP32 PCG K*u from the committed ncu
-    summary (measured on a smaller case, scaled by nodes), or None."""
+    captures: the capture of this workload's grid if there is one, else the
+    largest capture scaled by nodes; None without captures."""
     p = os.path.join(ROOT, "profiles", "ku_pcg_fp32_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        d = json.load(f)
-    return d["dram_bytes_per_launch"] * nodes / d["nodes"]
+        caps = json.load(f)["captures"]
+    for c in caps.values():
+        if c["nodes"] == nodes and c["elements"] == elements:
+            return float(c["dram_bytes_per_launch"])
+    c = max(caps.values(), key=lambda c: c["nodes"])
+    return c["dram_bytes_per_launch"] * nodes / c["nodes"]
 
 
 def cpu_baseline(W, steps_gpu_its, pcg_iters_sample=20):
