@@ -207,6 +207,7 @@ SIGNATURES = {
     "am_problem_set_residual_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_plan": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "am_batch_axes": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
     "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.POINTER(_vp)]),
@@ -706,6 +707,13 @@ class Batch:
 
     def set_device_loop(self, on=True):
         check(load().am_batch_set_device_loop(self.handle, int(bool(on))), "am_batch_set_device_loop")
+
+    def axes(self, i):
+        """The caller's axis (0 = x, 1 = y, 2 = z) that problem i stores as each of its
+        internal axes (the first is the K*u tiles' 30-column axis)."""
+        a = (ctypes.c_int * 3)()
+        check(load().am_batch_axes(self.handle, int(i), a), "am_batch_axes")
+        return tuple(a)
 
     def set_plan(self, warps, z_chunk=0, ctas_per_sm=2):
         """Pins the batched K*u plan: warps 0 (per problem), 4 or 8."""

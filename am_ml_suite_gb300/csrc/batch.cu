@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -78,7 +79,10 @@ struct am_batch {
     int device = 0;
     cudaStream_t st = nullptr;
     int n = 0;
-    std::vector<Layout> L;
+    std::vector<Layout> L;  // internal (axis-permuted) layouts
+    // per problem: the caller's grid dimensions, and the caller's axis that each
+    // internal axis holds (axes[p][a] = physical axis of internal axis a)
+    std::vector<std::array<int, 3>> dims, axes;
     double h = 1, E0 = 1, nu = 0.3;
     BatchConst C{};
     // offsets (in elements of the pool type) per problem
@@ -122,6 +126,50 @@ struct am_batch {
 namespace {
 
 int div_up_i(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// The axis order a problem is stored in.  The cube's element stiffness is the
+// same when the three axes and the displacement components are permuted together
+// (and the cone filter and OC step do not see axes), so each problem may keep its
+// grid in whichever axis order makes the batched K*u's tiles (30 node columns x
+// 15 node rows x all planes plus a halo plane) overhang it least; the caller's
+// order is restored at the boundary (loads, constraints, densities).  Ties keep
+// the caller's order.
+std::array<int, 3> best_axes(const int d[3]) {
+    static const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    long long best = -1;
+    std::array<int, 3> out{0, 1, 2};
+    for (const auto &q : P) {
+        const long long slots = (long long)div_up_i(d[q[0]] + 1, 30) * 32 * div_up_i(d[q[1]] + 1, 15) * 16 *
+                                (d[q[2]] + 2);
+        if (best < 0 || slots < best) {
+            best = slots;
+            out = {q[0], q[1], q[2]};
+        }
+    }
+    return out;
+}
+
+// internal coordinates of the caller's (i, j, k) and the internal component of the
+// caller's component c
+inline void to_internal(const std::array<int, 3> &ax, const long long c3[3], long long q[3]) {
+    for (int a = 0; a < 3; ++a) q[a] = c3[ax[a]];
+}
+// the caller's index of internal element (ex, ey, ez): C order over the caller's
+// (nx, ny, nz) (z fastest) or x fastest, as the layout says
+inline long long host_element(const std::array<int, 3> &ax, const std::array<int, 3> &dm, int layout, long long ex,
+                              long long ey, long long ez) {
+    long long c3[3];
+    c3[ax[0]] = ex;
+    c3[ax[1]] = ey;
+    c3[ax[2]] = ez;
+    return layout == AM_LAYOUT_ZFASTEST ? (c3[0] * dm[1] + c3[1]) * dm[2] + c3[2]
+                                        : (c3[2] * dm[1] + c3[1]) * dm[0] + c3[0];
+}
+inline int internal_component(const std::array<int, 3> &ax, int c) {
+    for (int a = 0; a < 3; ++a)
+        if (ax[a] == c) return a;
+    return c;
+}
 
 am_status upload_worklist(am_batch *B, Pool<int2> &pool, WorkList &wl, const std::vector<int2> &w) {
     BCK(pool.alloc(w.size()));
@@ -391,7 +439,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         if (shapes[3 * p] < 1 || shapes[3 * p + 1] < 1 || shapes[3 * p + 2] < 1)
             return bfail(AM_ERR_INVALID_ARG, "problem " + std::to_string(p) + ": dimensions must be >= 1");
         // the batched warp-row K*u indexes a problem's nodes with 32-bit integers
-        if (3 * make_layout(shapes[3 * p], shapes[3 * p + 1], shapes[3 * p + 2]).cs >= (1LL << 31))
+        const std::array<int, 3> ax = best_axes(shapes + 3 * p);
+        if (3 * make_layout(shapes[3 * p + ax[0]], shapes[3 * p + ax[1]], shapes[3 * p + ax[2]]).cs >= (1LL << 31))
             return bfail(AM_ERR_SIZE_MISMATCH, "problem " + std::to_string(p) + ": too large for a batch");
     }
     int ndev = 0;
@@ -406,6 +455,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     B->C.M32 = modal_float(B->C.M64);
     B->C.d0 = element_stiffness_entry(B->C.M64, 0, 0);
     B->L.resize(n);
+    B->dims.resize(n);
+    B->axes.resize(n);
     B->eoff.resize(n + 1);
     B->noff.resize(n + 1);
     B->poff.resize(n + 1);
@@ -413,7 +464,11 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     B->pcg_its.assign(n, 0);
     size_t e = 0, nn = 0, pp = 0;
     for (int p = 0; p < n; ++p) {
-        const Layout L = make_layout(shapes[3 * p], shapes[3 * p + 1], shapes[3 * p + 2]);
+        const int *d = shapes + 3 * p;
+        B->dims[p] = {d[0], d[1], d[2]};
+        B->axes[p] = best_axes(d);
+        const std::array<int, 3> &ax = B->axes[p];
+        const Layout L = make_layout(d[ax[0]], d[ax[1]], d[ax[2]]);
         B->L[p] = L;
         BatchItem &it = B->items[p];
         it.L = L;
@@ -526,21 +581,30 @@ am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed,
     size_t fo = 0, xo = 0;
     for (int p = 0; p < B->n; ++p) {
         const Layout &L = B->L[p];
+        const std::array<int, 3> &ax = B->axes[p], &dm = B->dims[p];
         const long long nn = (long long)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
         const size_t no = B->noff[p];
+        // the internal node of reference node r = (i*(ny+1) + j)*(nz+1) + k (the
+        // caller's dimensions and axis order)
+        auto node_of = [&](long long r) {
+            long long c3[3], q[3];
+            c3[2] = r % (dm[2] + 1);
+            const long long t = r / (dm[2] + 1);
+            c3[1] = t % (dm[1] + 1);
+            c3[0] = t / (dm[1] + 1);
+            to_internal(ax, c3, q);
+            return node_index(L, (int)q[0], (int)q[1], (int)q[2]);
+        };
         foff[p] = idx.size();
         for (long long r = 0; r < nn; ++r) {
-            // reference node r = (i*(ny+1) + j)*(nz+1) + k
-            const int k = (int)(r % (L.nz + 1));
-            const long long t = r / (L.nz + 1);
-            const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
-            const long long d = node_index(L, i, j, k);
+            const long long d = node_of(r);
             for (int c = 0; c < 3; ++c) {
                 const double v = F[fo + 3 * r + c];
                 if (!std::isfinite(v)) return bfail(AM_ERR_NAN_DETECTED, "non-finite force, problem " + std::to_string(p));
-                Fd[3 * no + (size_t)c * L.cs + d] = v;
+                const int ci = internal_component(ax, c);
+                Fd[3 * no + (size_t)ci * L.cs + d] = v;
                 if (v != 0.0) {
-                    idx.push_back((long long)c * L.cs + d);
+                    idx.push_back((long long)ci * L.cs + d);
                     val.push_back(v);
                 }
             }
@@ -552,12 +616,8 @@ am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed,
             const int64_t dof = fixed[xo + q];
             if (dof < 0 || dof >= 3 * nn)
                 return bfail(AM_ERR_DOF_OUT_OF_RANGE, "fixed DOF out of range, problem " + std::to_string(p));
-            const long long r = dof / 3;
-            const int c = (int)(dof % 3);
-            const int k = (int)(r % (L.nz + 1));
-            const long long t = r / (L.nz + 1);
-            const int j = (int)(t % (L.ny + 1)), i = (int)(t / (L.ny + 1));
-            fb[no + node_index(L, i, j, k)] |= (uint8_t)(1u << c);
+            const int c = internal_component(ax, (int)(dof % 3));
+            fb[no + node_of(dof / 3)] |= (uint8_t)(1u << c);
         }
         fo += 3 * (size_t)nn;
         xo += (size_t)nf;
@@ -579,6 +639,13 @@ am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed,
     }
     BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
     B->loads_set = true;
+    return AM_OK;
+}
+
+am_status am_batch_axes(am_batch *B, int i, int *axes) {
+    BCKS(check_batch(B));
+    if (i < 0 || i >= B->n || !axes) return bfail(AM_ERR_INVALID_ARG, "problem index out of range or null output");
+    for (int a = 0; a < 3; ++a) axes[a] = B->axes[i][a];
     return AM_OK;
 }
 
@@ -682,8 +749,7 @@ am_status am_batch_simp_begin(am_batch *B, const am_simp_config *cfgs, const dou
             for (long long ey = 0; ey < L.ny; ++ey)
                 for (long long ex = 0; ex < L.nx; ++ex) {
                     const long long e = (ez * L.ny + ey) * L.nx + ex;
-                    const long long hidx =
-                        c.layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
+                    const long long hidx = host_element(B->axes[p], B->dims[p], c.layout, ex, ey, ez);
                     const double v = rho0 ? rho0[ho + hidx] : c.volume_fraction;
                     r0[eo + e] = v;
                     // design mask from the initial density (topology_optimizer.cpp:419-428)
@@ -800,8 +866,7 @@ am_status am_batch_get_density(am_batch *B, double *rho_out) {
             for (long long ey = 0; ey < L.ny; ++ey)
                 for (long long ex = 0; ex < L.nx; ++ex) {
                     const long long e = (ez * L.ny + ey) * L.nx + ex;
-                    const long long hidx =
-                        B->cfg[p].layout == AM_LAYOUT_ZFASTEST ? (ex * L.ny + ey) * L.nz + ez : e;
+                    const long long hidx = host_element(B->axes[p], B->dims[p], B->cfg[p].layout, ex, ey, ez);
                     rho_out[o + hidx] = r[eo + e];
                 }
         o += (size_t)L.nel;

@@ -439,9 +439,18 @@ am_status am_unet_eval(am_unet *u, double *mse);
 typedef struct am_batch am_batch;
 
 /* n problems on the current device; problem i has shapes[3i] x shapes[3i+1] x
- * shapes[3i+2] cubic elements of edge h; material (E0, nu) is shared. */
+ * shapes[3i+2] cubic elements of edge h; material (E0, nu) is shared.  Each
+ * problem is stored in the axis order in which the batched K*u's tiles (30 node
+ * columns x 15 node rows) overhang its grid least.  That is exact for cubic
+ * elements, the cone filter and the OC step when the displacement components
+ * are permuted with the axes.  Loads, constraints and densities cross this
+ * boundary in the caller's order (am_batch_axes reports the order chosen). */
 am_status am_batch_create(int n, const int *shapes, double h, double E0, double nu, am_batch **out);
 am_status am_batch_destroy(am_batch *b);
+/* The internal axis order of problem i: axes[a] is the caller's axis (0 = x,
+ * 1 = y, 2 = z) that the batch stores as its axis a (a = 0 is the tiles' 30-column
+ * axis).  No reference counterpart. */
+am_status am_batch_axes(am_batch *b, int i, int *axes);
 
 /* One load case per problem: F concatenates the problems' force vectors
  * (3 (nx+1)(ny+1)(nz+1) entries each, reference DOF order), fixed their

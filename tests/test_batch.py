@@ -182,3 +182,34 @@ def test_batch_per_problem_tile_heights():
         b.set_plan(6)
     with pytest.raises(nat.AmError):
         b.set_plan(8, 0, 7)
+
+
+def test_batch_axis_order_and_layouts():
+    """Each problem is stored in the axis order whose K*u tiles overhang it least:
+    (6, 40, 9) keeps its 40-element axis in the 30-column tile direction and its
+    6-element axis as the marching axis, (9, 5, 7) swaps y and z, (20, 4, 3) keeps
+    the caller's order.  Loads, constraints, non-uniform initial densities (both
+    density layouts) and the results cross the boundary in the caller's order:
+    every problem matches the FP64 oracle of its unpermuted grid."""
+    shapes = [(6, 40, 9), (9, 5, 7), (20, 4, 3)]
+    b, loads = _batch(shapes, seed=5)
+    assert [b.axes(i) for i in range(3)] == [(1, 2, 0), (0, 2, 1), (0, 1, 2)]
+    iters = 4
+    rng = np.random.default_rng(6)
+    rho0 = [rng.uniform(0.2, 0.5, size=s) for s in shapes]
+    layouts = [nat.LAYOUT_ZFASTEST, nat.LAYOUT_XFASTEST, nat.LAYOUT_XFASTEST]
+    cfgs = [_cfg(iters) for _ in shapes]
+    for c, lay in zip(cfgs, layouts):
+        c.layout = lay
+    host = [r.ravel() if lay == nat.LAYOUT_ZFASTEST else r.ravel(order="F") for r, lay in zip(rho0, layouts)]
+    res = b.simp_run(cfgs, host)
+    for shape, (F, fixed), r0, lay, out in zip(shapes, loads, rho0, layouts, res):
+        prm = O.make_params(volume_fraction=0.3, filter_radius=1.5, move_limit=0.2, rho_min=0.01, E_min=1e-9,
+                            convergence_tol=0.0, max_iterations=iters, cg_tol=1e-12, warm_start=1)
+        ref = O.simp_cpp(shape, 1.0, 1.0, 0.3, prm, r0, F, fixed)
+        assert np.allclose(out["compliance"], ref["compliance"], rtol=1e-6, atol=0), shape
+        got = out["density"].reshape(shape) if lay == nat.LAYOUT_ZFASTEST else \
+            out["density"].reshape(shape, order="F")
+        assert np.abs(got - ref["density"].reshape(shape)).max() <= 1e-4, shape
+    with pytest.raises(nat.AmError):
+        b.axes(3)
