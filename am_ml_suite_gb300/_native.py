@@ -208,6 +208,8 @@ SIGNATURES = {
     "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_plan": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "am_batch_axes": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "am_batch_set_staged": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_batch_bench_ku": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "am_precond_set_kernels": (ctypes.c_int, [ctypes.c_int]),
     "am_unet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.POINTER(_vp)]),
@@ -707,6 +709,18 @@ class Batch:
 
     def set_device_loop(self, on=True):
         check(load().am_batch_set_device_loop(self.handle, int(bool(on))), "am_batch_set_device_loop")
+
+    def set_staged(self, on=True):
+        """True (default): the FP32 PCG K*u runs the tensor-copy staged kernel;
+        False: the warp-row kernel with the autotuned / pinned plan."""
+        check(load().am_batch_set_staged(self.handle, int(bool(on))), "am_batch_set_staged")
+
+    def bench_ku(self, reps=10):
+        """Average ms of one batched FP32 PCG K*u launch (every problem active), on
+        the state the last simp_step left."""
+        ms = ctypes.c_double(0.0)
+        check(load().am_batch_bench_ku(self.handle, int(reps), ctypes.byref(ms)), "am_batch_bench_ku")
+        return ms.value
 
     def axes(self, i):
         """The caller's axis (0 = x, 1 = y, 2 = z) that problem i stores as each of its

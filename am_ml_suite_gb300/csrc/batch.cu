@@ -24,6 +24,7 @@
 #include "batch.cuh"
 #include "host_util.h"
 #include "kernels.cuh"
+#include "ku3.cuh"
 
 using namespace amk;
 
@@ -95,6 +96,15 @@ struct am_batch {
     Pool<double> F, x64, r64, dinv64;
     Pool<float> r32, pa, pb, q32, dinv32, xh, xl;
     Pool<uint8_t> mask, fixed_bits;
+    // the tensor-copy staged PCG K*u: padded scale / constraint copies, per-problem
+    // tensor maps and arguments, (problem, tile) work list; staged = 0 runs the
+    // warp-row kernel with the autotuned plan instead
+    Pool<float> s32pad;
+    Pool<uint8_t> maskpad;
+    Pool<Ku3BatchItem> k3items;
+    Pool<int2> w_k3;
+    WorkList k3{};
+    bool staged = true;
     Pool<long long> f_idx;
     Pool<double> f_val;
     Pool<int4> tap_d;
@@ -130,16 +140,16 @@ int div_up_i(long long a, long long b) { return (int)((a + b - 1) / b); }
 // The axis order a problem is stored in.  The cube's element stiffness is the
 // same when the three axes and the displacement components are permuted together
 // (and the cone filter and OC step do not see axes), so each problem may keep its
-// grid in whichever axis order makes the batched K*u's tiles (30 node columns x
-// 15 node rows x all planes plus a halo plane) overhang it least; the caller's
-// order is restored at the boundary (loads, constraints, densities).  Ties keep
-// the caller's order.
+// grid in whichever axis order makes the batched K*u's tiles (28 node columns, as
+// the staged kernel's, x 15 node rows x all planes plus a halo plane) overhang it
+// least; the caller's order is restored at the boundary (loads, constraints,
+// densities).  Ties keep the caller's order.
 std::array<int, 3> best_axes(const int d[3]) {
     static const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
     long long best = -1;
     std::array<int, 3> out{0, 1, 2};
     for (const auto &q : P) {
-        const long long slots = (long long)div_up_i(d[q[0]] + 1, 30) * 32 * div_up_i(d[q[1]] + 1, 15) * 16 *
+        const long long slots = (long long)div_up_i(d[q[0]] + 1, 28) * 32 * div_up_i(d[q[1]] + 1, 15) * 16 *
                                 (d[q[2]] + 2);
         if (best < 0 || slots < best) {
             best = slots;
@@ -244,6 +254,52 @@ am_status plan_k2(am_batch *B, int warps, int zchunk) {
     return AM_OK;
 }
 
+// The staged K*u's records and work list: per problem the tensor maps of its
+// FP32 PCG vectors and padded copies, tiles of 28 x 15 nodes over all planes (one
+// z chunk: long tiles amortise each tile's pipeline fill), the tiles of the
+// problems with the most planes first.
+am_status plan_k3(am_batch *B) {
+    using Sh = Ku3Shape<8, 4>;
+    std::vector<Ku3BatchItem> rec(B->n);
+    std::vector<std::pair<int, int2>> w;
+    for (int p = 0; p < B->n; ++p) {
+        const BatchItem &it = B->items[p];
+        const Layout &L = it.L;
+        cudaError_t err = cudaSuccess;
+        Ku3Maps *T = ku3_make_maps(L, it.r32, it.pa, it.pb, it.dinv32, it.maskpad, it.s32pad, it.q32, &err);
+        if (!T) return bfail(AM_ERR_CUDA, "tensor maps of problem " + std::to_string(p) + ": " + cudaGetErrorString(err));
+        Ku3BatchItem &r = rec[p];
+        std::memset(&r, 0, sizeof(r));
+        r.T = *T;
+        ku3_free_maps(T);
+        r.A.M = B->C.M32;
+        r.A.partial = it.partial;
+        r.A.S = it.S;
+        r.A.tiles_x = div_up_i(L.nx + 1, Sh::TX);
+        r.A.tiles_y = div_up_i(L.ny + 1, Sh::TY);
+        r.A.tz = L.nz + 1;
+        r.A.nz = L.nz;
+        r.ntiles = r.A.tiles_x * r.A.tiles_y;
+        for (int b = 0; b < r.ntiles; ++b) w.push_back({L.nz, make_int2(p, b)});
+    }
+    std::stable_sort(w.begin(), w.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    std::vector<int2> wl(w.size());
+    for (size_t i = 0; i < w.size(); ++i) wl[i] = w[i].second;
+    BCK(B->k3items.alloc(rec.size()));
+    BCK(cudaMemcpy(B->k3items.p, rec.data(), rec.size() * sizeof(Ku3BatchItem), cudaMemcpyHostToDevice));
+    return upload_worklist(B, B->w_k3, B->k3, wl);
+}
+
+// one batched FP32 PCG iteration: the staged K*u over the (problem, tile) list or
+// the warp-row K*u of the autotuned plan, then the bulk-copy update
+cudaError_t pcg_iteration(am_batch *B) {
+    if (!B->staged)
+        return batch_pcg_iteration(B->items_d.p, B->k2, B->k2b, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2,
+                                   B->st);
+    if (cudaError_t e = batch_ku3_pcg(B->k3items.p, B->k3, B->C.M32, B->st)) return e;
+    return batch_pcg_update(B->items_d.p, B->chunk, kSms * 2, B->st);
+}
+
 // The device-side loop of a batched FP32 PCG round: a CUDA-graph while node whose
 // body is one chunk followed by batch_loop_next_kernel, which keeps the loop going
 // while some problem of the batch is still iterating and fewer than the cap's
@@ -304,8 +360,7 @@ am_status build_loop_graph(am_batch *B) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     e = cudaStreamBeginCaptureToGraph(B->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return bail(e, "batch loop body capture");
-    for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
-        e = batch_pcg_iteration(B->items_d.p, B->k2, B->k2b, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
+    for (int k = 0; k < kChunk && e == cudaSuccess; ++k) e = pcg_iteration(B);
     if (e == cudaSuccess) {
         batch_loop_next_kernel<<<1, 256, 0, B->st>>>(h, B->S.p, B->n, B->loopc.p);
         e = cudaGetLastError();
@@ -332,8 +387,7 @@ am_status build_graph(am_batch *B) {
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < kChunk && e == cudaSuccess; ++k)
-        e = batch_pcg_iteration(B->items_d.p, B->k2, B->k2b, B->chunk, B->C, B->warps, kSms * B->ctas, kSms * 2, B->st);
+    for (int k = 0; k < kChunk && e == cudaSuccess; ++k) e = pcg_iteration(B);
     cudaError_t e2 = cudaStreamEndCapture(B->st, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -416,8 +470,10 @@ am_status am_batch_destroy(am_batch *B) {
     for (auto *q : {&B->rho, &B->rho_new, &B->s64, &B->ce, &B->dc, &B->dcf, &B->oc_a, &B->oc_lo, &B->oc_hi,
                     &B->F, &B->x64, &B->r64, &B->dinv64, &B->f_val, &B->tap_w, &B->partial})
         q->release();
-    for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32, &B->xh, &B->xl}) q->release();
-    for (auto *q : {&B->design, &B->mask, &B->fixed_bits}) q->release();
+    for (auto *q : {&B->s32, &B->r32, &B->pa, &B->pb, &B->q32, &B->dinv32, &B->xh, &B->xl, &B->s32pad}) q->release();
+    for (auto *q : {&B->design, &B->mask, &B->fixed_bits, &B->maskpad}) q->release();
+    B->k3items.release();
+    B->w_k3.release();
     for (auto *q : {&B->w_elem, &B->w_vec, &B->w_k2, &B->w_k2b, &B->w_k64, &B->w_prob, &B->w_chunk}) q->release();
     B->f_idx.release();
     B->tap_d.release();
@@ -462,7 +518,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     B->poff.resize(n + 1);
     B->items.assign(n, BatchItem{});
     B->pcg_its.assign(n, 0);
-    size_t e = 0, nn = 0, pp = 0;
+    size_t e = 0, nn = 0, pp = 0, sp = 0, mp = 0;
+    std::vector<size_t> spoff(n), mpoff(n);
     for (int p = 0; p < n; ++p) {
         const int *d = shapes + 3 * p;
         B->dims[p] = {d[0], d[1], d[2]};
@@ -488,9 +545,17 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         // ku2 tiles of 1 plane), 3 per element block, 2 per vector block
         const size_t k2max = (size_t)div_up_i(L.nx + 1, 30) * div_up_i(L.ny + 1, 7) * (L.nz + 1);
         const size_t nchunk = 3 * (size_t)div_up_i(L.cs, BATCH_UPD_CHUNK);
-        pp += align_up(std::max({2 * k2max, 2 * (size_t)it.n_k64, 3 * (size_t)it.n_elem, 2 * (size_t)it.n_vec,
-                                 2 * nchunk, (size_t)16}),
+        const size_t k3 = (size_t)div_up_i(L.nx + 1, Ku3Shape<8, 4>::TX) * div_up_i(L.ny + 1, Ku3Shape<8, 4>::TY);
+        pp += align_up(std::max({2 * k2max, 2 * k3, 2 * (size_t)it.n_k64, 3 * (size_t)it.n_elem,
+                                 2 * (size_t)it.n_vec, 2 * nchunk, (size_t)16}),
                        32);
+        // padded copies for the staged K*u (16-byte aligned rows; 256-byte aligned starts)
+        long long se = 0, mb = 0;
+        ku3_padded_sizes(L, &se, &mb);
+        spoff[p] = sp;
+        mpoff[p] = mp;
+        sp += align_up((size_t)se, 64);
+        mp += align_up((size_t)mb, 256);
     }
     B->eoff[n] = e;
     B->noff[n] = nn;
@@ -510,6 +575,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     A(B->dinv32, nn);
     A(B->mask, nn);
     A(B->fixed_bits, nn);
+    A(B->s32pad, sp);
+    A(B->maskpad, mp);
     A(B->partial, pp);
     A(B->S, (size_t)n);
     A(B->items_d, (size_t)n);
@@ -546,6 +613,8 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
         it.xl = B->xl.p + 3 * no;
         it.dinv32 = B->dinv32.p + no;
         it.mask = B->mask.p + no;
+        it.s32pad = B->s32pad.p + spoff[p];
+        it.maskpad = B->maskpad.p + mpoff[p];
         it.fixed_bits = B->fixed_bits.p + no;
         it.partial = B->partial.p + B->poff[p];
         it.S = B->S.p + p;
@@ -561,7 +630,9 @@ am_status am_batch_create(int n, const int *shapes, double h, double E0, double 
     if (s == AM_OK) s = upload_worklist(B, B->w_prob, B->prob, wp);
     if (s == AM_OK) s = upload_worklist(B, B->w_chunk, B->chunk, wc);
     if (s == AM_OK) s = plan_k2(B, 8, 0);
-    if (s == AM_OK && ku_init_attributes() != cudaSuccess) s = bfail(AM_ERR_CUDA, "kernel attributes");
+    if (s == AM_OK) s = plan_k3(B);
+    if (s == AM_OK && (ku_init_attributes() != cudaSuccess || batch_ku3_init_attributes() != cudaSuccess))
+        s = bfail(AM_ERR_CUDA, "kernel attributes");
     if (s != AM_OK) {
         am_batch_destroy(B);
         return s;
@@ -639,6 +710,66 @@ am_status am_batch_set_loads(am_batch *B, const double *F, const int64_t *fixed,
     }
     BCK(cudaMemcpy(B->items_d.p, B->items.data(), B->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
     B->loads_set = true;
+    return AM_OK;
+}
+
+am_status am_batch_set_staged(am_batch *B, int on) {
+    BCKS(check_batch(B));
+    if ((on != 0) != B->staged) {
+        B->staged = on != 0;
+        // the chunk graphs hold the other kernel
+        if (B->graph) cudaGraphExecDestroy(B->graph);
+        if (B->loop) cudaGraphExecDestroy(B->loop);
+        B->graph = nullptr;
+        B->loop = nullptr;
+        // the padded copies are refreshed with the operator at every step; a switch
+        // between steps refreshes them now
+        if (B->staged && B->begun) BCK(batch_ku3_pad(B->items_d.p, B->vec, kSms * 8, B->st));
+    }
+    return AM_OK;
+}
+
+am_status am_batch_bench_ku(am_batch *B, int reps, double *avg_ms) {
+    BCKS(check_batch(B));
+    if (!B->begun) return bfail(AM_ERR_INVALID_ARG, "am_batch_simp_begin not called");
+    if (reps < 1 || !avg_ms) return bfail(AM_ERR_INVALID_ARG, "need reps >= 1 and an output");
+    // every problem iterating, first PCG iteration (beta 0: p = D^-1 r, p_prev not
+    // read), on the residual and operator the last step left; state restored after
+    BCK(batch_operator(B->items_d.p, B->elem, B->vec, B->C, kSms * 8, B->st));
+    if (B->staged) BCK(batch_ku3_pad(B->items_d.p, B->vec, kSms * 8, B->st));
+    BCKS(sync_scalars(B));
+    std::vector<Scalars> saved(B->Sh, B->Sh + B->n), run(saved);
+    for (Scalars &S : run) {
+        S.done = 0;
+        S.frozen = 0;
+        S.it = 0;
+        S.beta = 0.0;
+        S.rz = 1.0;
+        S.cnt_ku = 0;
+        S.kerr = 0;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    double tot = 0.0;
+    for (int r = 0; r < reps + 1; ++r) {  // the first launch warms up
+        BCK(cudaMemcpyAsync(B->S.p, run.data(), sizeof(Scalars) * B->n, cudaMemcpyHostToDevice, B->st));
+        BCK(cudaEventRecord(e0, B->st));
+        if (B->staged)
+            BCK(batch_ku3_pcg(B->k3items.p, B->k3, B->C.M32, B->st));
+        else
+            BCK(batch_pcg_ku(B->items_d.p, B->k2, B->k2b, B->C, B->warps, kSms * B->ctas, B->st));
+        BCK(cudaEventRecord(e1, B->st));
+        BCK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0) tot += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    BCK(cudaMemcpyAsync(B->S.p, saved.data(), sizeof(Scalars) * B->n, cudaMemcpyHostToDevice, B->st));
+    BCK(cudaStreamSynchronize(B->st));
+    *avg_ms = tot / reps;
     return AM_OK;
 }
 
@@ -819,6 +950,7 @@ am_status am_batch_simp_step(am_batch *B, double *compliance, double *volume, do
         return AM_OK;
     }
     BCK(batch_operator(B->items_d.p, B->elem, B->vec, B->C, kSms * 8, B->st));
+    if (B->staged) BCK(batch_ku3_pad(B->items_d.p, B->vec, kSms * 8, B->st));
     BCK(batch_prepare_solve(B->items_d.p, B->vec, B->prob, kSms * 8, B->st));
     BCKS(batch_solve(B, B->max_chunks));
     BCK(batch_resid(B->items_d.p, B->k64, B->C, 1, kSms * 4, B->st));

@@ -27,6 +27,10 @@ struct BatchItem {
     double *F, *x64, *r64, *dinv64;
     float *r32, *pa, *pb, *q32, *dinv32;
     float *xh, *xl;  // the FP32 PCG's iterate as a double-float pair (x64 = xh + xl)
+    // padded copies of s32 and mask read by the tensor-copy staged K*u (rows of
+    // round_up(nx, 4) scales, round_up(nx+1, 16) constraint bytes)
+    float *s32pad;
+    uint8_t *maskpad;
     uint8_t *mask, *fixed_bits;
     // nonzeros of F (node-plane index) for u.F and |F|^2
     const long long *f_idx;
@@ -87,6 +91,19 @@ constexpr int BATCH_UPD_CHUNK = 2048;
 // plain FP32 K*u (y = q32, u = pa) over the batch, for the autotuner
 cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
                            cudaStream_t st);
+// The tensor-copy staged FP32 PCG K*u of the single-problem solver over a batch
+// (ku3.cu): one CTA per (problem, tile) work item of k3, each problem's tensor maps
+// and arguments in items; the padded scale and constraint copies it reads are
+// refreshed by batch_ku3_pad after every change of the operator or mask.
+struct Ku3BatchItem;
+cudaError_t batch_ku3_init_attributes();
+cudaError_t batch_ku3_pcg(const Ku3BatchItem *items, WorkList k3, const Modal<float> &M, cudaStream_t st);
+cudaError_t batch_ku3_pad(const BatchItem *items, WorkList vec, int grid, cudaStream_t st);
+// the K*u half of batch_pcg_iteration alone (warp-row kernel)
+cudaError_t batch_pcg_ku(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
+                         cudaStream_t st);
+// the update half of batch_pcg_iteration alone (after batch_ku3_pcg)
+cudaError_t batch_pcg_update(const BatchItem *it, WorkList chunks, int grid_vec, cudaStream_t st);
 // sensitivities + u.F, filter, OC bisection (FP64), new density copied into rho
 cudaError_t batch_update(const BatchItem *it, WorkList elem, WorkList prob, int grid, cudaStream_t st);
 

@@ -2092,6 +2092,14 @@ cudaError_t batch_pcg_iteration(const BatchItem *it, WorkList k2, WorkList k2b, 
     b_update_df_kernel<<<std::max(1, std::min(grid_vec, vec.n)), 256, UPD_SMEM, st>>>(it, vec);
     return counted(cudaGetLastError());
 }
+cudaError_t batch_pcg_ku(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
+                         cudaStream_t st) {
+    return batch_ku_launch<KU_PCG>(it, k2, k2b, C, warps, grid, st);
+}
+cudaError_t batch_pcg_update(const BatchItem *it, WorkList chunks, int grid_vec, cudaStream_t st) {
+    b_update_df_kernel<<<std::max(1, std::min(grid_vec, chunks.n)), 256, UPD_SMEM, st>>>(it, chunks);
+    return counted(cudaGetLastError());
+}
 cudaError_t batch_ku_plain(const BatchItem *it, WorkList k2, WorkList k2b, const BatchConst &C, int warps, int grid,
                            cudaStream_t st) {
     return batch_ku_launch<KU_PLAIN>(it, k2, k2b, C, warps, grid, st);

@@ -5,12 +5,13 @@
 #include <algorithm>
 #include <new>
 
+#include "batch.cuh"
 #include "kernels.cuh"
 #include "ku3.cuh"
 
 namespace amk {
 
-static inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+__host__ __device__ inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
 void ku3_padded_sizes(const Layout &L, long long *scale_entries, long long *mask_bytes) {
     if (scale_entries) *scale_entries = round_up(L.nx, 4) * L.ny * L.nz;
@@ -19,10 +20,11 @@ void ku3_padded_sizes(const Layout &L, long long *scale_entries, long long *mask
 
 // scale_pad[(ez ny + ey) sxe + ex] = s32[(ez ny + ey) nx + ex];
 // mask_pad[(iz (ny+1) + iy) sxm + ix] = mask[iz sxy + iy sx + ix]
-__global__ void ku3_pad_kernel(Layout L, const float *__restrict__ s32, const uint8_t *__restrict__ mask,
-                               float *__restrict__ scale_pad, uint8_t *__restrict__ mask_pad, int sxe, int sxm) {
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// (entries i0, i0 + stride, ... of both)
+__device__ __forceinline__ void ku3_pad_body(const Layout &L, const float *__restrict__ s32,
+                                             const uint8_t *__restrict__ mask, float *__restrict__ scale_pad,
+                                             uint8_t *__restrict__ mask_pad, int sxe, int sxm, long long i0,
+                                             long long stride) {
     for (long long e = i0; e < L.nel; e += stride) {
         const long long row = e / L.nx;
         const int ex = (int)(e - row * L.nx);
@@ -35,6 +37,23 @@ __global__ void ku3_pad_kernel(Layout L, const float *__restrict__ s32, const ui
         const int ix = (int)(n - row * (L.nx + 1));
         const long long iz = row / (L.ny + 1), iy = row - iz * (L.ny + 1);
         mask_pad[row * sxm + ix] = mask[iz * L.sxy + iy * L.sx + ix];
+    }
+}
+__global__ void ku3_pad_kernel(Layout L, const float *__restrict__ s32, const uint8_t *__restrict__ mask,
+                               float *__restrict__ scale_pad, uint8_t *__restrict__ mask_pad, int sxe, int sxm) {
+    ku3_pad_body(L, s32, mask, scale_pad, mask_pad, sxe, sxm, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
+}
+// the same for every problem of a batch: block b of a problem's n handles
+// entries b * 256 + t, stride n * 256
+__global__ void __launch_bounds__(256) b_ku3_pad_kernel(const BatchItem *items, WorkList W) {
+    for (int w = blockIdx.x; w < W.n; w += gridDim.x) {
+        const int2 k = W.w[w];
+        const BatchItem &it = items[k.x];
+        if (it.S->frozen) continue;
+        ku3_pad_body(it.L, it.s32, it.mask, it.s32pad, it.maskpad, (int)round_up(it.L.nx, 4),
+                     (int)round_up(it.L.nx + 1, 16), (long long)k.y * blockDim.x + threadIdx.x,
+                     (long long)it.n_vec * blockDim.x);
     }
 }
 
@@ -209,6 +228,46 @@ cudaError_t ku3b_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const
         ku3b_kernel<8, 4><<<K.ntiles(), 256, Ku3bShape<8, 4>::SMEM_ALLOC, st>>>(*T, a);
     else
         return cudaErrorInvalidValue;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+// ---- batches ----------------------------------------------------------------------
+
+// One tile of one problem per CTA (work items (problem, tile), the longest tiles
+// first); problems that are frozen or whose PCG is done leave at once.
+// The element constants come from the launch's parameters (one material per
+// batch), so the arithmetic can read them there as the single-problem kernel does.
+__global__ void __launch_bounds__(256, 2) b_ku3_kernel(const Ku3BatchItem *items, WorkList W, const Modal<float> M) {
+    const int2 k = W.w[blockIdx.x];
+    const Ku3BatchItem &it = items[k.x];
+    Ku3Args A = it.A;
+    A.M = M;
+    if (A.S->frozen) return;
+    if (threadIdx.x == 0) {
+        for (const CUtensorMap *m : {&it.T.r, &it.T.pa, &it.T.pb, &it.T.d, &it.T.m, &it.T.s, &it.T.qst, &it.T.past,
+                                     &it.T.pbst})
+            tensormap_acquire(m);
+    }
+    ku3_tile<8, 4>(it.T, A, k.y, it.ntiles);
+}
+
+cudaError_t batch_ku3_init_attributes() {
+    return cudaFuncSetAttribute(b_ku3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Ku3Shape<8, 4>::SMEM_ALLOC);
+}
+
+cudaError_t batch_ku3_pcg(const Ku3BatchItem *items, WorkList k3, const Modal<float> &M, cudaStream_t st) {
+    if (k3.n < 1) return cudaSuccess;
+    b_ku3_kernel<<<k3.n, 256, Ku3Shape<8, 4>::SMEM_ALLOC, st>>>(items, k3, M);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+cudaError_t batch_ku3_pad(const BatchItem *items, WorkList vec, int grid, cudaStream_t st) {
+    if (vec.n < 1) return cudaSuccess;
+    b_ku3_pad_kernel<<<std::max(1, std::min(grid, vec.n)), 256, 0, st>>>(items, vec);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) count_launches(1);
     return e;

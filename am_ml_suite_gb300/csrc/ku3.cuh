@@ -123,8 +123,12 @@ __device__ __forceinline__ void prefetch_map(const CUtensorMap *m) {
 
 // p = D^-1 r + beta p_prev (p_prev / p the ping-pong pair chosen by the parity of
 // S->it), q = mask(K p), partial p.q -> S->alpha (last block).  One tile per CTA.
+// The body of one tile: tile `blk` of the problem's `nblk`, which take part in
+// the p.q reduction together (ku3_kernel: one problem, a tile per CTA; the
+// batched kernel: a tile of one problem of a batch per CTA).  T may live in the
+// kernel's parameters or in global memory.
 template <int W, int S>
-__global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ Ku3Maps T, const Ku3Args A) {
+__device__ __forceinline__ void ku3_tile(const Ku3Maps &T, const Ku3Args &A, const int blk, const int nblk) {
     using namespace k2;
     using Sh = Ku3Shape<W, S>;
     constexpr int TX = Sh::TX, BX = Sh::BX, BY = Sh::BY, BXM = Sh::BXM, TY = Sh::TY, OCS = Sh::OUT_CS;
@@ -139,7 +143,7 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
 
     if (A.S->done) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int b = blockIdx.x;
+    int b = blk;
     const int tx_ = b % A.tiles_x;
     b /= A.tiles_x;
     const int ty_ = b % A.tiles_y;
@@ -338,10 +342,10 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
 
     double dv[1] = {dot.value()};
     block_sum<1>(dv, red);
-    if (threadIdx.x == 0) A.partial[2 * blockIdx.x] = dv[0];
-    if (!arrive_last_n(&A.S->cnt_ku, &last_flag, gridDim.x)) return;
+    if (threadIdx.x == 0) A.partial[2 * blk] = dv[0];
+    if (!arrive_last_n(&A.S->cnt_ku, &last_flag, nblk)) return;
     double tot[1];
-    reduce_partials<1>(A.partial, gridDim.x, 2, tot, red);
+    reduce_partials<1>(A.partial, nblk, 2, tot, red);
     if (threadIdx.x == 0) {
         Scalars *Sc = A.S;
         const double pq = tot[0];
@@ -355,6 +359,27 @@ __global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ 
         }
         Sc->cnt_ku = 0;
     }
+}
+
+template <int W, int S>
+__global__ void __launch_bounds__(32 * W, 2) ku3_kernel(const __grid_constant__ Ku3Maps T, const Ku3Args A) {
+    ku3_tile<W, S>(T, A, blockIdx.x, gridDim.x);
+}
+
+// ---- batches: one tile of one problem per CTA ---------------------------------------
+// A batch problem's tensor maps and arguments (a 64-byte aligned record per
+// problem in global memory) and its tile count, the p.q reduction's participants.
+struct Ku3BatchItem {
+    Ku3Maps T;
+    Ku3Args A;
+    int ntiles;
+};
+
+// orders this thread's later tensor copies through map m after the map's bytes
+// were written to global memory (by a copy from the host before the launch)
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(m))
+                 : "memory");
 }
 
 // ---- the same product without a CTA-wide barrier per plane -----------------------

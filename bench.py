@@ -131,6 +131,7 @@ def run_batch(args, nat, world, rank, emit=True):
     cfgs = [batch_config(nat, pr) for pr in probs]
     b.simp_begin(cfgs)
     plan = b.autotune(reps=5)
+    b.set_staged(args.batch_ku == "staged")
     for _ in range(args.warmup):
         b.simp_step()
     its0 = b.pcg_iterations.copy()
@@ -158,11 +159,13 @@ def run_batch(args, nat, world, rank, emit=True):
         dist.all_reduce(t, op=dist.ReduceOp.SUM)
         elapsed, stepped = float(tmax[0]), int(t[1])
     value = stepped / elapsed
-    # roofline: plain batched FP32 K*u of the chosen plan (u, y: 12 B per node
-    # each, scale 4 B per element)
-    alg = 24 * nodes + 4 * nel
+    # roofline: the batched FP32 PCG K*u the solve runs (p = D^-1 r + beta p, q =
+    # mask(K p), p.q: reads p, r 12 B per node each, D^-1 4 B, constraint bits 1 B,
+    # scale 4 B per element; writes p, q 12 B per node each), every problem active
+    ku_ms = b.bench_ku(reps=10)
+    alg = 53 * nodes + 4 * nel
     peak, peak_kind = measured_peaks()
-    achieved = alg / (plan["ms"] * 1e-3) / 1e9
+    achieved = alg / (ku_ms * 1e-3) / 1e9
     b.close()
     e2e = None
     if not args.no_e2e:
@@ -170,6 +173,7 @@ def run_batch(args, nat, world, rank, emit=True):
         q = nat.Batch(shapes)
         if world > 1:
             dist.barrier()
+        q.set_staged(args.batch_ku == "staged")
         te0 = time.perf_counter()
         q.set_loads([pr["F"] for pr in probs], [pr["fixed"] for pr in probs])
         out = q.simp_run([batch_config(nat, pr, total) for pr in probs])
@@ -228,15 +232,18 @@ def run_batch(args, nat, world, rank, emit=True):
             "config": {"workload": "batch256", "problems": 256, "problems_rank0": len(probs), "elements_rank0": nel,
                        "nodes_rank0": nodes,
                        "description": build_batch256.__doc__.strip().replace("\n", " "), "cg_tol": 1e-6,
+                       "pcg_ku": args.batch_ku,
                        "autotuned_plan": plan, "l2": "working set per step > 129 MB L2",
                        "parallelism": f"problems sharded over {world} ranks (LPT by cost)" if world > 1 else "1 GPU"},
             "pcg_iterations_per_problem_step": float(np.mean(its_per_step)),
             "roofline": {"bound": "hbm",
-                         "kernel": ("b_ku2_kernel<8|4,KU_PLAIN> (batched FP32 K*u, tile height per problem)"
+                         "kernel": ("b_ku3_kernel (batched tensor-copy staged FP32 PCG K*u, 28 x 15-node tiles)"
+                                    if args.batch_ku == "staged" else
+                                    "b_ku2_kernel<8|4,KU_PCG> (batched warp-row FP32 PCG K*u, tile height per problem)"
                                     if plan["warps"] == 0 else
-                                    f"b_ku2_kernel<{plan['warps']},KU_PLAIN> (batched FP32 K*u)"),
+                                    f"b_ku2_kernel<{plan['warps']},KU_PCG> (batched warp-row FP32 PCG K*u)"),
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": alg, "avg_ms": plan["ms"]},
+                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": alg, "avg_ms": ku_ms},
             "gpu_launches": int(l1 - l0), "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,
         }
         if emit:
@@ -572,6 +579,8 @@ def main():
     ap.add_argument("--mixed-solver", default="reliable", choices=sorted(MIXED_SOLVER),
                     help="jacobi arm: one FP32 PCG with FP64 residual replacement (reliable) or the FP64 "
                          "flexible CG over FP32 inner solves (flexible)")
+    ap.add_argument("--batch-ku", default="staged", choices=["staged", "warp-row"],
+                    help="batch256: the FP32 PCG K*u kernel (tensor-copy staged, or warp-row with the autotuned plan)")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive every inner PCG solve chunk by chunk from the host instead of the device-side "
                          "graph loop (same results; the measurement baseline of the loop)")
@@ -808,12 +817,13 @@ def main():
                             "frac": bb / (kb_ms * 1e-3) / 1e9 / peak, "avg_ms": kb_ms, "algorithmic_bytes": bb}}
         import types
 
-        lbatch = run_batch(types.SimpleNamespace(steps=3, warmup=2, no_e2e=True, no_cpu_baseline=True), nat, 1, 0,
-                           emit=False)
+        lbatch = run_batch(types.SimpleNamespace(steps=3, warmup=2, no_e2e=True, no_cpu_baseline=True,
+                                                 batch_ku=args.batch_ku), nat, 1, 0, emit=False)
         other["batch256"] = {k: lbatch[k] for k in ("metric", "value", "unit", "ms_per_step",
                                                    "pcg_iterations_per_problem_step", "roofline")}
         other["batch256"]["steps"] = 3
         other["batch256"]["autotuned_plan"] = lbatch["config"]["autotuned_plan"]
+        other["batch256"]["pcg_ku"] = lbatch["config"]["pcg_ku"]
 
     if rank == 0:
         ref = results.get("jacobi")

@@ -467,6 +467,18 @@ am_status am_batch_autotune(am_batch *b, int reps, int *warps, int *z_chunk, int
  * z_chunk 0 (all planes) or >= 1; ctas_per_sm 1-4. */
 am_status am_batch_set_plan(am_batch *b, int warps, int z_chunk, int ctas_per_sm);
 
+/* Which kernel runs the batch's FP32 PCG K*u.  on != 0 (the default): the
+ * single-problem solver's tensor-copy staged kernel, one CTA per tile of 28 x 15
+ * nodes over all of a problem's planes, each problem's tensor maps in device
+ * memory; 0: the warp-row kernel with the plan of am_batch_autotune /
+ * am_batch_set_plan.  Both compute the same p and q.  No reference counterpart. */
+am_status am_batch_set_staged(am_batch *b, int on);
+/* Times the batch's FP32 PCG K*u (the kernel am_batch_set_staged selects) with CUDA
+ * events over `reps` launches after one warm-up, every problem iterating, on the
+ * residual and densities the last am_batch_simp_step left; the solver state is
+ * restored afterwards.  Measurement only; no reference counterpart. */
+am_status am_batch_bench_ku(am_batch *b, int reps, double *avg_ms);
+
 /* The CUDA stream the batch's kernels run on (cudaStream_t). */
 am_status am_batch_stream(am_batch *b, void **stream);
 

@@ -213,3 +213,43 @@ def test_batch_axis_order_and_layouts():
         assert np.abs(got - ref["density"].reshape(shape)).max() <= 1e-4, shape
     with pytest.raises(nat.AmError):
         b.axes(3)
+
+
+def test_batch_staged_ku_matches_warp_row_ku():
+    """The batch's FP32 PCG K*u on the tensor-copy staged kernel (default, one CTA
+    per 28 x 15-node tile of a problem, tensor maps in device memory) and on the
+    warp-row kernel compute the same p and q; their p.q sums run over different
+    tiles, so two batches solved to rel-res 1e-9 agree to rounding: compliance
+    within 1e-7, densities within 1e-6."""
+    out = []
+    for staged in (True, False):
+        b, _ = _batch(SHAPES, seed=13)
+        b.set_staged(staged)
+        out.append(b.simp_run([_cfg(4) for _ in SHAPES]))
+        b.close()
+    for x, y in zip(*out):
+        assert x["pcg_iterations"] > 0 and y["pcg_iterations"] > 0
+        assert np.allclose(x["compliance"], y["compliance"], rtol=1e-7, atol=0)
+        assert np.abs(x["density"] - y["density"]).max() <= 1e-6
+
+
+def test_batch_bench_ku_restores_state():
+    """am_batch_bench_ku times the PCG K*u of either kernel between SIMP steps and
+    leaves the solver state as it found it: the steps after it are bitwise those of
+    an uninterrupted run."""
+    ref, _ = _batch(SHAPES, seed=17)
+    cfgs = [_cfg(4, tol=1e-7) for _ in SHAPES]
+    ref.simp_begin(cfgs)
+    hist_ref = [ref.simp_step()[0] for _ in range(4)]
+    b, _ = _batch(SHAPES, seed=17)
+    b.simp_begin(cfgs)
+    hist = [b.simp_step()[0] for _ in range(2)]
+    assert b.bench_ku(reps=3) > 0
+    b.set_staged(False)
+    assert b.bench_ku(reps=3) > 0
+    b.set_staged(True)
+    hist += [b.simp_step()[0] for _ in range(2)]
+    for h, r in zip(hist, hist_ref):
+        assert np.array_equal(h, r)
+    for p in range(len(SHAPES)):
+        assert np.array_equal(b.densities()[p], ref.densities()[p])
