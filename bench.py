@@ -132,6 +132,7 @@ def run_batch(args, nat, world, rank, emit=True):
     b.simp_begin(cfgs)
     plan = b.autotune(reps=5)
     b.set_staged(args.batch_ku == "staged")
+    b.set_device_loop(not getattr(args, "host_loop", False))
     for _ in range(args.warmup):
         b.simp_step()
     its0 = b.pcg_iterations.copy()
@@ -174,6 +175,7 @@ def run_batch(args, nat, world, rank, emit=True):
         if world > 1:
             dist.barrier()
         q.set_staged(args.batch_ku == "staged")
+        q.set_device_loop(not getattr(args, "host_loop", False))
         te0 = time.perf_counter()
         q.set_loads([pr["F"] for pr in probs], [pr["fixed"] for pr in probs])
         out = q.simp_run([batch_config(nat, pr, total) for pr in probs])
@@ -818,7 +820,8 @@ def main():
         import types
 
         lbatch = run_batch(types.SimpleNamespace(steps=3, warmup=2, no_e2e=True, no_cpu_baseline=True,
-                                                 batch_ku=args.batch_ku), nat, 1, 0, emit=False)
+                                                 batch_ku=args.batch_ku, host_loop=_host_loop), nat, 1, 0,
+                           emit=False)
         other["batch256"] = {k: lbatch[k] for k in ("metric", "value", "unit", "ms_per_step",
                                                    "pcg_iterations_per_problem_step", "roofline")}
         other["batch256"]["steps"] = 3
