@@ -1,5 +1,6 @@
 // ku3.cu -- host side of the TMA-staged FP32 PCG K*u (ku3.cuh): tensor maps,
-// the padded copies they read, the launch plan and the launcher.
+// the padded copies they read, the launch plan and the launchers; and the same
+// kernel over a batch of problems (one CTA per tile of one problem).
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(256, 2) b_ku3_kernel(const Ku3BatchItem *items
     const Ku3BatchItem &it = items[k.x];
     Ku3Args A = it.A;
     A.M = M;
-    if (A.S->frozen) return;
+    if (A.S->frozen || A.S->done) return;
     if (threadIdx.x == 0) {
         for (const CUtensorMap *m : {&it.T.r, &it.T.pa, &it.T.pb, &it.T.d, &it.T.m, &it.T.s, &it.T.qst, &it.T.past,
                                      &it.T.pbst})
