@@ -73,8 +73,10 @@ struct Ku3Shape {
     static constexpr int OFF_S = OFF_M + r128(MSK_B);
     static constexpr int STAGE = OFF_S + r128(SCL_B);
     // one output tile [3][TY+1][TX]: row TY of each component is a scratch row
-    // that lanes and rows owning no node write to, so the stores need no branch
-    static constexpr int OUT_CS = (TY + 1) * TX;  // component stride (floats)
+    // that lanes and rows owning no node write to, so the stores need no branch.
+    // A tensor copy's shared-memory operand starts on a 128-byte boundary, so
+    // the component stride is rounded up to 32 floats (448 already for 8 warps).
+    static constexpr int OUT_CS = ((TY + 1) * TX + 31) / 32 * 32;  // component stride (floats)
     static constexpr int OUT_B = 3 * OUT_CS * 4;
     static constexpr int OFF_OUT = S * STAGE;  // q[2], p[2]
     static constexpr int OFF_XCH = OFF_OUT + 4 * r128(OUT_B);
@@ -87,6 +89,12 @@ struct Ku3Shape {
     static constexpr int SMEM = OFF_FLAG + 8;
     // dynamic shared memory requested: the kernel aligns its base to 1024 bytes
     static constexpr int SMEM_ALLOC = SMEM + 1024;
+    // every tensor-copy destination and source in shared memory on a 128-byte boundary
+    static_assert(OFF_P % 128 == 0 && OFF_D % 128 == 0 && OFF_M % 128 == 0 && OFF_S % 128 == 0 && STAGE % 128 == 0,
+                  "stage buffers must start on 128-byte boundaries");
+    static_assert(OFF_OUT % 128 == 0 && (OUT_CS * 4) % 128 == 0 && r128(OUT_B) % 128 == 0,
+                  "output tiles and their components must start on 128-byte boundaries");
+    static_assert(OFF_BAR % 8 == 0, "mbarriers are 8-byte aligned");
 };
 
 namespace tma {
