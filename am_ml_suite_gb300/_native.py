@@ -204,6 +204,9 @@ SIGNATURES = {
     "am_precond_eval": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, _dp]),
     "am_problem_set_preconditioner": (ctypes.c_int, [_vp, _vp]),
     "am_problem_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_problem_set_ku_plan": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "am_problem_get_ku_plan": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int)]),
     "am_problem_set_residual_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_device_loop": (ctypes.c_int, [_vp, ctypes.c_int]),
     "am_batch_set_plan": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
@@ -464,6 +467,17 @@ class Problem:
         """True (default): each inner PCG solve is one CUDA-graph launch with a
         device-side loop; False: the host launches and checks chunk by chunk."""
         check(load().am_problem_set_device_loop(self.handle, int(bool(on))), "am_problem_set_device_loop")
+
+    def set_ku_plan(self, warps=0):
+        """Tile height of the FP32 PCG's staged K*u: 0 (chosen by grid), 7 or 8 warps."""
+        check(load().am_problem_set_ku_plan(self.handle, int(warps)), "am_problem_set_ku_plan")
+
+    def ku_plan(self):
+        """The staged K*u's plan: dict(warps, tiles, z_chunk)."""
+        w, t, z = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        check(load().am_problem_get_ku_plan(self.handle, ctypes.byref(w), ctypes.byref(t), ctypes.byref(z)),
+              "am_problem_get_ku_plan")
+        return {"warps": w.value, "tiles": t.value, "z_chunk": z.value}
 
     def set_residual_arithmetic(self, mode):
         """RESID_DOUBLE_FLOAT (default) or RESID_FP64: the arithmetic of the mixed

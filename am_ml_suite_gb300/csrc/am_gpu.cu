@@ -110,7 +110,7 @@ struct am_problem {
     Modal<double> M64;
     Modal<float> M32;
     KuLaunch plan32, plan64;
-    KuLaunch plan3;           // TMA-staged FP32 PCG K*u (ku3)
+    KuLaunch plan3;           // TMA-staged FP32 PCG K*u (ku3): 7- or 8-warp tiles
     int ku3_stages = 4;
     // the solver's K*u: 0 = ku3_kernel (tensor-store output tiles, ku3_stages
     // stages; the faster on GB300), 1 = ku3b_kernel (no CTA barrier per plane)
@@ -218,8 +218,9 @@ am_status ensure_vectors(am_problem *P, bool fp64) {
         CK(P->s32pad.alloc((size_t)se));
         CK(P->maskpad.alloc((size_t)mb));
     }
-    const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), P->plan3.ntiles(), P->nblocks_vec,
-                                            152 * 16});
+    // the staged K*u's partials for either tile height (am_problem_set_ku_plan)
+    const size_t np = 3 * (size_t)std::max({P->plan32.ntiles(), P->plan64.ntiles(), ku3_plan(P->L, 7).ntiles(),
+                                            ku3_plan(P->L, 8).ntiles(), P->nblocks_vec, 152 * 16});
     CK(P->partial.alloc(np));
     return AM_OK;
 }
@@ -298,7 +299,7 @@ am_status ku3_ready(am_problem *P) {
     if (!P->maps3) {
         cudaError_t e = cudaSuccess;
         P->maps3 = ku3_make_maps(P->L, P->r32.p, P->p32a.p, P->p32b.p, P->dinv32.p, P->maskpad.p, P->s32pad.p,
-                                 P->q32v.p, &e);
+                                 P->q32v.p, P->plan3.warps, &e);
         if (!P->maps3) return fail(AM_ERR_CUDA, std::string("tensor maps of the PCG vectors: ") + cudaGetErrorString(e));
     }
     if (P->pad_dirty) {
@@ -1595,6 +1596,33 @@ am_status am_problem_set_residual_arithmetic(am_problem *P, int mode) {
     CKS(check_problem(P));
     if (mode != AM_RESID_DOUBLE_FLOAT && mode != AM_RESID_FP64) return fail(AM_ERR_INVALID_ARG, "unknown residual mode");
     P->resid_df = mode == AM_RESID_DOUBLE_FLOAT;
+    return AM_OK;
+}
+
+am_status am_problem_set_ku_plan(am_problem *P, int warps) {
+    CKS(check_problem(P));
+    if (warps != 0 && warps != 7 && warps != 8) return fail(AM_ERR_INVALID_ARG, "warps must be 0, 7 or 8");
+    const KuLaunch K = ku3_plan(P->L, warps);
+    if (K.warps != P->plan3.warps || K.tz != P->plan3.tz) {
+        CK(cudaStreamSynchronize(P->st));
+        // the tensor maps' boxes and the FP32 solver graphs hold the old plan
+        ku3_free_maps(P->maps3);
+        P->maps3 = nullptr;
+        for (cudaGraphExec_t *g : {&P->g32, &P->gl32})
+            if (*g) {
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
+        P->plan3 = K;
+    }
+    return AM_OK;
+}
+
+am_status am_problem_get_ku_plan(am_problem *P, int *warps, int *tiles, int *z_chunk) {
+    CKS(check_problem(P));
+    if (warps) *warps = P->plan3.warps;
+    if (tiles) *tiles = P->plan3.ntiles();
+    if (z_chunk) *z_chunk = P->plan3.tz;
     return AM_OK;
 }
 

@@ -266,7 +266,7 @@ am_status plan_k3(am_batch *B) {
         const BatchItem &it = B->items[p];
         const Layout &L = it.L;
         cudaError_t err = cudaSuccess;
-        Ku3Maps *T = ku3_make_maps(L, it.r32, it.pa, it.pb, it.dinv32, it.maskpad, it.s32pad, it.q32, &err);
+        Ku3Maps *T = ku3_make_maps(L, it.r32, it.pa, it.pb, it.dinv32, it.maskpad, it.s32pad, it.q32, 8, &err);
         if (!T) return bfail(AM_ERR_CUDA, "tensor maps of problem " + std::to_string(p) + ": " + cudaGetErrorString(err));
         Ku3BatchItem &r = rec[p];
         std::memset(&r, 0, sizeof(r));

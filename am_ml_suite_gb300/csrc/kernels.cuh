@@ -36,11 +36,11 @@ KuLaunch ku_plan_shape(const Layout &L, int tx, int ty, int warps, int ctas_per_
 
 // ---- TMA-staged FP32 PCG K*u (ku3.cuh) -----------------------------------------
 struct Ku3Maps;
-// tensor maps of the problem's FP32 PCG vectors; the two padded arrays are
-// ku3_padded_sizes() long and filled by ku3_pad().  Returns nullptr and sets
-// *err on failure.  Free with ku3_free_maps.
+// tensor maps of the problem's FP32 PCG vectors for tiles of `warps` (7 or 8)
+// warps; the two padded arrays are ku3_padded_sizes() long and filled by
+// ku3_pad().  Returns nullptr and sets *err on failure.  Free with ku3_free_maps.
 Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const float *pb, const float *dinv,
-                       const uint8_t *mask_pad, const float *scale_pad, float *q, cudaError_t *err);
+                       const uint8_t *mask_pad, const float *scale_pad, float *q, int warps, cudaError_t *err);
 void ku3_free_maps(Ku3Maps *m);
 // entries of the padded element-scale copy (rows of round_up(nx, 4)) and bytes of
 // the padded constraint-bit copy (rows of round_up(nx+1, 16))
@@ -49,8 +49,9 @@ void ku3_padded_sizes(const Layout &L, long long *scale_entries, long long *mask
 // per-node constraint bits
 cudaError_t ku3_pad(const Layout &L, const float *s32, const uint8_t *mask, float *scale_pad, uint8_t *mask_pad,
                     cudaStream_t st);
-// the launch plan (28 x 15 node tiles, two CTAs per SM)
-KuLaunch ku3_plan(const Layout &L, int sms = 152);
+// the launch plan: tiles of 28 node columns and 2 warps - 1 node rows (warps 8 or
+// 7; 0 picks the one whose one-wave plan fills more CTA slots), two CTAs per SM
+KuLaunch ku3_plan(const Layout &L, int warps = 0, int sms = 152);
 // p = dinv r + beta p_prev, q = mask(K p), p.q -> S->alpha (ku_pcg's contract) with
 // `stages` (3 or 4) shared-memory stages
 cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,

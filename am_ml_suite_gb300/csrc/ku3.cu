@@ -100,9 +100,15 @@ bool encode(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, CUtensorMapDat
 }  // namespace
 
 Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const float *pb, const float *dinv,
-                       const uint8_t *mask_pad, const float *scale_pad, float *q, cudaError_t *err) {
-    using Sh = Ku3Shape<8, 4>;
+                       const uint8_t *mask_pad, const float *scale_pad, float *q, int warps, cudaError_t *err) {
     *err = cudaSuccess;
+    if (warps != 7 && warps != 8) {
+        *err = cudaErrorInvalidValue;
+        return nullptr;
+    }
+    // boxes of the tile shape (the node columns and the staged widths do not depend on warps)
+    using Sh = Ku3Shape<8, 4>;
+    const cuuint32_t BY = 2 * warps + 1, BYE = 2 * warps, TY = 2 * warps - 1;
     PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn(err);
     if (!fn) return nullptr;
     Ku3Maps *T = new (std::nothrow) Ku3Maps;
@@ -113,16 +119,16 @@ Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const f
     const cuuint64_t nx1 = L.nx + 1, ny1 = L.ny + 1, nz1 = L.nz + 1;
     const cuuint64_t vdims[4] = {nx1, ny1, nz1, 3};
     const cuuint64_t vstr[3] = {(cuuint64_t)L.sx * 4, (cuuint64_t)L.sxy * 4, (cuuint64_t)L.cs * 4};
-    const cuuint32_t vload[4] = {Sh::BX, Sh::BY, 1, 3};
-    const cuuint32_t vstore[4] = {Sh::TX, Sh::TY, 1, 1};
+    const cuuint32_t vload[4] = {Sh::BX, BY, 1, 3};
+    const cuuint32_t vstore[4] = {Sh::TX, TY, 1, 1};
     const cuuint64_t ndims[3] = {nx1, ny1, nz1};
-    const cuuint32_t dbox[3] = {Sh::BX, Sh::BY, 1};
+    const cuuint32_t dbox[3] = {Sh::BX, BY, 1};
     const long long sxm = round_up(L.nx + 1, 16), sxe = round_up(L.nx, 4);
     const cuuint64_t mstr[2] = {(cuuint64_t)sxm, (cuuint64_t)(sxm * (L.ny + 1))};
-    const cuuint32_t mbox[3] = {Sh::BXM, Sh::BY, 1};
+    const cuuint32_t mbox[3] = {Sh::BXM, BY, 1};
     const cuuint64_t edims[3] = {(cuuint64_t)L.nx, (cuuint64_t)L.ny, (cuuint64_t)L.nz};
     const cuuint64_t estr[2] = {(cuuint64_t)sxe * 4, (cuuint64_t)(sxe * L.ny * 4)};
-    const cuuint32_t ebox[3] = {Sh::BX, Sh::BYE, 1};
+    const cuuint32_t ebox[3] = {Sh::BX, BYE, 1};
     const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const bool ok = encode(fn, &T->r, F, 4, r, vdims, vstr, vload) && encode(fn, &T->pa, F, 4, pa, vdims, vstr, vload) &&
                     encode(fn, &T->pb, F, 4, pb, vdims, vstr, vload) &&
@@ -142,27 +148,44 @@ Ku3Maps *ku3_make_maps(const Layout &L, const float *r, const float *pa, const f
 
 void ku3_free_maps(Ku3Maps *m) { delete m; }
 
-// One wave of tiles (every tile resident at once, the z chunks as long as that
-// allows) whenever it keeps at least 3/4 of the CTA slots busy, else the plan
-// that minimises waves x chunk height.  Measured on GB300: on the 256x128x128 grid
-// 3 chunks of 43 planes (270 tiles, one wave) take 68.8 us against 71.9 us for 10
-// chunks of 13 (900 tiles, three waves) -- each tile's pipeline fill and p.q
-// hand-off cost more than the idle slots -- and on 192x96x96 the one-wave plan is
-// the minimiser's choice already (6 chunks of 17 planes, 35.5 us; 9 or 13 planes
-// 40.7 / 41.6 us).
-KuLaunch ku3_plan(const Layout &L, int sms) {
-    using Sh = Ku3Shape<8, 4>;
-    const long long cols = (long long)((L.nx + Sh::TX) / Sh::TX) * ((L.ny + Sh::TY) / Sh::TY);
+// The launch plan for tiles of `warps` warps (2 warps - 1 node rows): one wave of
+// tiles (every tile resident at once, the z chunks as long as that allows)
+// whenever it keeps at least 3/4 of the CTA slots busy, else the plan that
+// minimises waves x chunk height.  Measured on GB300 (8-warp tiles): on the
+// 256x128x128 grid 3 chunks of 43 planes (270 tiles, one wave) take 68.8 us
+// against 71.9 us for 10 chunks of 13 (900 tiles, three waves) -- each tile's
+// pipeline fill and p.q hand-off cost more than the idle slots -- and on 192x96x96
+// the one-wave plan is the minimiser's choice already (6 chunks of 17 planes,
+// 35.5 us; 9 or 13 planes 40.7 / 41.6 us).
+static KuLaunch ku3_plan_w(const Layout &L, int warps, int sms, long long *one_wave_tiles) {
+    const int tx = Ku3Shape<8, 4>::TX, ty = 2 * warps - 1;
+    const long long cols = (long long)((L.nx + tx) / tx) * ((L.ny + ty) / ty);
     const long long slots = 2LL * sms;
     const int planes = L.nz + 1;
     int tz = 0;
+    *one_wave_tiles = 0;
     if (cols <= slots) {
         const int chunks = (int)std::min<long long>(slots / cols, std::max(1, planes / 4));
         const int t = (planes + chunks - 1) / chunks;
         const long long tiles = cols * ((planes + t - 1) / t);
-        if (4 * tiles >= 3 * slots) tz = t;
+        if (4 * tiles >= 3 * slots) {
+            tz = t;
+            *one_wave_tiles = tiles;
+        }
     }
-    return ku_plan_shape(L, Sh::TX, Sh::TY, 8, 2, tz, sms);
+    return ku_plan_shape(L, tx, ty, warps, 2, tz, sms);
+}
+// warps 0: 7-warp tiles (13 node rows) when their one-wave plan keeps more CTA
+// slots busy than the 8-warp tiles' (15 rows) does, else 8-warp tiles.  On
+// 256x128x128 the 7-warp plan is 300 tiles against 270: 63.5 against 69.5 us; on
+// 192x96x96 it is 280 against 294: 36.7 against 35.6 us (GB300, 30 launches each).
+KuLaunch ku3_plan(const Layout &L, int warps, int sms) {
+    long long t8 = 0, t7 = 0;
+    const KuLaunch k8 = ku3_plan_w(L, 8, sms, &t8);
+    if (warps == 8) return k8;
+    const KuLaunch k7 = ku3_plan_w(L, 7, sms, &t7);
+    if (warps == 7) return k7;
+    return t7 > t8 ? k7 : k8;
 }
 
 cudaError_t ku3_init_attributes() {
@@ -171,6 +194,9 @@ cudaError_t ku3_init_attributes() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(ku3_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  Ku3Shape<8, 4>::SMEM_ALLOC);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ku3_kernel<7, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Ku3Shape<7, 4>::SMEM_ALLOC);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(ku3b_kernel<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  Ku3bShape<8, 4>::SMEM_ALLOC);
@@ -182,7 +208,8 @@ cudaError_t ku3_init_attributes() {
 
 cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const Modal<float> &M, double *partial,
                     Scalars *S, int stages, cudaStream_t st) {
-    if (!T || K.warps != 8 || K.tx != Ku3Shape<8, 4>::TX || K.ty != Ku3Shape<8, 4>::TY) return cudaErrorInvalidValue;
+    if (!T || (K.warps != 8 && K.warps != 7) || K.tx != Ku3Shape<8, 4>::TX || K.ty != 2 * K.warps - 1)
+        return cudaErrorInvalidValue;
     Ku3Args a{};
     a.M = M;
     a.partial = partial;
@@ -191,9 +218,11 @@ cudaError_t ku3_pcg(const Ku3Maps *T, const KuLaunch &K, const Layout &L, const 
     a.tiles_y = K.tiles_y;
     a.tz = K.tz;
     a.nz = L.nz;
-    if (stages == 4)
+    if (K.warps == 7 && stages == 4)
+        ku3_kernel<7, 4><<<K.ntiles(), 224, Ku3Shape<7, 4>::SMEM_ALLOC, st>>>(*T, a);
+    else if (K.warps == 8 && stages == 4)
         ku3_kernel<8, 4><<<K.ntiles(), 256, Ku3Shape<8, 4>::SMEM_ALLOC, st>>>(*T, a);
-    else if (stages == 3)
+    else if (K.warps == 8 && stages == 3)
         ku3_kernel<8, 3><<<K.ntiles(), 256, Ku3Shape<8, 3>::SMEM_ALLOC, st>>>(*T, a);
     else
         return cudaErrorInvalidValue;

@@ -758,7 +758,10 @@ def main():
     # ku3: reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B),
     # scale (4 B per element); writes p, q (3 x 4 B each per node)
     alg_bytes = 53 * nodes + 4 * nel
-    ku_roof = {"bound": "hbm", "kernel": "ku3_kernel<8,4> (tensor-copy staged p-update + FP32 K*p + p.q)",
+    kplan = keep_p.ku_plan()
+    ku_roof = {"bound": "hbm",
+               "kernel": (f"ku3_kernel<{kplan['warps']},4> (tensor-copy staged p-update + FP32 K*p + p.q; "
+                          f"{kplan['tiles']} tiles of 28 x {2 * kplan['warps'] - 1} nodes x {kplan['z_chunk']} planes)"),
                "achieved": alg_bytes / (ku_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                "frac": alg_bytes / (ku_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
                "traffic": ku_traffic_per_launch(W, nodes, nel), "algorithmic_bytes": alg_bytes,

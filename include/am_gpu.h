@@ -285,7 +285,7 @@ long long am_launch_count(void);
  * barrier per plane), 12 the same kernel, 13 the staged kernel without a
  * CTA-wide barrier per plane (4 stages), 1 the FP64
  * residual K*u, 2 the FP32 PCG vector update, 3 the plain FP32 K*u, 4 the
- * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages,
+ * register-direct FP32 PCG K*u it replaced, 5 the staged kernel with 3 stages (8-warp tiles),
  * 14 the double-float residual of the mixed solvers (1 is its FP64 form),
  * 6 / 7 the FP32 PCG vector update of an even (residual only) / odd (residual
  * and folded iterate) iteration, 8 the C++ cone sensitivity filter
@@ -383,6 +383,18 @@ am_status am_problem_set_preconditioner(am_problem *p, am_precond *m);
  * results); no reference counterpart (Eigen's CG loop runs on the host,
  * linear_solver.cpp:136-155). */
 am_status am_problem_set_device_loop(am_problem *p, int on);
+
+/* The tile height of the FP32 inner PCG's staged K*u (tiles of 28 node columns and
+ * 2 warps - 1 node rows).  warps 0 (the default): 7 warps where the 7-warp tiles'
+ * one-wave plan keeps more CTA slots busy than the 8-warp tiles' (the 256x128x128
+ * cantilever: 300 tiles against 270), else 8; 7 or 8 pins it.  Every choice gives
+ * the same p and q; p.q is summed over different tiles.  The barrier-free
+ * measurement kernel (am_ku_pcg_step impl 4, am_bench_kernel 13) needs 8-warp tiles.
+ * No reference counterpart. */
+am_status am_problem_set_ku_plan(am_problem *p, int warps);
+/* The staged K*u's plan in use: warps per tile, tiles per launch, node planes per
+ * z chunk (each nullable). */
+am_status am_problem_get_ku_plan(am_problem *p, int *warps, int *tiles, int *z_chunk);
 
 /* The arithmetic of the residuals r = mask(f - K u) (with the element energies)
  * that the mixed-precision solvers (AM_PREC_MIXED) recompute at every residual

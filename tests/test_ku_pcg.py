@@ -10,7 +10,13 @@ diagonal and mask zeroing the fixed and orphan DOFs.  Checked against
     FP32, the nodes in double-float);
   * the staged kernel without a CTA-wide barrier per plane (impl 4) and the
     register-direct kernel (impl 2): p and q bitwise equal, p.q equal to the
-    impl-4 kernel's.
+    impl-4 kernel's;
+  * the staged kernel on 7-warp tiles (13 node rows, am_problem_set_ku_plan): p
+    bitwise equal; q within one FP32 rounding of each node's sum (a node's
+    contributions from the element rows above and below it are added in an order
+    that depends on its row within a warp, so nodes whose row position differs
+    between 13- and 15-row tiles round differently), exactly 0 on masked DOFs; p.q
+    within rounding.
 Shapes span several 28-column, 15-row and z-chunk tiles, odd remainders and a
 single element.
 """
@@ -87,6 +93,35 @@ def test_pcg_step_matches_oracle_and_previous_kernel(shape, beta):
 
     assert abs(pq3 - p3 @ q3) <= 1e-6 * (np.abs(p3) @ np.abs(q3))
     assert abs(pq3 - pq2) <= 1e-6 * (np.abs(p3) @ np.abs(q3))
+
+    p.set_ku_plan(7)
+    assert p.ku_plan()["warps"] == 7
+    p7, q7, pq7 = p.ku_pcg_step(cfg, rho, r, p_prev, beta, impl=3)
+    assert np.array_equal(p7, p2)
+    assert np.all(q7[mask] == 0.0)
+    assert np.abs(q7 - q2).max() <= 1e-6 * np.abs(q2).max()
+    assert np.abs(q7 - q_ref).max() <= 2e-6 * np.abs(q_ref).max()
+    assert abs(pq7 - pq3) <= 1e-6 * (np.abs(p3) @ np.abs(q3))
+    p.set_ku_plan(0)
+    assert p.ku_plan()["warps"] == 8  # small grids keep the 8-warp tiles
+
+
+def test_ku_plan_tile_height_by_grid():
+    """The staged K*u's plan: one wave of tiles with the longest z chunks, on the
+    tile height whose one wave fills more CTA slots -- 7-warp tiles on the
+    256x128x128 cantilever (10 x 10 columns x 3 chunks of 43 planes = 300 tiles),
+    8-warp tiles on the 192x96x96 bracket (7 x 7 x 6 chunks of 17 = 294); the plan
+    is computed when the problem is created, before any vector is allocated."""
+    p = nat.Problem((256, 128, 128))
+    assert p.ku_plan() == {"warps": 7, "tiles": 300, "z_chunk": 43}
+    p.set_ku_plan(8)
+    assert p.ku_plan() == {"warps": 8, "tiles": 270, "z_chunk": 43}
+    p.close()
+    p = nat.Problem((192, 96, 96))
+    assert p.ku_plan() == {"warps": 8, "tiles": 294, "z_chunk": 17}
+    with pytest.raises(nat.AmError):
+        p.set_ku_plan(6)
+    p.close()
 
 
 def test_pcg_step_rejects_bad_arguments():
