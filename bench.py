@@ -753,12 +753,12 @@ def main():
     res_ms, _ = keep_p.bench_kernel(1, reps=5, flush_l2=True)
     res_df_ms, _ = keep_p.bench_kernel(14, reps=5, flush_l2=True)
     upd_ms, upd_min = keep_p.bench_kernel(2, reps=20, flush_l2=True)
+    kplan = keep_p.ku_plan()
     keep_p.close()
     peak, peak_kind = measured_peaks()
     # ku3: reads p, r (3 x 4 B each per node), dinv (4 B), constraint bits (1 B),
     # scale (4 B per element); writes p, q (3 x 4 B each per node)
     alg_bytes = 53 * nodes + 4 * nel
-    kplan = keep_p.ku_plan()
     ku_roof = {"bound": "hbm",
                "kernel": (f"ku3_kernel<{kplan['warps']},4> (tensor-copy staged p-update + FP32 K*p + p.q; "
                           f"{kplan['tiles']} tiles of 28 x {2 * kplan['warps'] - 1} nodes x {kplan['z_chunk']} planes)"),
