@@ -30,3 +30,22 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_ku_traffic_uses_the_workload_capture():
+    """The K*u roofline's DRAM traffic: the committed ncu capture of the workload's
+    own grid where there is one (the cantilever and the bracket), else the largest
+    capture scaled by nodes; every capture names the command that made it."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    with open(os.path.join(ROOT, "profiles", "ku_pcg_fp32_traffic.json")) as f:
+        caps = json.load(f)["captures"]
+    for name, c in caps.items():
+        assert c["source"].startswith("ncu ") and "--clock-control none" in c["source"], name
+        assert c["dram_bytes_per_launch"] == c["dram_bytes_read"] + c["dram_bytes_write"] or \
+            abs(c["dram_bytes_per_launch"] - (c["dram_bytes_read"] + c["dram_bytes_write"])) < 1e3, name
+        assert bench.ku_traffic_per_launch(None, c["nodes"], c["elements"]) == c["dram_bytes_per_launch"]
+    big = max(caps.values(), key=lambda c: c["nodes"])
+    assert bench.ku_traffic_per_launch(None, big["nodes"] // 2, 1) == big["dram_bytes_per_launch"] * (
+        big["nodes"] // 2) / big["nodes"]
