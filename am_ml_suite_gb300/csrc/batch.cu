@@ -748,27 +748,33 @@ am_status am_batch_bench_ku(am_batch *B, int reps, double *avg_ms) {
         S.cnt_ku = 0;
         S.kerr = 0;
     }
+    // the timed launches; the events are destroyed and the solver state restored
+    // whether or not they succeed
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    BCK(cudaEventCreate(&e0));
-    BCK(cudaEventCreate(&e1));
     double tot = 0.0;
-    for (int r = 0; r < reps + 1; ++r) {  // the first launch warms up
-        BCK(cudaMemcpyAsync(B->S.p, run.data(), sizeof(Scalars) * B->n, cudaMemcpyHostToDevice, B->st));
-        BCK(cudaEventRecord(e0, B->st));
-        if (B->staged)
-            BCK(batch_ku3_pcg(B->k3items.p, B->k3, B->C.M32, B->st));
-        else
-            BCK(batch_pcg_ku(B->items_d.p, B->k2, B->k2b, B->C, B->warps, kSms * B->ctas, B->st));
-        BCK(cudaEventRecord(e1, B->st));
-        BCK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        BCK(cudaEventElapsedTime(&ms, e0, e1));
-        if (r > 0) tot += ms;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    auto timed = [&]() -> cudaError_t {
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        for (int r = 0; r < reps + 1 && e == cudaSuccess; ++r) {  // the first launch warms up
+            e = cudaMemcpyAsync(B->S.p, run.data(), sizeof(Scalars) * B->n, cudaMemcpyHostToDevice, B->st);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, B->st);
+            if (e == cudaSuccess)
+                e = B->staged ? batch_ku3_pcg(B->k3items.p, B->k3, B->C.M32, B->st)
+                              : batch_pcg_ku(B->items_d.p, B->k2, B->k2b, B->C, B->warps, kSms * B->ctas, B->st);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, B->st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) tot += ms;
+        }
+        return e;
+    };
+    const cudaError_t et = timed();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     BCK(cudaMemcpyAsync(B->S.p, saved.data(), sizeof(Scalars) * B->n, cudaMemcpyHostToDevice, B->st));
     BCK(cudaStreamSynchronize(B->st));
+    BCK(et);
     *avg_ms = tot / reps;
     return AM_OK;
 }
