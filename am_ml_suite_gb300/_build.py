@@ -38,7 +38,8 @@ def _sources():
 
 
 def _deps():
-    return _sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    return (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
+            glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 def up_to_date() -> bool:

@@ -22,6 +22,7 @@
 
 #include "../../include/am_gpu.h"
 #include "batch.cuh"
+#include "batch_axes.h"
 #include "host_util.h"
 #include "kernels.cuh"
 #include "ku3.cuh"
@@ -136,50 +137,6 @@ struct am_batch {
 namespace {
 
 int div_up_i(long long a, long long b) { return (int)((a + b - 1) / b); }
-
-// The axis order a problem is stored in.  The cube's element stiffness is the
-// same when the three axes and the displacement components are permuted together
-// (and the cone filter and OC step do not see axes), so each problem may keep its
-// grid in whichever axis order makes the batched K*u's tiles (28 node columns, as
-// the staged kernel's, x 15 node rows x all planes plus a halo plane) overhang it
-// least; the caller's order is restored at the boundary (loads, constraints,
-// densities).  Ties keep the caller's order.
-std::array<int, 3> best_axes(const int d[3]) {
-    static const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-    long long best = -1;
-    std::array<int, 3> out{0, 1, 2};
-    for (const auto &q : P) {
-        const long long slots = (long long)div_up_i(d[q[0]] + 1, 28) * 32 * div_up_i(d[q[1]] + 1, 15) * 16 *
-                                (d[q[2]] + 2);
-        if (best < 0 || slots < best) {
-            best = slots;
-            out = {q[0], q[1], q[2]};
-        }
-    }
-    return out;
-}
-
-// internal coordinates of the caller's (i, j, k) and the internal component of the
-// caller's component c
-inline void to_internal(const std::array<int, 3> &ax, const long long c3[3], long long q[3]) {
-    for (int a = 0; a < 3; ++a) q[a] = c3[ax[a]];
-}
-// the caller's index of internal element (ex, ey, ez): C order over the caller's
-// (nx, ny, nz) (z fastest) or x fastest, as the layout says
-inline long long host_element(const std::array<int, 3> &ax, const std::array<int, 3> &dm, int layout, long long ex,
-                              long long ey, long long ez) {
-    long long c3[3];
-    c3[ax[0]] = ex;
-    c3[ax[1]] = ey;
-    c3[ax[2]] = ez;
-    return layout == AM_LAYOUT_ZFASTEST ? (c3[0] * dm[1] + c3[1]) * dm[2] + c3[2]
-                                        : (c3[2] * dm[1] + c3[1]) * dm[0] + c3[0];
-}
-inline int internal_component(const std::array<int, 3> &ax, int c) {
-    for (int a = 0; a < 3; ++a)
-        if (ax[a] == c) return a;
-    return c;
-}
 
 am_status upload_worklist(am_batch *B, Pool<int2> &pool, WorkList &wl, const std::vector<int2> &w) {
     BCK(pool.alloc(w.size()));
@@ -886,7 +843,7 @@ am_status am_batch_simp_begin(am_batch *B, const am_simp_config *cfgs, const dou
             for (long long ey = 0; ey < L.ny; ++ey)
                 for (long long ex = 0; ex < L.nx; ++ex) {
                     const long long e = (ez * L.ny + ey) * L.nx + ex;
-                    const long long hidx = host_element(B->axes[p], B->dims[p], c.layout, ex, ey, ez);
+                    const long long hidx = host_element(B->axes[p], B->dims[p], c.layout == AM_LAYOUT_ZFASTEST, ex, ey, ez);
                     const double v = rho0 ? rho0[ho + hidx] : c.volume_fraction;
                     r0[eo + e] = v;
                     // design mask from the initial density (topology_optimizer.cpp:419-428)
@@ -1004,7 +961,7 @@ am_status am_batch_get_density(am_batch *B, double *rho_out) {
             for (long long ey = 0; ey < L.ny; ++ey)
                 for (long long ex = 0; ex < L.nx; ++ex) {
                     const long long e = (ez * L.ny + ey) * L.nx + ex;
-                    const long long hidx = host_element(B->axes[p], B->dims[p], B->cfg[p].layout, ex, ey, ez);
+                    const long long hidx = host_element(B->axes[p], B->dims[p], B->cfg[p].layout == AM_LAYOUT_ZFASTEST, ex, ey, ez);
                     rho_out[o + hidx] = r[eo + e];
                 }
         o += (size_t)L.nel;
